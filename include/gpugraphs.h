@@ -1,0 +1,192 @@
+/*
+ * gpugraphs.h — C ABI of libgpugraphs.so, the sm_103a (GB300) implementation of the
+ * semiring sparse kernels and graph algorithms of GPUGraphs.jl.
+ *
+ * Every entry point replaces one Julia method of the reference package; the citation
+ * beside each declaration is the reference interface it stands in for (paths are
+ * relative to the GPUGraphs.jl repository).
+ *
+ * Conventions
+ *  - Every call returns an int status (GG_OK == 0).  No exceptions cross the ABI.
+ *    gg_last_error() returns a thread-local message for the last failing call.
+ *  - Index arrays follow the reference: 1-based Int32 rowptr / colval / slice_ptr,
+ *    colval == -1 for SELL padding, 1-based vertex ids in BFS/SSSP.
+ *  - Vectors and dense matrices passed to compute calls are caller-owned DEVICE
+ *    pointers.  Matrix handles (gg_mat) own their device storage until
+ *    gg_mat_destroy().
+ *  - Work is enqueued on the context's stream (gg_set_stream; default: the legacy
+ *    default stream) and is asynchronous unless stated otherwise, like the
+ *    reference's KernelAbstractions launches (callers synchronize before reading).
+ *  - A context may be used from one host thread at a time.
+ */
+#ifndef GPUGRAPHS_H
+#define GPUGRAPHS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (Julia exception the reference throws in brackets) ---- */
+enum {
+  GG_OK = 0,
+  GG_ERR_DIMENSION = 1,     /* DimensionMismatch  (src/spmv/CSR.jl:374-379) */
+  GG_ERR_ARGUMENT = 2,      /* ArgumentError      (src/storage/CSR.jl:48-63) */
+  GG_ERR_TYPE = 3,          /* ArgumentError "Result type must be able to hold ..." (src/spmv/CSR.jl:381-387) */
+  GG_ERR_UNSUPPORTED = 4,   /* no neutral element / no method for this operator and type (src/algebra.jl:10-11) */
+  GG_ERR_OOM = 5,           /* device allocation failed */
+  GG_ERR_CUDA = 6,          /* any other CUDA runtime error */
+  GG_ERR_TIMEOUT = 7,       /* a bounded device-side wait ran out */
+  GG_ERR_BOUNDS = 8,        /* BoundsError (source vertex outside 1..n) */
+  GG_ERR_ASSERTION = 9,     /* AssertionError (src/spmm/CSR.jl:131-133) */
+  GG_ERR_NOT_CONVERGED = 10 /* Bellman-Ford still improving after n rounds (negative cycle) */
+};
+
+/* ---- element types, numbered in Julia's promotion order (promote = max) ---- */
+enum {
+  GG_BOOL = 1,    /* Julia Bool, one byte holding 0 or 1 */
+  GG_INT32 = 2,
+  GG_INT64 = 3,
+  GG_FLOAT32 = 4,
+  GG_FLOAT64 = 5
+};
+
+/* ---- semiring operators: the GPUGraphs_* functions of src/algebra.jl:31-111 ---- */
+enum {
+  GG_OP_FIRST = 1,     /* GPUGraphs_first    x                        algebra.jl:31  */
+  GG_OP_SECOND = 2,    /* GPUGraphs_second   y                        algebra.jl:32  */
+  GG_OP_ANY = 3,       /* GPUGraphs_any      max(x,y), neutral 0      algebra.jl:35  */
+  GG_OP_PAIR = 4,      /* GPUGraphs_pair     y != 0 ? 1 : 0           algebra.jl:40  */
+  GG_OP_ADD = 5,       /* GPUGraphs_add      x + y                    algebra.jl:43  */
+  GG_OP_SAFE_ADD = 6,  /* GPUGraphs_safe_add typemax-saturating +     algebra.jl:47  */
+  GG_OP_MINUS = 7,     /* GPUGraphs_minus    x - y                    algebra.jl:52  */
+  GG_OP_RMINUS = 8,    /* GPUGraphs_rminus   y - x                    algebra.jl:53  */
+  GG_OP_MUL = 9,       /* GPUGraphs_mul      x * y                    algebra.jl:55  */
+  GG_OP_MIN = 10,      /* GPUGraphs_min                               algebra.jl:65  */
+  GG_OP_MAX = 11,      /* GPUGraphs_max                               algebra.jl:68  */
+  GG_OP_LOR = 12,      /* GPUGraphs_lor      x | y (Bool monoid)      algebra.jl:77  */
+  GG_OP_LAND = 13,     /* GPUGraphs_land     x & y (Bool monoid)      algebra.jl:80  */
+  GG_OP_BOR = 14,      /* GPUGraphs_bor      x | y                    algebra.jl:95  */
+  GG_OP_BAND = 15,     /* GPUGraphs_band     x & y                    algebra.jl:98  */
+  GG_OP_BXOR = 16,     /* GPUGraphs_bxor     x xor y                  algebra.jl:102 */
+  GG_OP_FIRSTI = 17,   /* GPUGraphs_firsti   A_i (row)                algebra.jl:106 */
+  GG_OP_FIRSTJ = 18,   /* GPUGraphs_firstj   A_j (column of A)        algebra.jl:107 */
+  GG_OP_SECONDI = 19,  /* GPUGraphs_secondi  B_i * y                  algebra.jl:109 */
+  GG_OP_SECONDJ = 20   /* GPUGraphs_secondj  B_j (column of B)        algebra.jl:111 */
+};
+
+enum { GG_FMT_CSR = 1, GG_FMT_SELL = 2 };
+
+/* dense layouts for gg_spmm: Julia matrices are column-major */
+enum { GG_COL_MAJOR = 0, GG_ROW_MAJOR = 1 };
+
+/* BFS parent rules (which frontier in-neighbour becomes the parent) */
+enum {
+  GG_PARENT_FORMAT_DEFAULT = 0, /* CSR: FIRST_IN_ROW, SELL: MAX_INDEX, as the reference */
+  GG_PARENT_FIRST_IN_ROW = 1,   /* first frontier column in storage order (src/spmv/CSR.jl:147-171) */
+  GG_PARENT_MAX_INDEX = 2       /* largest frontier column index (src/algebra.jl:35 via src/spmv/SELL.jl:100-133) */
+};
+
+typedef struct gg_ctx gg_ctx; /* device, stream, scratch arena */
+typedef struct gg_mat gg_mat; /* a CSR or SELL-C-sigma matrix resident on the device */
+
+/* ---- library / context ---------------------------------------------------- */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* gg_last_error(void);
+
+/* Library version string. */
+const char* gg_version(void);
+
+/* Replaces KernelAbstractions backend selection (test/spmv.jl:1-8): binds device `device`. */
+int gg_init(int device, gg_ctx** out);
+
+/* Frees the context and its scratch arena (matrices must be destroyed separately). */
+int gg_destroy(gg_ctx* ctx);
+
+/* Enqueue subsequent work on `stream` (a cudaStream_t; NULL = legacy default stream). */
+int gg_set_stream(gg_ctx* ctx, void* stream);
+
+/* Replaces KernelAbstractions.synchronize(backend) (test/spmv.jl:25). */
+int gg_stream_sync(gg_ctx* ctx);
+
+/* ---- storage ------------------------------------------------------------------ */
+
+/*
+ * Replaces SparseGPUMatrixCSR(m, n, rowptr, colval, nzval, backend)
+ * (src/storage/CSR.jl:34-92).  rowptr (m+1), colval (nnz) are 1-based Int32,
+ * nzval (nnz) has element type `dtype`.  on_device != 0: the three pointers are
+ * device pointers, else host pointers.  The arrays are copied.  Validation follows
+ * src/storage/CSR.jl:48-63 (rowptr[1] == 1, rowptr[m+1] == nnz+1, 1 <= colval <= n)
+ * and also requires rowptr to be non-decreasing; violations return GG_ERR_ARGUMENT.
+ */
+int gg_csr_create(gg_ctx* ctx, int64_t m, int64_t n, int64_t nnz, const int32_t* rowptr,
+                  const int32_t* colval, const void* nzval, int dtype, int on_device,
+                  gg_mat** out);
+
+/*
+ * Replaces SparseGPUMatrixSELL(transpose(A_csc), backend, slice_size)
+ * (src/storage/SELL.jl:99-181), built on the device from a CSR handle.
+ * slice_size C is clamped to m like the reference (SELL.jl:108).  sigma == 1 gives
+ * the reference layout exactly (identity perm, test/structs.jl:188-190); sigma > 1
+ * sorts rows by decreasing length inside windows of sigma rows (SELL-C-sigma) and
+ * records the permutation.
+ */
+int gg_sell_create(gg_ctx* ctx, const gg_mat* csr, int64_t slice_size, int64_t sigma,
+                   gg_mat** out);
+
+/* Frees a matrix handle and its device storage. */
+int gg_mat_destroy(gg_mat* A);
+
+/*
+ * Replaces size(A), nnz(A) and the SELL fields m, n, slice_size, nslices, n_stored
+ * (src/storage/CSR.jl:142-184, src/storage/SELL.jl:9-16,193-242).  Any out pointer
+ * may be NULL.
+ */
+int gg_mat_info(const gg_mat* A, int* format, int64_t* m, int64_t* n, int64_t* nnz,
+                int* dtype, int64_t* n_stored, int64_t* slice_size, int64_t* nslices);
+
+/*
+ * Device pointers of the fields A.rowptr / A.colval / A.nzval (CSR) or
+ * A.slice_ptr / A.colval / A.nzval / perm (SELL; perm is 1-based Int32, length m).
+ * The memory stays owned by the handle.  Any out pointer may be NULL.
+ */
+int gg_mat_arrays(const gg_mat* A, void** ptr, void** colval, void** nzval, void** perm);
+
+/* ---- semiring kernels -------------------------------------------------------- */
+
+/*
+ * Replaces gpu_spmv!(C, A, B; mul, add, accum, range, mask)
+ * (src/spmv/CSR.jl:2-29 and src/spmv/SELL.jl:2-29):
+ *   y[r] = accum(y[r], add_k mul(A[r,k], x[k], r, k, k, 1))   for every selected row r
+ * Rows are selected by the optional dense mask (mask[r] != 0; NULL = all rows) and the
+ * optional 1-based inclusive row range [range_lo, range_hi] (range_lo == 0: no range).
+ * Unselected rows are not written.  With add == GG_OP_ANY on CSR and a mask, the
+ * first stored column (storage order) whose x is nonzero is taken, as
+ * any_dense_masked_csr_spmv_kernel! does (src/spmv/CSR.jl:147-171), and rows without
+ * such a column are not written.  Checks of _validate_args (src/spmv/CSR.jl:358-408)
+ * return GG_ERR_DIMENSION / GG_ERR_TYPE.
+ */
+int gg_spmv(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* y, int y_dtype,
+            int64_t y_len, const void* x, int x_dtype, int64_t x_len, const void* mask,
+            int mask_dtype, int64_t mask_len, int64_t range_lo, int64_t range_hi);
+
+/*
+ * Replaces gpu_spmm!(C, A, B; mul, add, accum, mask, range)
+ * (src/spmm/CSR.jl:111-204, src/spmm/SELL.jl:84-124):
+ *   C[r,j] = accum(C[r,j], add_k mul(A[r,k], B[k,j], r, k, k, j))
+ * B is b_rows x k, C is c_rows x k, both in `layout` with leading dimensions ldb/ldc
+ * (elements).  Mask / range select rows as in gg_spmv.  Shape checks return
+ * GG_ERR_ASSERTION like the reference's @assert.
+ */
+int gg_spmm(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* C, int c_dtype,
+            int64_t c_rows, int64_t ldc, const void* B, int b_dtype, int64_t b_rows,
+            int64_t ldb, int64_t k, int layout, const void* mask, int mask_dtype,
+            int64_t mask_len, int64_t range_lo, int64_t range_hi);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUGRAPHS_H */
