@@ -1,0 +1,374 @@
+// gg_common.cuh -- shared definitions of libgpugraphs: handles, error reporting,
+// element types and the device-side semantics of the GPUGraphs.jl operators
+// (src/algebra.jl), evaluated exactly as Julia does: Int32/Int64 wrap around,
+// Float32 operations round once each (no FMA contraction), min/max propagate NaN
+// and order -0.0 below +0.0, Bool is a 0/1 byte.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/gpugraphs.h"
+
+// ---------------------------------------------------------------------------------
+// error reporting (thread-local message behind gg_last_error)
+// ---------------------------------------------------------------------------------
+namespace gg {
+
+int set_error(int code, const char* fmt, ...);
+int cuda_error(cudaError_t e, const char* what);
+
+#define GG_CUDA(call)                                   \
+  do {                                                  \
+    cudaError_t _e = (call);                            \
+    if (_e != cudaSuccess) return gg::cuda_error(_e, #call); \
+  } while (0)
+
+#define GG_CHECK(call)           \
+  do {                           \
+    int _rc = (call);            \
+    if (_rc != GG_OK) return _rc; \
+  } while (0)
+
+// ---------------------------------------------------------------------------------
+// element types
+// ---------------------------------------------------------------------------------
+template <int TC> struct CType;
+template <> struct CType<GG_BOOL> { typedef uint8_t T; };
+template <> struct CType<GG_INT32> { typedef int32_t T; };
+template <> struct CType<GG_INT64> { typedef int64_t T; };
+template <> struct CType<GG_FLOAT32> { typedef float T; };
+template <> struct CType<GG_FLOAT64> { typedef double T; };
+
+inline int dtype_size(int t) {
+  switch (t) {
+    case GG_BOOL: return 1;
+    case GG_INT32: return 4;
+    case GG_FLOAT32: return 4;
+    case GG_INT64: return 8;
+    case GG_FLOAT64: return 8;
+  }
+  return 0;
+}
+inline bool dtype_valid(int t) { return t >= GG_BOOL && t <= GG_FLOAT64; }
+__host__ __device__ inline bool dtype_is_float(int t) { return t == GG_FLOAT32 || t == GG_FLOAT64; }
+
+// A value read in its own element type: integers (and Bool) in i, floats in d
+// (every Float32 is exact in a double).
+struct Raw {
+  int64_t i;
+  double d;
+};
+
+__device__ __forceinline__ Raw load_raw(const void* p, int t, int64_t k) {
+  Raw r;
+  r.i = 0;
+  r.d = 0.0;
+  switch (t) {
+    case GG_BOOL: r.i = static_cast<const uint8_t*>(p)[k] != 0; break;
+    case GG_INT32: r.i = static_cast<const int32_t*>(p)[k]; break;
+    case GG_INT64: r.i = static_cast<const int64_t*>(p)[k]; break;
+    case GG_FLOAT32: r.d = static_cast<const float*>(p)[k]; break;
+    default: r.d = static_cast<const double*>(p)[k]; break;
+  }
+  return r;
+}
+
+__device__ __forceinline__ bool raw_is_zero(const Raw& r, int t) {
+  return dtype_is_float(t) ? (r.d == 0.0) : (r.i == 0);
+}
+
+// Julia convert from a raw value of type t into compute type TC.
+template <int TC>
+__device__ __forceinline__ typename CType<TC>::T raw_to(const Raw& r, int t) {
+  typedef typename CType<TC>::T T;
+  if (!dtype_is_float(t)) {
+    if (TC == GG_BOOL) return static_cast<T>(r.i != 0);
+    if (TC == GG_INT32) return static_cast<T>(static_cast<int32_t>(static_cast<uint32_t>(r.i)));
+    return static_cast<T>(r.i);
+  }
+  if (TC == GG_FLOAT32) return static_cast<T>(static_cast<float>(r.d));
+  if (TC == GG_BOOL) return static_cast<T>(r.d != 0.0);
+  return static_cast<T>(r.d);
+}
+
+// Store v (compute type TC) into an array of element type t.  Float -> integer
+// conversion truncates (Julia would throw InexactError for non-integral values).
+template <int TC>
+__device__ __forceinline__ void store_as(void* p, int t, int64_t k, typename CType<TC>::T v) {
+  switch (t) {
+    case GG_BOOL: static_cast<uint8_t*>(p)[k] = (v != 0) ? 1 : 0; break;
+    case GG_INT32:
+      static_cast<int32_t*>(p)[k] =
+          dtype_is_float(TC) ? static_cast<int32_t>(v)
+                             : static_cast<int32_t>(static_cast<uint32_t>(static_cast<int64_t>(v)));
+      break;
+    case GG_INT64: static_cast<int64_t*>(p)[k] = static_cast<int64_t>(v); break;
+    case GG_FLOAT32: static_cast<float*>(p)[k] = static_cast<float>(v); break;
+    default: static_cast<double*>(p)[k] = static_cast<double>(v); break;
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// scalar semantics of src/algebra.jl
+// ---------------------------------------------------------------------------------
+template <typename T> struct Lim;
+template <> struct Lim<uint8_t> {
+  __host__ __device__ static uint8_t max() { return 1; }
+  __host__ __device__ static uint8_t min() { return 0; }
+};
+template <> struct Lim<int32_t> {
+  __host__ __device__ static int32_t max() { return INT32_MAX; }
+  __host__ __device__ static int32_t min() { return INT32_MIN; }
+};
+template <> struct Lim<int64_t> {
+  __host__ __device__ static int64_t max() { return INT64_MAX; }
+  __host__ __device__ static int64_t min() { return INT64_MIN; }
+};
+template <> struct Lim<float> {
+  __host__ __device__ static float max() { return __builtin_huge_valf(); }
+  __host__ __device__ static float min() { return -__builtin_huge_valf(); }
+};
+template <> struct Lim<double> {
+  __host__ __device__ static double max() { return __builtin_huge_val(); }
+  __host__ __device__ static double min() { return -__builtin_huge_val(); }
+};
+
+// Julia max / min (base/math.jl): NaN if either is NaN, -0.0 < +0.0
+template <typename T> __device__ __forceinline__ T jl_max(T x, T y) { return x > y ? x : y; }
+template <typename T> __device__ __forceinline__ T jl_min(T x, T y) { return x < y ? x : y; }
+template <> __device__ __forceinline__ float jl_max<float>(float x, float y) {
+  if (x != x || y != y) return __int_as_float(0x7fc00000);
+  if (x == y) return signbit(x) ? y : x;
+  return x > y ? x : y;
+}
+template <> __device__ __forceinline__ float jl_min<float>(float x, float y) {
+  if (x != x || y != y) return __int_as_float(0x7fc00000);
+  if (x == y) return signbit(x) ? x : y;
+  return x < y ? x : y;
+}
+template <> __device__ __forceinline__ double jl_max<double>(double x, double y) {
+  if (x != x || y != y) return __longlong_as_double(0x7ff8000000000000LL);
+  if (x == y) return signbit(x) ? y : x;
+  return x > y ? x : y;
+}
+template <> __device__ __forceinline__ double jl_min<double>(double x, double y) {
+  if (x != x || y != y) return __longlong_as_double(0x7ff8000000000000LL);
+  if (x == y) return signbit(x) ? x : y;
+  return x < y ? x : y;
+}
+
+// wrapping integer arithmetic; floats round once per operation
+__device__ __forceinline__ uint8_t w_add(uint8_t x, uint8_t y) { return (x + y) & 1; }
+__device__ __forceinline__ int32_t w_add(int32_t x, int32_t y) {
+  return static_cast<int32_t>(static_cast<uint32_t>(x) + static_cast<uint32_t>(y));
+}
+__device__ __forceinline__ int64_t w_add(int64_t x, int64_t y) {
+  return static_cast<int64_t>(static_cast<uint64_t>(x) + static_cast<uint64_t>(y));
+}
+__device__ __forceinline__ float w_add(float x, float y) { return __fadd_rn(x, y); }
+__device__ __forceinline__ double w_add(double x, double y) { return __dadd_rn(x, y); }
+
+__device__ __forceinline__ uint8_t w_sub(uint8_t x, uint8_t y) { return (x - y) & 1; }
+__device__ __forceinline__ int32_t w_sub(int32_t x, int32_t y) {
+  return static_cast<int32_t>(static_cast<uint32_t>(x) - static_cast<uint32_t>(y));
+}
+__device__ __forceinline__ int64_t w_sub(int64_t x, int64_t y) {
+  return static_cast<int64_t>(static_cast<uint64_t>(x) - static_cast<uint64_t>(y));
+}
+__device__ __forceinline__ float w_sub(float x, float y) { return __fsub_rn(x, y); }
+__device__ __forceinline__ double w_sub(double x, double y) { return __dsub_rn(x, y); }
+
+__device__ __forceinline__ uint8_t w_mul(uint8_t x, uint8_t y) { return x & y; }
+__device__ __forceinline__ int32_t w_mul(int32_t x, int32_t y) {
+  return static_cast<int32_t>(static_cast<uint32_t>(x) * static_cast<uint32_t>(y));
+}
+__device__ __forceinline__ int64_t w_mul(int64_t x, int64_t y) {
+  return static_cast<int64_t>(static_cast<uint64_t>(x) * static_cast<uint64_t>(y));
+}
+__device__ __forceinline__ float w_mul(float x, float y) { return __fmul_rn(x, y); }
+__device__ __forceinline__ double w_mul(double x, double y) { return __dmul_rn(x, y); }
+
+template <typename T> __device__ __forceinline__ T bit_or(T x, T y) { return x | y; }
+template <typename T> __device__ __forceinline__ T bit_and(T x, T y) { return x & y; }
+template <typename T> __device__ __forceinline__ T bit_xor(T x, T y) { return x ^ y; }
+template <> __device__ __forceinline__ float bit_or<float>(float x, float) { return x; }
+template <> __device__ __forceinline__ float bit_and<float>(float x, float) { return x; }
+template <> __device__ __forceinline__ float bit_xor<float>(float x, float) { return x; }
+template <> __device__ __forceinline__ double bit_or<double>(double x, double) { return x; }
+template <> __device__ __forceinline__ double bit_and<double>(double x, double) { return x; }
+template <> __device__ __forceinline__ double bit_xor<double>(double x, double) { return x; }
+
+// GPUGraphs_safe_add (src/algebra.jl:47-48) in one type
+template <typename T> __device__ __forceinline__ T safe_add(T x, T y) {
+  T mx = jl_max<T>(x, y);
+  if (mx == Lim<T>::max()) return Lim<T>::max();
+  return w_add(x, y);
+}
+
+// Evaluate operator `op` on (x, y) already in compute type TC.  Index operators
+// receive the row / column ids of the reference kernels: A_i = row (Int64), A_j =
+// column of A (Int32), B_i = column of A (Int32), B_j = column of B (Int64).
+// For GPUGraphs_secondi the product B_i * y is taken in promote_type(Int32, typeof(y))
+// before conversion, so it needs the raw y and its type.
+template <int TC>
+__device__ __forceinline__ typename CType<TC>::T apply_op(int op, typename CType<TC>::T x,
+                                                          typename CType<TC>::T y, const Raw& yraw,
+                                                          int ty_raw, int64_t ai, int64_t aj,
+                                                          int64_t bi, int64_t bj) {
+  typedef typename CType<TC>::T T;
+  switch (op) {
+    case GG_OP_FIRST: return x;
+    case GG_OP_SECOND: return y;
+    case GG_OP_ANY: return jl_max<T>(x, y);
+    case GG_OP_PAIR: return (y != T(0)) ? T(1) : T(0);
+    case GG_OP_ADD: return w_add(x, y);
+    case GG_OP_SAFE_ADD: return safe_add<T>(x, y);
+    case GG_OP_MINUS: return w_sub(x, y);
+    case GG_OP_RMINUS: return w_sub(y, x);
+    case GG_OP_MUL: return w_mul(x, y);
+    case GG_OP_MIN: return jl_min<T>(x, y);
+    case GG_OP_MAX: return jl_max<T>(x, y);
+    case GG_OP_LOR:
+    case GG_OP_BOR: return bit_or<T>(x, y);
+    case GG_OP_LAND:
+    case GG_OP_BAND: return bit_and<T>(x, y);
+    case GG_OP_BXOR: return bit_xor<T>(x, y);
+    case GG_OP_FIRSTI: { Raw r; r.i = ai; r.d = 0; return raw_to<TC>(r, GG_INT64); }
+    case GG_OP_FIRSTJ: { Raw r; r.i = aj; r.d = 0; return raw_to<TC>(r, GG_INT32); }
+    case GG_OP_SECONDJ: { Raw r; r.i = bj; r.d = 0; return raw_to<TC>(r, GG_INT64); }
+    case GG_OP_SECONDI: {
+      Raw p;
+      p.i = 0;
+      p.d = 0;
+      if (ty_raw == GG_FLOAT32) {
+        p.d = __fmul_rn(static_cast<float>(static_cast<int32_t>(bi)), static_cast<float>(yraw.d));
+        return raw_to<TC>(p, GG_FLOAT32);
+      }
+      if (ty_raw == GG_FLOAT64) {
+        p.d = __dmul_rn(static_cast<double>(static_cast<int32_t>(bi)), yraw.d);
+        return raw_to<TC>(p, GG_FLOAT64);
+      }
+      if (ty_raw == GG_INT64) {
+        p.i = w_mul(static_cast<int64_t>(static_cast<int32_t>(bi)), yraw.i);
+        return raw_to<TC>(p, GG_INT64);
+      }
+      p.i = w_mul(static_cast<int32_t>(bi), static_cast<int32_t>(yraw.i));
+      return raw_to<TC>(p, GG_INT32);
+    }
+  }
+  return x;
+}
+
+// monoid_neutral / monoid_absorb (src/algebra.jl:10-100) for the add operator
+template <typename T> __host__ __device__ inline T all_ones() { return static_cast<T>(-1); }
+template <> __host__ __device__ inline uint8_t all_ones<uint8_t>() { return 1; }
+
+template <typename T> __host__ __device__ inline T neutral_of(int add) {
+  switch (add) {
+    case GG_OP_MUL: return T(1);
+    case GG_OP_MIN: return Lim<T>::max();
+    case GG_OP_MAX: return Lim<T>::min();
+    case GG_OP_BAND:
+    case GG_OP_LAND: return all_ones<T>();
+    default: return T(0);  // add, safe_add, any, bor, lor
+  }
+}
+
+// returns false when the monoid has no absorbing value (GPUGraphs_any)
+template <typename T> __host__ __device__ inline bool absorb_of(int add, T* out) {
+  switch (add) {
+    case GG_OP_ADD:
+    case GG_OP_SAFE_ADD:
+    case GG_OP_MAX: *out = Lim<T>::max(); return true;
+    case GG_OP_MUL: *out = T(0); return true;
+    case GG_OP_MIN: *out = Lim<T>::min(); return true;
+    case GG_OP_BOR:
+    case GG_OP_LOR: *out = all_ones<T>(); return true;
+    case GG_OP_BAND:
+    case GG_OP_LAND: *out = T(0); return true;
+  }
+  return false;
+}
+
+// warp shuffle that also handles the one-byte Bool type
+template <typename T> __device__ __forceinline__ T shfl_xor(T v, int off, int width) {
+  return __shfl_xor_sync(0xffffffffu, v, off, width);
+}
+template <> __device__ __forceinline__ uint8_t shfl_xor<uint8_t>(uint8_t v, int off, int width) {
+  return static_cast<uint8_t>(__shfl_xor_sync(0xffffffffu, static_cast<int>(v), off, width));
+}
+
+// ---------------------------------------------------------------------------------
+// handles
+// ---------------------------------------------------------------------------------
+
+// Row-block partition of a CSR matrix for the SpMV / SpMM row-block kernels.
+// Regular blocks: contiguous rows [first, last) holding at most kBlockNnz stored
+// entries and kBlockRows rows.  Long rows (more than kBlockNnz entries) are cut into
+// segments of kSegNnz entries; the warp that finishes a row's last segment combines
+// the partials in segment order.
+struct RowBlocks {
+  int64_t nblocks = 0;      // regular blocks
+  int64_t nsegs = 0;        // long-row segments
+  int64_t nlong = 0;        // long rows
+  int2* blocks = nullptr;   // [nblocks] (first row, last row) 0-based, half-open
+  int4* segs = nullptr;     // [nsegs] (row, k_begin, k_end, long-row index) 0-based
+  int32_t* long_first_seg = nullptr;  // [nlong + 1] first segment of each long row
+  int32_t* long_rows = nullptr;       // [nlong] row id
+  unsigned int* long_count = nullptr; // [nlong] arrival counters (self-resetting)
+  void* partials = nullptr;           // [nsegs * partial_stride] bytes
+  int64_t partial_bytes = 0;
+};
+
+struct GraphAux;  // graph-algorithm analysis (gg_graph.cu)
+
+static const int kBlockNnz = 256;
+static const int kBlockRows = 256;
+static const int kSegNnz = 2048;
+
+}  // namespace gg
+
+struct gg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  // scratch arena, grown on demand, freed by gg_destroy
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  unsigned int* d_flags = nullptr;  // small device word array for status flags
+  unsigned int* h_flags = nullptr;  // pinned mirror
+};
+
+struct gg_mat {
+  int format = GG_FMT_CSR;
+  int64_t m = 0, n = 0, nnz = 0;
+  int dtype = GG_FLOAT32;
+  int device = 0;
+  // CSR (1-based)
+  int32_t* rowptr = nullptr;
+  int32_t* colval = nullptr;
+  void* nzval = nullptr;
+  // SELL (1-based slice_ptr / perm; colval -1 padded)
+  int64_t slice_size = 0, nslices = 0, n_stored = 0, sigma = 1;
+  int32_t* slice_ptr = nullptr;
+  int32_t* perm = nullptr;   // stored row -> original row (1-based)
+  int32_t* iperm = nullptr;  // original row (0-based) -> stored row (0-based)
+  // lazily built analysis
+  gg::RowBlocks* blocks = nullptr;
+  gg::GraphAux* aux = nullptr;
+  int64_t max_row_len = -1;
+};
+
+namespace gg {
+int ensure_scratch(gg_ctx* ctx, size_t bytes);
+void free_graph_aux(gg_mat* A);
+int compute_type(int tv, int tx, int mul);
+int check_semiring(int tv, int tx, int ty, int mul, int add, int accum, int* tc_out);
+int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, void* y, int ty,
+                  const void* x, int tx, const void* mask, int tmask, int64_t lo, int64_t hi);
+int build_row_blocks(gg_ctx* ctx, gg_mat* A);
+int row_stats(gg_ctx* ctx, gg_mat* A);
+}  // namespace gg

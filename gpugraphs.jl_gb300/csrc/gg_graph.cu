@@ -1,0 +1,1087 @@
+// gg_graph.cu -- BFS (levels and parents) and Bellman-Ford shortest paths of
+// GPUGraphs.jl (src/algorithms/bfs.jl, src/algorithms/shortest_path.jl).
+//
+// The reference runs level-synchronous masked SpMVs on A_T with host-side
+// convergence checks.  Its results are properties of the graph alone, so any exact
+// method reproduces them:
+//  * BFS levels: hop distance along in-edges of A_T whose stored value is odd (the
+//    reference tests band(A[v,u], curr[u]) with curr in {0,1}, bfs.jl:52-59).  Here:
+//    direction-optimising BFS.  Push steps walk out-edges (the transpose of A_T,
+//    built once per matrix) and claim vertices with an atomic OR on a visited
+//    bitmap; pull steps scan the in-edges of unvisited vertices against a frontier
+//    bitmap with early exit.  While the frontier is small, one CTA runs level after
+//    level with only block barriers (high-diameter graphs never leave it).
+//  * BFS parents: parent = first frontier column in storage order for CSR
+//    (src/spmv/CSR.jl:147-171) or the largest for SELL (GPUGraphs_any = max,
+//    algebra.jl:35); every stored edge counts.  Levels over all stored edges, then
+//    one pass picks, per reached vertex, the rule's in-neighbour one level up.
+//  * Shortest paths: the Jacobi fixpoint d(v) = min(d(v), min_u safe_add(w, d(u)))
+//    is order independent for non-negative weights (floating addition is monotone),
+//    so a frontier-based Bellman-Ford with atomicMin relaxations gives the same bits.
+//    Negative or NaN weights run the reference's Jacobi rounds (min-plus SpMV).
+#include <vector>
+
+#include "gg_semiring.cuh"
+
+namespace gg {
+
+static const unsigned kFullG = 0xffffffffu;
+
+struct PushCSR {       // out-edges (transpose of A_T), 0-based
+  int32_t* rowptr = nullptr;  // n + 1
+  int32_t* colval = nullptr;  // target vertex
+  void* w = nullptr;          // weights in the distance type (SSSP only)
+  int wtype = 0;
+  int64_t nnz = 0;
+  bool built = false;
+};
+
+struct GraphAux {
+  int32_t* vrowptr = nullptr;  // CSR view of A_T in original row order (1-based)
+  int32_t* vcolval = nullptr;
+  void* vnz = nullptr;
+  bool owns_view = false;
+  bool flags_ready = false;
+  bool all_odd = false;  // every stored value has bit 0 set (Bool true / odd integer)
+  bool nonneg = false;   // every stored value is >= 0 and not NaN
+  PushCSR push[3];       // 0: odd-valued edges, 1: all edges, 2: all edges + weights
+};
+
+void free_graph_aux(gg_mat* A) {
+  GraphAux* g = A->aux;
+  if (!g) return;
+  if (g->owns_view) {
+    cudaFree(g->vrowptr);
+    cudaFree(g->vcolval);
+    cudaFree(g->vnz);
+  }
+  for (int i = 0; i < 3; ++i) {
+    if (i == 1 && g->push[1].rowptr == g->push[0].rowptr) continue;
+    cudaFree(g->push[i].rowptr);
+    cudaFree(g->push[i].colval);
+    cudaFree(g->push[i].w);
+  }
+  delete g;
+  A->aux = nullptr;
+}
+
+static int gridsz(gg_ctx* ctx, int64_t work, int block = 256) {
+  int64_t g = (work + block - 1) / block;
+  const int64_t cap = (int64_t)ctx->num_sms * (2048 / block);
+  if (g > cap) g = cap;
+  return (int)(g < 1 ? 1 : g);
+}
+
+// ---------------------------------------------------------------------------------
+// exclusive scan of int32 counts -> int32 offsets (n + 1 entries, out[0] = base)
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ int32_t block_incl_scan(int32_t v, int32_t* wsum) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t y = __shfl_up_sync(kFullG, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int32_t s = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t y = __shfl_up_sync(kFullG, s, o);
+      if (lane >= o) s += y;
+    }
+    wsum[lane] = s;
+  }
+  __syncthreads();
+  const int32_t r = x + (w > 0 ? wsum[w - 1] : 0);
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(const int32_t* in, int64_t n, int32_t* out,
+                                                      int32_t* bsum) {
+  __shared__ int32_t wsum[32];
+  const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+  const int32_t v = i < n ? in[i] : 0;
+  const int32_t incl = block_incl_scan(v, wsum);
+  if (i < n) out[i] = incl - v;
+  if (threadIdx.x == 1023) bsum[blockIdx.x] = incl;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(int32_t* bsum, int64_t nb, int32_t* total) {
+  __shared__ int32_t wsum[32];
+  __shared__ int32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t b0 = 0; b0 < nb; b0 += 1024) {
+    const int64_t i = b0 + threadIdx.x;
+    const int32_t v = i < nb ? bsum[i] : 0;
+    const int32_t incl = block_incl_scan(v, wsum);
+    const int32_t c = carry;
+    if (i < nb) bsum[i] = c + incl - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = c + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(int32_t* out, int64_t n, const int32_t* bsum, const int32_t* total,
+                           int32_t base) {
+  const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+  if (i < n) out[i] += bsum[blockIdx.x] + base;
+  if (i == 0) out[n] = *total + base;
+}
+
+// out[0..n] = base + exclusive prefix sums of cnt[0..n-1]; out[n] = base + total
+static int scan_counts(gg_ctx* ctx, const int32_t* cnt, int64_t n, int32_t* out, int32_t base) {
+  const int64_t nb = (n + 1023) / 1024;
+  int32_t* tmp = nullptr;
+  GG_CUDA(cudaMalloc((void**)&tmp, (nb + 2) * sizeof(int32_t)));
+  if (n > 0) {
+    k_scan_blocks<<<(unsigned)nb, 1024, 0, ctx->stream>>>(cnt, n, out, tmp);
+    k_scan_sums<<<1, 1024, 0, ctx->stream>>>(tmp, nb, tmp + nb);
+    k_scan_add<<<(unsigned)nb, 1024, 0, ctx->stream>>>(out, n, tmp, tmp + nb, base);
+  } else {
+    cudaMemcpyAsync(out, &base, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream);
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return cuda_error(e, "scan");
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// analysis: CSR view, value flags, push (transpose) structures
+// ---------------------------------------------------------------------------------
+__global__ void k_value_flags(const void* nz, int tv, int64_t nnz, unsigned* flags) {
+  unsigned bad = 0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const Raw r = load_raw(nz, tv, k);
+    if (dtype_is_float(tv)) {
+      bad |= 1u;  // band has no Float method: never "odd"
+      if (!(r.d >= 0.0)) bad |= 2u;
+    } else {
+      if ((r.i & 1) == 0) bad |= 1u;
+      if (r.i < 0) bad |= 2u;
+    }
+  }
+  if (bad) atomicOr(flags, bad);
+}
+
+__global__ void k_sell_rowlen(int64_t m, int64_t C, const int32_t* slice_ptr, const int32_t* colval,
+                              const int32_t* iperm, int32_t* len) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = iperm[r], s = t / C, o = t - s * C;
+    const int64_t i0 = (int64_t)slice_ptr[s] - 1 + o, i1 = (int64_t)slice_ptr[s + 1] - 1;
+    int32_t l = 0;
+    for (int64_t i = i0; i < i1 && colval[i] != -1; i += C) ++l;
+    len[r] = l;
+  }
+}
+
+__global__ void k_sell_to_csr(int64_t m, int64_t C, const int32_t* slice_ptr, const int32_t* colval,
+                              const char* nz, int esz, const int32_t* iperm, const int32_t* rowptr,
+                              int32_t* ocol, char* onz) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = iperm[r], s = t / C, o = t - s * C;
+    const int64_t i0 = (int64_t)slice_ptr[s] - 1 + o;
+    const int64_t d0 = (int64_t)rowptr[r] - 1, len = (int64_t)rowptr[r + 1] - rowptr[r];
+    for (int64_t j = 0; j < len; ++j) {
+      const int64_t i = i0 + j * C;
+      ocol[d0 + j] = colval[i];
+      for (int b = 0; b < esz; ++b) onz[(d0 + j) * esz + b] = nz[i * esz + b];
+    }
+  }
+}
+
+__device__ __forceinline__ bool value_odd(const void* nz, int tv, int64_t k) {
+  switch (tv) {
+    case GG_BOOL: return static_cast<const uint8_t*>(nz)[k] & 1;
+    case GG_INT32: return static_cast<const int32_t*>(nz)[k] & 1;
+    case GG_INT64: return static_cast<const int64_t*>(nz)[k] & 1;
+  }
+  return false;
+}
+
+// warp per row of A_T: count (mode 0: odd-valued edges only) out-degree of each column
+__global__ void k_tr_count(int64_t n, const int32_t* rp, const int32_t* cv, const void* nz, int tv,
+                           int odd_only, int32_t* cnt) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    for (int64_t k = (int64_t)rp[r] - 1 + lane; k < (int64_t)rp[r + 1] - 1; k += 32)
+      if (!odd_only || value_odd(nz, tv, k)) atomicAdd(cnt + (cv[k] - 1), 1);
+  }
+}
+
+template <typename TD>
+__global__ void k_tr_scatter(int64_t n, const int32_t* rp, const int32_t* cv, const void* nz,
+                             int tv, int odd_only, int32_t* cursor, int32_t* ocol, TD* ow) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    for (int64_t k = (int64_t)rp[r] - 1 + lane; k < (int64_t)rp[r + 1] - 1; k += 32) {
+      if (odd_only && !value_odd(nz, tv, k)) continue;
+      const int32_t pos = atomicAdd(cursor + (cv[k] - 1), 1);
+      ocol[pos] = (int32_t)r;
+      if (ow) {
+        const Raw v = load_raw(nz, tv, k);
+        ow[pos] = dtype_is_float(tv) ? static_cast<TD>(v.d) : static_cast<TD>(v.i);
+      }
+    }
+  }
+}
+
+static int dist_type_of(int tv) { return tv == GG_BOOL ? GG_INT32 : tv; }
+
+static int ensure_aux(gg_ctx* ctx, gg_mat* A) {
+  if (A->aux && A->aux->flags_ready) return GG_OK;
+  GraphAux* g = A->aux ? A->aux : new GraphAux();
+  A->aux = g;
+  const int64_t n = A->m;
+  if (A->format == GG_FMT_CSR) {
+    g->vrowptr = A->rowptr;
+    g->vcolval = A->colval;
+    g->vnz = A->nzval;
+    g->owns_view = false;
+  } else if (!g->vrowptr) {
+    int32_t* len = nullptr;
+    const int esz = dtype_size(A->dtype);
+    GG_CUDA(cudaMalloc((void**)&len, (n > 0 ? n : 1) * sizeof(int32_t)));
+    GG_CUDA(cudaMalloc((void**)&g->vrowptr, (n + 1) * sizeof(int32_t)));
+    g->owns_view = true;
+    if (n > 0)
+      k_sell_rowlen<<<gridsz(ctx, n), 256, 0, ctx->stream>>>(n, A->slice_size, A->slice_ptr,
+                                                             A->colval, A->iperm, len);
+    int rc = scan_counts(ctx, len, n, g->vrowptr, 1);
+    cudaFree(len);
+    if (rc) return rc;
+    GG_CUDA(cudaMalloc((void**)&g->vcolval, (A->nnz > 0 ? A->nnz : 1) * sizeof(int32_t)));
+    GG_CUDA(cudaMalloc(&g->vnz, (A->nnz > 0 ? A->nnz : 1) * esz));
+    if (n > 0)
+      k_sell_to_csr<<<gridsz(ctx, n), 256, 0, ctx->stream>>>(
+          n, A->slice_size, A->slice_ptr, A->colval, static_cast<const char*>(A->nzval), esz,
+          A->iperm, g->vrowptr, g->vcolval, static_cast<char*>(g->vnz));
+    GG_CUDA(cudaGetLastError());
+  }
+  GG_CUDA(cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned), ctx->stream));
+  if (A->nnz > 0)
+    k_value_flags<<<gridsz(ctx, A->nnz), 256, 0, ctx->stream>>>(g->vnz, A->dtype, A->nnz, ctx->d_flags);
+  GG_CUDA(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  g->all_odd = !(ctx->h_flags[0] & 1u);
+  g->nonneg = !(ctx->h_flags[0] & 2u);
+  g->flags_ready = true;
+  return GG_OK;
+}
+
+// which: 0 odd-valued edges, 1 all edges, 2 all edges with weights in the distance type
+static int ensure_push(gg_ctx* ctx, gg_mat* A, int which) {
+  GG_CHECK(ensure_aux(ctx, A));
+  GraphAux* g = A->aux;
+  if (which == 0 && g->all_odd) which = 1;
+  PushCSR& P = g->push[which];
+  if (P.built) return GG_OK;
+  if (which == 1 && g->all_odd && g->push[0].built) {
+    P = g->push[0];
+    return GG_OK;
+  }
+  const int64_t n = A->m;
+  const int odd_only = which == 0 ? 1 : 0;
+  int32_t* cnt = nullptr;
+  GG_CUDA(cudaMalloc((void**)&cnt, (n > 0 ? n : 1) * sizeof(int32_t)));
+  GG_CUDA(cudaMemsetAsync(cnt, 0, (n > 0 ? n : 1) * sizeof(int32_t), ctx->stream));
+  if (n > 0)
+    k_tr_count<<<gridsz(ctx, n * 32), 256, 0, ctx->stream>>>(n, g->vrowptr, g->vcolval, g->vnz,
+                                                             A->dtype, odd_only, cnt);
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaMalloc((void**)&P.rowptr, (n + 1) * sizeof(int32_t)));
+  int rc = scan_counts(ctx, cnt, n, P.rowptr, 0);
+  if (rc) {
+    cudaFree(cnt);
+    return rc;
+  }
+  int32_t total = 0;
+  GG_CUDA(cudaMemcpy(&total, P.rowptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  P.nnz = total;
+  GG_CUDA(cudaMemcpyAsync(cnt, P.rowptr, (n > 0 ? n : 1) * sizeof(int32_t),
+                          cudaMemcpyDeviceToDevice, ctx->stream));
+  GG_CUDA(cudaMalloc((void**)&P.colval, (total > 0 ? total : 1) * sizeof(int32_t)));
+  const int td = dist_type_of(A->dtype);
+  if (which == 2) {
+    P.wtype = td;
+    GG_CUDA(cudaMalloc(&P.w, (total > 0 ? total : 1) * dtype_size(td)));
+  }
+  if (n > 0) {
+    const int grid = gridsz(ctx, n * 32);
+    switch (which == 2 ? td : GG_INT32) {
+      case GG_INT64:
+        k_tr_scatter<int64_t><<<grid, 256, 0, ctx->stream>>>(n, g->vrowptr, g->vcolval, g->vnz, A->dtype,
+                                                             odd_only, cnt, P.colval, (int64_t*)P.w);
+        break;
+      case GG_FLOAT32:
+        k_tr_scatter<float><<<grid, 256, 0, ctx->stream>>>(n, g->vrowptr, g->vcolval, g->vnz, A->dtype,
+                                                           odd_only, cnt, P.colval, (float*)P.w);
+        break;
+      case GG_FLOAT64:
+        k_tr_scatter<double><<<grid, 256, 0, ctx->stream>>>(n, g->vrowptr, g->vcolval, g->vnz, A->dtype,
+                                                            odd_only, cnt, P.colval, (double*)P.w);
+        break;
+      default:
+        k_tr_scatter<int32_t><<<grid, 256, 0, ctx->stream>>>(n, g->vrowptr, g->vcolval, g->vnz, A->dtype,
+                                                             odd_only, cnt, P.colval, (int32_t*)P.w);
+    }
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(cnt);
+  if (e != cudaSuccess) return cuda_error(e, "transpose");
+  GG_CUDA(cudaGetLastError());
+  P.built = true;
+  return GG_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// BFS kernels
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ bool bit_of(const unsigned* bm, int32_t v) {
+  return (bm[v >> 5] >> (v & 31)) & 1u;
+}
+
+// counters: [0] next frontier size, [1] sum of out-degrees of the next frontier
+struct Counters {
+  unsigned long long nf, mf, level, status;
+};
+
+// warp-aggregated append of the lanes with `want` into q (full warp must call)
+__device__ __forceinline__ void warp_append(bool want, int32_t v, int32_t deg, int32_t* q,
+                                            Counters* ctr) {
+  const int lane = threadIdx.x & 31;
+  const unsigned b = __ballot_sync(kFullG, want);
+  if (!b) return;
+  int32_t d = want ? deg : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(kFullG, d, o);
+  const int leader = __ffs(b) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) {
+    base = atomicAdd(&ctr->nf, (unsigned long long)__popc(b));
+    atomicAdd(&ctr->mf, (unsigned long long)d);
+  }
+  base = __shfl_sync(kFullG, base, leader);
+  if (want) q[base + __popc(b & ((1u << lane) - 1u))] = v;
+}
+
+__global__ void k_bfs_init(int32_t s, unsigned* visited, int32_t* dist, int32_t* q) {
+  visited[s >> 5] |= 1u << (s & 31);
+  dist[s] = 0;
+  q[0] = s;
+}
+
+// top-down level: warp per frontier vertex, lanes over its out-edges
+__global__ void __launch_bounds__(256)
+    k_bfs_push(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+               const int32_t* __restrict__ q, int64_t nf, int32_t level, unsigned* visited,
+               int32_t* dist, int32_t* qn, Counters* ctr) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nf;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int32_t u = q[i];
+    const int32_t k0 = prow[u], k1 = prow[u + 1];
+    for (int32_t base = k0; base < k1; base += 32) {
+      const int32_t k = base + lane;
+      bool claim = false;
+      int32_t w = 0, deg = 0;
+      if (k < k1) {
+        w = __ldg(pcol + k);
+        const unsigned bit = 1u << (w & 31);
+        if (!(__ldcg(visited + (w >> 5)) & bit)) claim = !(atomicOr(visited + (w >> 5), bit) & bit);
+        if (claim) {
+          dist[w] = level;
+          deg = prow[w + 1] - prow[w];
+        }
+      }
+      warp_append(claim, w, deg, qn, ctr);
+    }
+  }
+}
+
+// bottom-up level: thread per vertex; an unvisited vertex joins when one of its
+// in-neighbours (A_T row) is in the frontier bitmap over an active edge
+template <bool kOddOnly>
+__global__ void __launch_bounds__(256)
+    k_bfs_pull(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cv,
+               const void* nz, int tv, const unsigned* __restrict__ fb, unsigned* visited,
+               int32_t* dist, int32_t level, unsigned* fbn, int32_t* qn, Counters* ctr,
+               const int32_t* __restrict__ prow) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int64_t v = base + threadIdx.x;
+    bool found = false;
+    const unsigned vw = (v < n) ? visited[v >> 5] : ~0u;
+    if (v < n && !((vw >> (v & 31)) & 1u)) {
+      const int32_t k1 = rp[v + 1] - 1;
+      for (int32_t k = rp[v] - 1; k < k1; ++k) {
+        const int32_t u = __ldg(cv + k) - 1;
+        if (bit_of(fb, u) && (!kOddOnly || value_odd(nz, tv, k))) {
+          found = true;
+          break;
+        }
+      }
+    }
+    const unsigned bal = __ballot_sync(kFullG, found);
+    if (found) dist[v] = level;
+    if (lane == 0 && bal) {
+      const int64_t word = v >> 5;  // the warp's 32 vertices share one bitmap word
+      visited[word] = vw | bal;
+      fbn[word] = bal;
+    }
+    warp_append(found, (int32_t)v, found ? prow[v + 1] - prow[v] : 0, qn, ctr);
+  }
+}
+
+__global__ void k_queue_to_bitmap(const int32_t* q, int64_t nf, unsigned* bm) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t v = q[i];
+    atomicOr(bm + (v >> 5), 1u << (v & 31));
+  }
+}
+
+// Small-frontier BFS: one CTA runs top-down levels back to back while the frontier
+// fits in shared memory.  qg holds the starting frontier (nf0 <= cap) and receives
+// the overflowing frontier when it grows past cap.  Out: ctr->nf = size of the last
+// discovered frontier (0 when the search is finished), ctr->level = its level.
+__global__ void __launch_bounds__(1024)
+    k_bfs_small(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol, int32_t* qg,
+                int32_t nf0, int32_t level0, int32_t cap, unsigned* visited, int32_t* dist,
+                Counters* ctr) {
+  extern __shared__ int32_t smem[];
+  int32_t* cur = smem;
+  int32_t* nxt = smem + cap;
+  int32_t* heavy = smem + 2 * cap;
+  __shared__ int32_t s_nn, s_nh;
+  __shared__ unsigned long long s_mf;
+  for (int32_t i = threadIdx.x; i < nf0; i += blockDim.x) cur[i] = qg[i];
+  int32_t nf = nf0, level = level0;
+  __syncthreads();
+  for (;;) {
+    ++level;
+    if (threadIdx.x == 0) {
+      s_nn = 0;
+      s_nh = 0;
+      s_mf = 0;
+    }
+    __syncthreads();
+    // light vertices: one thread each; heavy ones are deferred to the whole block
+    for (int32_t i = threadIdx.x; i < nf; i += blockDim.x) {
+      const int32_t u = cur[i];
+      const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
+      if (k1 - k0 > 32) {
+        heavy[atomicAdd(&s_nh, 1)] = u;
+        continue;
+      }
+      for (int32_t k = k0; k < k1; ++k) {
+        const int32_t w = __ldg(pcol + k);
+        const unsigned bit = 1u << (w & 31);
+        if (__ldcg(visited + (w >> 5)) & bit) continue;
+        if (atomicOr(visited + (w >> 5), bit) & bit) continue;
+        dist[w] = level;
+        const int32_t pos = atomicAdd(&s_nn, 1);
+        if (pos < cap) nxt[pos] = w;
+        else qg[pos] = w;
+        atomicAdd(&s_mf, (unsigned long long)(__ldg(prow + w + 1) - __ldg(prow + w)));
+      }
+    }
+    __syncthreads();
+    const int32_t nh = s_nh;
+    for (int32_t h = 0; h < nh; ++h) {
+      const int32_t u = heavy[h];
+      const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
+      for (int32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const int32_t w = __ldg(pcol + k);
+        const unsigned bit = 1u << (w & 31);
+        if (__ldcg(visited + (w >> 5)) & bit) continue;
+        if (atomicOr(visited + (w >> 5), bit) & bit) continue;
+        dist[w] = level;
+        const int32_t pos = atomicAdd(&s_nn, 1);
+        if (pos < cap) nxt[pos] = w;
+        else qg[pos] = w;
+        atomicAdd(&s_mf, (unsigned long long)(__ldg(prow + w + 1) - __ldg(prow + w)));
+      }
+    }
+    __syncthreads();
+    const int32_t nn = s_nn;
+    if (nn == 0 || nn > cap) {
+      if (nn > cap)
+        for (int32_t i = threadIdx.x; i < cap; i += blockDim.x) qg[i] = nxt[i];
+      if (threadIdx.x == 0) {
+        ctr->nf = (unsigned long long)nn;
+        ctr->mf = s_mf;
+        ctr->level = (unsigned long long)level;
+      }
+      return;
+    }
+    int32_t* t = cur;
+    cur = nxt;
+    nxt = t;
+    nf = nn;
+    __syncthreads();
+  }
+}
+
+static const int kSmallCap = 8192;
+static const int kSmallThreads = 1024;
+static const size_t kSmallSmem = 3 * kSmallCap * sizeof(int32_t);
+
+struct BfsScratch {
+  unsigned* visited;
+  unsigned* fb[2];
+  int32_t* q[2];
+  Counters* ctr;
+};
+
+static int bfs_scratch(gg_ctx* ctx, int64_t n, BfsScratch* s) {
+  const int64_t nw = (n + 31) / 32 + 1;
+  const size_t bm = ((nw * sizeof(unsigned)) + 255) & ~(size_t)255;
+  const size_t qb = (((n + 1) * sizeof(int32_t)) + 255) & ~(size_t)255;
+  GG_CHECK(ensure_scratch(ctx, 3 * bm + 2 * qb + 256));
+  char* p = static_cast<char*>(ctx->scratch);
+  s->visited = (unsigned*)p;
+  s->fb[0] = (unsigned*)(p + bm);
+  s->fb[1] = (unsigned*)(p + 2 * bm);
+  s->q[0] = (int32_t*)(p + 3 * bm);
+  s->q[1] = (int32_t*)(p + 3 * bm + qb);
+  s->ctr = (Counters*)(p + 3 * bm + 2 * qb);
+  GG_CUDA(cudaMemsetAsync(p, 0, 3 * bm, ctx->stream));
+  return GG_OK;
+}
+
+// Runs the BFS from source s (0-based) over the edges selected by `which` (0: odd
+// values, 1: all stored); writes level(v) into dist for every reached v.
+static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
+                   int64_t* levels_out) {
+  GG_CHECK(ensure_push(ctx, A, which));
+  GraphAux* g = A->aux;
+  const bool odd_only = (which == 0 && !g->all_odd);
+  PushCSR& P = g->push[(which == 0 && g->all_odd) ? 1 : which];
+  const int64_t n = A->m;
+  BfsScratch sc;
+  GG_CHECK(bfs_scratch(ctx, n, &sc));
+  GG_CUDA(cudaFuncSetAttribute(k_bfs_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)kSmallSmem));
+  k_bfs_init<<<1, 1, 0, ctx->stream>>>(s, sc.visited, dist, sc.q[0]);
+  GG_CUDA(cudaGetLastError());
+  Counters* h = reinterpret_cast<Counters*>(ctx->h_flags);
+  int64_t nf = 1, level = 0, mf = 0, explored = 0;
+  int cur = 0;
+  bool frontier_is_bitmap = false, pull = false;
+  const int64_t total_edges = P.nnz;
+  while (nf > 0) {
+    if (!pull && nf <= kSmallCap) {
+      k_bfs_small<<<1, kSmallThreads, kSmallSmem, ctx->stream>>>(
+          P.rowptr, P.colval, sc.q[cur], (int32_t)nf, (int32_t)level, kSmallCap, sc.visited, dist,
+          sc.ctr);
+      GG_CUDA(cudaGetLastError());
+      GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+      GG_CUDA(cudaStreamSynchronize(ctx->stream));
+      nf = (int64_t)h->nf;
+      level = (int64_t)h->level;
+      mf = (int64_t)h->mf;
+      if (nf == 0) break;
+      explored += mf;
+      continue;  // frontier of `level` is in q[cur]
+    }
+    // direction heuristic (Beamer et al.): pull when the frontier's edges outweigh a
+    // 1/14 share of the unexplored edges, push again once the frontier is small
+    const int64_t unexplored = total_edges - explored > 0 ? total_edges - explored : 0;
+    if (!pull && mf * 14 > unexplored) pull = true;
+    else if (pull && nf * 24 < n) pull = false;
+    ++level;
+    GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+    if (pull) {
+      if (!frontier_is_bitmap) {
+        GG_CUDA(cudaMemsetAsync(sc.fb[cur], 0, ((n + 31) / 32) * sizeof(unsigned), ctx->stream));
+        k_queue_to_bitmap<<<gridsz(ctx, nf), 256, 0, ctx->stream>>>(sc.q[cur], nf, sc.fb[cur]);
+      }
+      GG_CUDA(cudaMemsetAsync(sc.fb[cur ^ 1], 0, ((n + 31) / 32) * sizeof(unsigned), ctx->stream));
+      if (odd_only)
+        k_bfs_pull<true><<<gridsz(ctx, n), 256, 0, ctx->stream>>>(
+            n, g->vrowptr, g->vcolval, g->vnz, A->dtype, sc.fb[cur], sc.visited, dist,
+            (int32_t)level, sc.fb[cur ^ 1], sc.q[cur ^ 1], sc.ctr, P.rowptr);
+      else
+        k_bfs_pull<false><<<gridsz(ctx, n), 256, 0, ctx->stream>>>(
+            n, g->vrowptr, g->vcolval, g->vnz, A->dtype, sc.fb[cur], sc.visited, dist,
+            (int32_t)level, sc.fb[cur ^ 1], sc.q[cur ^ 1], sc.ctr, P.rowptr);
+      frontier_is_bitmap = true;
+    } else {
+      k_bfs_push<<<gridsz(ctx, nf * 32), 256, 0, ctx->stream>>>(
+          P.rowptr, P.colval, sc.q[cur], nf, (int32_t)level, sc.visited, dist, sc.q[cur ^ 1], sc.ctr);
+      frontier_is_bitmap = false;
+    }
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    nf = (int64_t)h->nf;
+    mf = (int64_t)h->mf;
+    explored += mf;
+    cur ^= 1;  // the queue of the new frontier is always written; its bitmap only by pull levels
+  }
+  if (levels_out) *levels_out = level;
+  return GG_OK;
+}
+
+// parents: warp per reached vertex; rule 1 = first qualifying in-neighbour in
+// storage order, rule 2 = largest qualifying column
+__global__ void __launch_bounds__(256)
+    k_bfs_parents(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cv,
+                  const int32_t* __restrict__ lev, int32_t source, int rule, int32_t* parents) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n;
+       v += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int32_t lv = lev[v];
+    if (lv == INT32_MAX) continue;  // unreached: left untouched (bfs.jl:176)
+    if (v == source) {
+      if (lane == 0) parents[v] = 0;
+      continue;
+    }
+    const int32_t k0 = rp[v] - 1, k1 = rp[v + 1] - 1;
+    int32_t best = 0;
+    for (int32_t base = k0; base < k1; base += 32) {
+      const int32_t k = base + lane;
+      int32_t c = 0;
+      if (k < k1) {
+        const int32_t col = __ldg(cv + k);
+        if (__ldg(lev + col - 1) == lv - 1) c = col;
+      }
+      if (rule == GG_PARENT_FIRST_IN_ROW) {
+        const unsigned b = __ballot_sync(kFullG, c != 0);
+        if (b) {
+          best = __shfl_sync(kFullG, c, __ffs(b) - 1);
+          break;
+        }
+      } else {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c = max(c, __shfl_xor_sync(kFullG, c, o));
+        best = max(best, c);
+      }
+    }
+    if (lane == 0) parents[v] = best;
+  }
+}
+
+__global__ void k_fill_i32(int32_t* p, int64_t n, int32_t v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+// ---------------------------------------------------------------------------------
+// SSSP kernels (non-negative weights)
+// ---------------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ T atomic_min_t(T* p, T v);
+template <> __device__ __forceinline__ int32_t atomic_min_t<int32_t>(int32_t* p, int32_t v) {
+  return atomicMin(p, v);
+}
+template <> __device__ __forceinline__ int64_t atomic_min_t<int64_t>(int64_t* p, int64_t v) {
+  return (int64_t)atomicMin((long long*)p, (long long)v);
+}
+// non-negative floats order like their bit patterns
+template <> __device__ __forceinline__ float atomic_min_t<float>(float* p, float v) {
+  return __int_as_float(atomicMin((int*)p, __float_as_int(v)));
+}
+template <> __device__ __forceinline__ double atomic_min_t<double>(double* p, double v) {
+  return __longlong_as_double(atomicMin((long long*)p, __double_as_longlong(v)));
+}
+
+template <typename T> __device__ __forceinline__ T ld_cg(const T* p) { return __ldcg(p); }
+
+// safe_add on non-negative, non-NaN operands (algebra.jl:47-48)
+template <typename T> __device__ __forceinline__ T relax_add(T w, T d) {
+  return (w == Lim<T>::max() || d == Lim<T>::max()) ? Lim<T>::max() : w_add(w, d);
+}
+
+// relax the out-edges of frontier vertices; improved targets join the next frontier
+// once (bitmap inq); the frontier vertex's own bit in inq_cur is cleared
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_sssp_push(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+                const T* __restrict__ pw, const int32_t* __restrict__ q, int64_t nf, T* dist,
+                unsigned* inq_cur, unsigned* inq_next, int32_t* qn, Counters* ctr) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nf;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int32_t u = q[i];
+    if (lane == 0) atomicAnd(inq_cur + (u >> 5), ~(1u << (u & 31)));
+    const T du = ld_cg(dist + u);
+    const int32_t k0 = prow[u], k1 = prow[u + 1];
+    for (int32_t base = k0; base < k1; base += 32) {
+      const int32_t k = base + lane;
+      bool add = false;
+      int32_t w = 0;
+      if (k < k1) {
+        w = __ldg(pcol + k);
+        const T cand = relax_add(__ldg(pw + k), du);
+        if (cand < ld_cg(dist + w)) {
+          const T old = atomic_min_t(dist + w, cand);
+          if (cand < old) {
+            const unsigned bit = 1u << (w & 31);
+            add = !(atomicOr(inq_next + (w >> 5), bit) & bit);
+          }
+        }
+      }
+      warp_append(add, w, 0, qn, ctr);
+    }
+  }
+}
+
+// single-CTA rounds while the frontier is small (mirror of k_bfs_small)
+template <typename T>
+__global__ void __launch_bounds__(1024)
+    k_sssp_small(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+                 const T* __restrict__ pw, int32_t* qg, int32_t nf0, int32_t cap, T* dist,
+                 unsigned* inq_a, unsigned* inq_b, Counters* ctr, int64_t max_rounds) {
+  extern __shared__ int32_t smem[];
+  int32_t* cur = smem;
+  int32_t* nxt = smem + cap;
+  int32_t* heavy = smem + 2 * cap;
+  __shared__ int32_t s_nn, s_nh;
+  for (int32_t i = threadIdx.x; i < nf0; i += blockDim.x) cur[i] = qg[i];
+  int32_t nf = nf0;
+  unsigned* ic = inq_a;
+  unsigned* in = inq_b;
+  unsigned long long rounds = 0;
+  __syncthreads();
+  for (;;) {
+    ++rounds;
+    if (threadIdx.x == 0) {
+      s_nn = 0;
+      s_nh = 0;
+    }
+    __syncthreads();
+    for (int32_t i = threadIdx.x; i < nf; i += blockDim.x) {
+      const int32_t u = cur[i];
+      atomicAnd(ic + (u >> 5), ~(1u << (u & 31)));
+      const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
+      if (k1 - k0 > 32) {
+        heavy[atomicAdd(&s_nh, 1)] = u;
+        continue;
+      }
+      const T du = ld_cg(dist + u);
+      for (int32_t k = k0; k < k1; ++k) {
+        const int32_t w = __ldg(pcol + k);
+        const T cand = relax_add(__ldg(pw + k), du);
+        if (!(cand < ld_cg(dist + w))) continue;
+        if (!(cand < atomic_min_t(dist + w, cand))) continue;
+        const unsigned bit = 1u << (w & 31);
+        if (atomicOr(in + (w >> 5), bit) & bit) continue;
+        const int32_t pos = atomicAdd(&s_nn, 1);
+        if (pos < cap) nxt[pos] = w;
+        else qg[pos] = w;
+      }
+    }
+    __syncthreads();
+    const int32_t nh = s_nh;
+    for (int32_t h = 0; h < nh; ++h) {
+      const int32_t u = heavy[h];
+      const T du = ld_cg(dist + u);
+      const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
+      for (int32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const int32_t w = __ldg(pcol + k);
+        const T cand = relax_add(__ldg(pw + k), du);
+        if (!(cand < ld_cg(dist + w))) continue;
+        if (!(cand < atomic_min_t(dist + w, cand))) continue;
+        const unsigned bit = 1u << (w & 31);
+        if (atomicOr(in + (w >> 5), bit) & bit) continue;
+        const int32_t pos = atomicAdd(&s_nn, 1);
+        if (pos < cap) nxt[pos] = w;
+        else qg[pos] = w;
+      }
+    }
+    __syncthreads();
+    const int32_t nn = s_nn;
+    if (nn == 0 || nn > cap || (max_rounds > 0 && (int64_t)rounds >= max_rounds)) {
+      if (nn > cap)
+        for (int32_t i = threadIdx.x; i < cap; i += blockDim.x) qg[i] = nxt[i];
+      else
+        for (int32_t i = threadIdx.x; i < nn; i += blockDim.x) qg[i] = nxt[i];
+      if (threadIdx.x == 0) {
+        ctr->nf = (unsigned long long)nn;
+        ctr->level = rounds;
+        ctr->status = (in == inq_b) ? 1ull : 0ull;  // which bitmap holds the frontier bits
+      }
+      return;
+    }
+    int32_t* t = cur;
+    cur = nxt;
+    nxt = t;
+    unsigned* tb = ic;
+    ic = in;
+    in = tb;
+    nf = nn;
+    __syncthreads();
+  }
+}
+
+// frontier = every vertex whose start distance is finite
+template <typename T>
+__global__ void k_sssp_seed(int64_t n, const T* dist, unsigned* inq, int32_t* q, Counters* ctr) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int64_t v = base + threadIdx.x;
+    const bool fin = v < n && dist[v] != Lim<T>::max();
+    const unsigned bal = __ballot_sync(kFullG, fin);
+    if ((threadIdx.x & 31) == 0 && bal) inq[v >> 5] = bal;
+    warp_append(fin, (int32_t)v, 0, q, ctr);
+  }
+}
+
+template <typename T>
+__global__ void k_fill_t(T* p, int64_t n, T v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+template <typename T>
+__global__ void k_set_source(T* dist, T* next, int64_t s) {
+  dist[s] = T(0);
+  if (next) next[s] = T(0);
+}
+
+// Jacobi helpers for the fallback path
+template <typename T>
+__global__ void k_changed_copy(int64_t n, const T* next, T* dist, unsigned* flag) {
+  unsigned ch = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T a = next[i], b = dist[i];
+    if (a < b) ch = 1;
+    dist[i] = a;
+  }
+  if (ch) atomicOr(flag, 1u);
+}
+
+template <typename T>
+static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
+  GG_CHECK(ensure_push(ctx, A, 2));
+  GraphAux* g = A->aux;
+  PushCSR& P = g->push[2];
+  const int64_t n = A->m;
+  BfsScratch sc;  // visited -> unused; fb[0], fb[1] are the two membership bitmaps
+  GG_CHECK(bfs_scratch(ctx, n, &sc));
+  GG_CUDA(cudaFuncSetAttribute(k_sssp_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)kSmallSmem));
+  Counters* h = reinterpret_cast<Counters*>(ctx->h_flags);
+  GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+  k_sssp_seed<T><<<gridsz(ctx, n), 256, 0, ctx->stream>>>(n, d, sc.fb[0], sc.q[0], sc.ctr);
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  int64_t nf = (int64_t)h->nf, rounds = 0;
+  int cur = 0;
+  const int64_t max_rounds = n + 1;  // Bellman-Ford bound for non-negative weights
+  while (nf > 0) {
+    if (rounds > max_rounds) return set_error(GG_ERR_NOT_CONVERGED, "shortest_path did not converge");
+    if (nf <= kSmallCap) {
+      GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+      k_sssp_small<T><<<1, kSmallThreads, kSmallSmem, ctx->stream>>>(
+          P.rowptr, P.colval, static_cast<const T*>(P.w), sc.q[cur], (int32_t)nf, kSmallCap, d,
+          sc.fb[cur], sc.fb[cur ^ 1], sc.ctr, max_rounds - rounds);
+      GG_CUDA(cudaGetLastError());
+      GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+      GG_CUDA(cudaStreamSynchronize(ctx->stream));
+      nf = (int64_t)h->nf;
+      rounds += (int64_t)h->level;
+      // the remaining frontier is in q[cur]; its membership bits are in fb[cur] when
+      // status == 0, else in fb[cur ^ 1] -- then swap roles so bits and queue agree
+      if (nf > 0 && h->status == 1) {
+        cur ^= 1;
+        GG_CUDA(cudaMemcpyAsync(sc.q[cur], sc.q[cur ^ 1], nf * sizeof(int32_t),
+                                cudaMemcpyDeviceToDevice, ctx->stream));
+      }
+      continue;
+    }
+    ++rounds;
+    GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+    k_sssp_push<T><<<gridsz(ctx, nf * 32), 256, 0, ctx->stream>>>(
+        P.rowptr, P.colval, static_cast<const T*>(P.w), sc.q[cur], nf, d, sc.fb[cur],
+        sc.fb[cur ^ 1], sc.q[cur ^ 1], sc.ctr);
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    nf = (int64_t)h->nf;
+    cur ^= 1;
+  }
+  if (rounds_out) *rounds_out += rounds;
+  return GG_OK;
+}
+
+// Jacobi rounds of the reference (shortest_path.jl:61-80) with the generic min-plus
+// SpMV; used for negative / NaN weights.  Stops when a round changes nothing.
+template <typename T>
+static int sssp_jacobi(gg_ctx* ctx, gg_mat* A, T* dist, T* next, int td, int64_t* rounds_out) {
+  const int64_t n = A->m;
+  int tc = 0;
+  GG_CHECK(check_semiring(A->dtype, td, td, GG_OP_SAFE_ADD, GG_OP_MIN, GG_OP_MIN, &tc));
+  for (int64_t r = 0; r <= n + 1; ++r) {
+    GG_CHECK(spmv_dispatch(ctx, A, tc, GG_OP_SAFE_ADD, GG_OP_MIN, GG_OP_MIN, next, td, dist, td,
+                           nullptr, 0, 0, 0));
+    GG_CUDA(cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned), ctx->stream));
+    k_changed_copy<T><<<gridsz(ctx, n), 256, 0, ctx->stream>>>(n, next, dist, ctx->d_flags);
+    GG_CUDA(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (rounds_out) *rounds_out += 1;
+    if (!ctx->h_flags[0]) return GG_OK;
+  }
+  return set_error(GG_ERR_NOT_CONVERGED, "shortest_path did not converge (negative cycle?)");
+}
+
+template <typename T>
+static int sssp_column(gg_ctx* ctx, gg_mat* A, int64_t s, T* dist, T* next, int td, bool caller,
+                       int64_t* rounds_out) {
+  const int64_t n = A->m;
+  GraphAux* g = A->aux;
+  if (!caller) {
+    k_fill_t<T><<<gridsz(ctx, n), 256, 0, ctx->stream>>>(dist, n, Lim<T>::max());
+    if (next) k_fill_t<T><<<gridsz(ctx, n), 256, 0, ctx->stream>>>(next, n, Lim<T>::max());
+  }
+  k_set_source<T><<<1, 1, 0, ctx->stream>>>(dist, next, s);
+  GG_CUDA(cudaGetLastError());
+  if (!g->nonneg) {
+    T* nx = next;
+    if (!nx) {
+      GG_CUDA(cudaMalloc((void**)&nx, n * sizeof(T)));
+      GG_CUDA(cudaMemcpyAsync(nx, dist, n * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    int rc = sssp_jacobi<T>(ctx, A, dist, nx, td, rounds_out);
+    if (!next) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(nx);
+    }
+    return rc;
+  }
+  T* start = dist;
+  if (caller && next) {
+    // first Jacobi round exactly as the reference: next = min(next, F(dist))
+    int tc = 0;
+    GG_CHECK(check_semiring(A->dtype, td, td, GG_OP_SAFE_ADD, GG_OP_MIN, GG_OP_MIN, &tc));
+    GG_CHECK(spmv_dispatch(ctx, A, tc, GG_OP_SAFE_ADD, GG_OP_MIN, GG_OP_MIN, next, td, dist, td,
+                           nullptr, 0, 0, 0));
+    start = next;
+  }
+  GG_CHECK(sssp_fixpoint<T>(ctx, A, start, rounds_out));
+  if (start != dist)
+    GG_CUDA(cudaMemcpyAsync(dist, start, n * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+  if (next && start != next)
+    GG_CUDA(cudaMemcpyAsync(next, dist, n * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+  return GG_OK;
+}
+
+static int check_graph(const gg_mat* A) {
+  if (A->m != A->n) return set_error(GG_ERR_DIMENSION, "A_T must be square (got %lld x %lld)",
+                                     (long long)A->m, (long long)A->n);
+  return GG_OK;
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+int gg_bfs_levels(gg_ctx* ctx, const gg_mat* A_T, int64_t source, int32_t* dist, int64_t n,
+                  int64_t* levels_out) {
+  if (!ctx || !A_T || !dist) return set_error(GG_ERR_ARGUMENT, "NULL argument");
+  GG_CHECK(check_graph(A_T));
+  if (n != A_T->m) return set_error(GG_ERR_DIMENSION, "dist length must equal size(A_T, 1)");
+  if (source < 1 || source > A_T->m) return set_error(GG_ERR_BOUNDS, "source %lld out of 1:%lld",
+                                                      (long long)source, (long long)A_T->m);
+  if (dtype_is_float(A_T->dtype))
+    return set_error(GG_ERR_UNSUPPORTED, "GPUGraphs_band has no method for floating-point matrices");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  gg_mat* A = const_cast<gg_mat*>(A_T);
+  return bfs_run(ctx, A, (int32_t)(source - 1), 0, dist, levels_out);
+}
+
+int gg_bfs_parents(gg_ctx* ctx, const gg_mat* A_T, int64_t source, int32_t* parents, int64_t n,
+                   int rule, int64_t* levels_out) {
+  if (!ctx || !A_T || !parents) return set_error(GG_ERR_ARGUMENT, "NULL argument");
+  GG_CHECK(check_graph(A_T));
+  if (n != A_T->m) return set_error(GG_ERR_DIMENSION, "parents length must equal size(A_T, 1)");
+  if (source < 1 || source > A_T->m) return set_error(GG_ERR_BOUNDS, "source %lld out of 1:%lld",
+                                                      (long long)source, (long long)A_T->m);
+  if (rule == GG_PARENT_FORMAT_DEFAULT)
+    rule = A_T->format == GG_FMT_CSR ? GG_PARENT_FIRST_IN_ROW : GG_PARENT_MAX_INDEX;
+  if (rule != GG_PARENT_FIRST_IN_ROW && rule != GG_PARENT_MAX_INDEX)
+    return set_error(GG_ERR_ARGUMENT, "unknown parent rule %d", rule);
+  GG_CUDA(cudaSetDevice(ctx->device));
+  gg_mat* A = const_cast<gg_mat*>(A_T);
+  int32_t* lev = nullptr;
+  GG_CUDA(cudaMallocAsync((void**)&lev, n * sizeof(int32_t), ctx->stream));
+  k_fill_i32<<<gridsz(ctx, n), 256, 0, ctx->stream>>>(lev, n, INT32_MAX);
+  int rc = bfs_run(ctx, A, (int32_t)(source - 1), 1, lev, levels_out);
+  if (rc == GG_OK) {
+    GraphAux* g = A->aux;
+    k_bfs_parents<<<gridsz(ctx, n * 32), 256, 0, ctx->stream>>>(
+        n, g->vrowptr, g->vcolval, lev, (int32_t)(source - 1), rule, parents);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = cuda_error(e, "k_bfs_parents");
+  }
+  cudaFreeAsync(lev, ctx->stream);
+  return rc;
+}
+
+int gg_sssp(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, int64_t nsources, void* dist,
+            void* next, int dist_dtype, int64_t ld, int64_t* rounds_out) {
+  if (!ctx || !A_T || !dist || (nsources > 0 && !sources))
+    return set_error(GG_ERR_ARGUMENT, "NULL argument");
+  GG_CHECK(check_graph(A_T));
+  const int64_t n = A_T->m;
+  if (ld < n) return set_error(GG_ERR_DIMENSION, "leading dimension of dist must be >= n");
+  if (dist_dtype != dist_type_of(A_T->dtype))
+    return set_error(GG_ERR_TYPE, "dist element type must be Int32 for Bool matrices, else eltype(A_T)");
+  for (int64_t q = 0; q < nsources; ++q)
+    if (sources[q] < 1 || sources[q] > n)
+      return set_error(GG_ERR_BOUNDS, "source %lld out of 1:%lld", (long long)sources[q], (long long)n);
+  if (rounds_out) *rounds_out = 0;
+  GG_CUDA(cudaSetDevice(ctx->device));
+  gg_mat* A = const_cast<gg_mat*>(A_T);
+  GG_CHECK(ensure_aux(ctx, A));
+  const bool caller = next != nullptr;
+  const int esz = dtype_size(dist_dtype);
+  for (int64_t q = 0; q < nsources; ++q) {
+    char* dcol = static_cast<char*>(dist) + q * ld * esz;
+    char* ncol = next ? static_cast<char*>(next) + q * ld * esz : nullptr;
+    int rc = GG_OK;
+    switch (dist_dtype) {
+      case GG_INT32:
+        rc = sssp_column<int32_t>(ctx, A, sources[q] - 1, (int32_t*)dcol, (int32_t*)ncol, dist_dtype, caller, rounds_out);
+        break;
+      case GG_INT64:
+        rc = sssp_column<int64_t>(ctx, A, sources[q] - 1, (int64_t*)dcol, (int64_t*)ncol, dist_dtype, caller, rounds_out);
+        break;
+      case GG_FLOAT32:
+        rc = sssp_column<float>(ctx, A, sources[q] - 1, (float*)dcol, (float*)ncol, dist_dtype, caller, rounds_out);
+        break;
+      case GG_FLOAT64:
+        rc = sssp_column<double>(ctx, A, sources[q] - 1, (double*)dcol, (double*)ncol, dist_dtype, caller, rounds_out);
+        break;
+      default:
+        rc = set_error(GG_ERR_TYPE, "unsupported distance type");
+    }
+    if (rc) return rc;
+  }
+  return GG_OK;
+}
+
+}  // extern "C"

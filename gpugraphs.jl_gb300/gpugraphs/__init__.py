@@ -1,0 +1,32 @@
+"""gpugraphs -- Python host mirror of GPUGraphs.jl's API over libgpugraphs.so, the
+hand-written sm_103a (GB300) implementation of its semiring sparse kernels and
+graph algorithms.
+
+Julia's in-place ``f!`` functions are spelled ``f_`` here (gpu_spmv_, bfs_distances_,
+...); names, arguments, 1-based indices and raised errors otherwise follow the
+reference's exports (src/GPUGraphs.jl:25-51)."""
+from .algebra import (GPUGraphs_add, GPUGraphs_any, GPUGraphs_band, GPUGraphs_bor,
+                      GPUGraphs_bxor, GPUGraphs_first, GPUGraphs_firsti, GPUGraphs_firstj,
+                      GPUGraphs_land, GPUGraphs_lor, GPUGraphs_max, GPUGraphs_min,
+                      GPUGraphs_minus, GPUGraphs_mul, GPUGraphs_pair, GPUGraphs_rminus,
+                      GPUGraphs_safe_add, GPUGraphs_second, GPUGraphs_secondi,
+                      GPUGraphs_secondj, monoid_absorb, monoid_neutral)
+from .algorithms import (bfs_distances, bfs_distances_, bfs_parents, bfs_parents_,
+                         shortest_path, shortest_path_)
+from .errors import (ArgumentError, BoundsError, DimensionMismatch, GPUGraphsError,
+                     SpmmAssertionError, UnsupportedError)
+from .ops import gpu_spmm_, gpu_spmv_, synchronize
+from .storage import (AbstractSparseGPUMatrix, SparseGPUMatrixCSR, SparseGPUMatrixSELL,
+                      sprand_gpu)
+
+__all__ = [
+    "AbstractSparseGPUMatrix", "SparseGPUMatrixCSR", "SparseGPUMatrixSELL", "gpu_spmv_",
+    "gpu_spmm_", "sprand_gpu", "bfs_distances", "bfs_distances_", "bfs_parents",
+    "bfs_parents_", "shortest_path", "shortest_path_", "monoid_neutral", "monoid_absorb", "synchronize",
+    "GPUGraphs_add", "GPUGraphs_safe_add", "GPUGraphs_mul", "GPUGraphs_second",
+    "GPUGraphs_band", "GPUGraphs_bor", "GPUGraphs_any", "GPUGraphs_secondi", "GPUGraphs_max",
+    "GPUGraphs_min", "GPUGraphs_first", "GPUGraphs_pair", "GPUGraphs_minus", "GPUGraphs_rminus",
+    "GPUGraphs_lor", "GPUGraphs_land", "GPUGraphs_bxor", "GPUGraphs_firsti", "GPUGraphs_firstj",
+    "GPUGraphs_secondj", "ArgumentError", "DimensionMismatch", "BoundsError",
+    "UnsupportedError", "SpmmAssertionError", "GPUGraphsError",
+]

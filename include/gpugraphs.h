@@ -185,6 +185,76 @@ int gg_spmm(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* C, 
             int64_t ldb, int64_t k, int layout, const void* mask, int mask_dtype,
             int64_t mask_len, int64_t range_lo, int64_t range_hi);
 
+/* ---- graph algorithms ------------------------------------------------------- */
+
+/*
+ * Replaces bfs_distances!(A_T, source, dist, curr, next, to_explore)
+ * (src/algorithms/bfs.jl:31-73).  A_T is the transposed adjacency matrix (row v lists
+ * the in-neighbours of v); an edge counts when its stored value is odd / true, as the
+ * reference's band(A[v,u], curr[u]) test does.  Writes dist[v] = hop level for every
+ * reached vertex (dist[source] = 0) and leaves the other entries untouched, so the
+ * caller pre-fills dist with typemax(Int32) like bfs_distances (bfs.jl:16-18).
+ * Synchronous (returns after the search).  levels_out (may be NULL): levels searched.
+ */
+int gg_bfs_levels(gg_ctx* ctx, const gg_mat* A_T, int64_t source, int32_t* dist, int64_t n,
+                  int64_t* levels_out);
+
+/*
+ * Replaces bfs_parents!(A_T, source, parents, curr, next, to_explore)
+ * (src/algorithms/bfs.jl:135-183).  parents[source] = 0; every reached vertex gets a
+ * 1-based in-neighbour one level closer to the source, chosen by `rule`
+ * (GG_PARENT_FORMAT_DEFAULT: first in storage order for CSR, largest index for SELL,
+ * as the reference's kernels choose); other entries are untouched.  Every stored edge
+ * counts, whatever its value (GPUGraphs_secondi ignores A's values).  Synchronous.
+ */
+int gg_bfs_parents(gg_ctx* ctx, const gg_mat* A_T, int64_t source, int32_t* parents, int64_t n,
+                   int rule, int64_t* levels_out);
+
+/*
+ * Replaces shortest_path(A_T, source | sources) and shortest_path!(...)
+ * (src/algorithms/shortest_path.jl:12-161): the fixpoint of
+ *   next[v] = min(next[v], min_u safe_add(A_T[v,u], dist[u]))
+ * for each of the nsources (1-based, host array) columns of dist (n x nsources,
+ * column-major, leading dimension ld, element type Int32 for Bool A_T, else eltype).
+ * next == NULL: dist is initialised here (typemax, 0 at the source) -- the
+ * non-mutating form.  next != NULL: the caller's dist / next are the starting
+ * iterates, sources are set to 0 in both, and both hold the result on return -- the
+ * in-place form.  Non-negative weights use a frontier Bellman-Ford (same fixpoint);
+ * negative or NaN weights run the reference's Jacobi rounds and return
+ * GG_ERR_NOT_CONVERGED after n+1 rounds without convergence.  Synchronous.
+ * rounds_out (may be NULL): relaxation rounds used, summed over sources.
+ */
+int gg_sssp(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, int64_t nsources, void* dist,
+            void* next, int dist_dtype, int64_t ld, int64_t* rounds_out);
+
+/* ---- seeded synthetic inputs (no reference counterpart: the reference's benchmark
+ *      draws its inputs with Julia's sprand / Graphs.jl generators,
+ *      benchmark/benchmarks.jl:57-63,100-104) ------------------------------------ */
+
+enum {
+  GG_W_PATTERN = 0,   /* Bool true */
+  GG_W_U01_F32 = 1,   /* Float32 uniform [0, 1) */
+  GG_W_INT_1_255 = 2, /* Int32 uniform 1..255 */
+  GG_W_F32_1_10 = 3   /* Float32 uniform [1, 10) */
+};
+
+/*
+ * Edge lists written to device arrays (1-based vertex ids, generation order).
+ * Edge e draws its random numbers from splitmix64(splitmix64(seed) + 64*e + j), so
+ * any edge can be regenerated alone.  weights may be NULL.
+ * R-MAT: 2^scale vertices, quadrant probabilities a, b, c, 1-a-b-c.
+ * Erdos-Renyi: uniform (src, dst) pairs over n vertices.
+ * Grid: H x W 4-neighbour lattice, H*(W-1) + (H-1)*W undirected edges.
+ */
+int gg_gen_rmat_edges(gg_ctx* ctx, int scale, int64_t nedges, double a, double b, double c,
+                      uint64_t seed, int weight_kind, int32_t* src, int32_t* dst, void* weights);
+int gg_gen_er_edges(gg_ctx* ctx, int64_t n, int64_t nedges, uint64_t seed, int weight_kind,
+                    int32_t* src, int32_t* dst, void* weights);
+int gg_gen_grid_edges(gg_ctx* ctx, int64_t H, int64_t W, uint64_t seed, int weight_kind,
+                      int32_t* src, int32_t* dst, void* weights);
+/* Dense Float32 vector, element i uniform [0, 1) from the same stream definition. */
+int gg_gen_uniform_f32(gg_ctx* ctx, int64_t len, uint64_t seed, float* out);
+
 #ifdef __cplusplus
 }
 #endif

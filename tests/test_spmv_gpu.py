@@ -1,0 +1,383 @@
+"""GPU parity of gpu_spmv_ / gpu_spmm_ and the storage types against the CPU oracle,
+the reference's golden vectors and an FP64 oracle.
+
+Tolerance: integer, Bool, min/max/any/or semirings and every row folded in storage
+order are compared bit for bit.  Float32 plus-times rows that the kernels reduce in
+parallel (long rows, masked/range rows) are compared with rtol 1e-5 against the
+FP64 product (the reference's own isapprox tests use rtol ~3.4e-4)."""
+import itertools
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+import gpugraphs as G
+from gpugraphs import core
+from oracle import oracle as O
+from helpers import csr_from_scipy, golden_json, sprand_csr
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-5
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def nan_equal(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    if np.issubdtype(a.dtype, np.floating):
+        return np.array_equal(np.isnan(a), np.isnan(b)) and (a[~np.isnan(a)] == b[~np.isnan(b)]).all()
+    return np.array_equal(a, b)
+
+
+def power_law_csr(m, seed, dtype=np.float32):
+    """Rows with 0 .. ~5000 entries: exercises short-row blocks, empty rows and
+    long-row segments."""
+    rng = np.random.default_rng(seed)
+    deg = np.minimum((rng.pareto(1.2, m) * 3).astype(np.int64), m // 2)
+    deg[:3] = [m // 2, min(3000, m - 1), min(300, m - 1)]
+    deg[rng.random(m) < 0.2] = 0
+    rows, cols = [], []
+    for r in range(m):
+        c = rng.choice(m, deg[r], replace=False)
+        rows.append(np.full(deg[r], r))
+        cols.append(c)
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    vals = rng.random(len(rows)).astype(dtype)
+    A = sp.csr_matrix((vals, (rows, cols)), shape=(m, m))
+    return csr_from_scipy(A) + (A,)
+
+
+# --------------------------------------------------------------------------------
+# storage
+# --------------------------------------------------------------------------------
+
+def test_csr_fields_roundtrip():
+    """test/structs.jl:30-78: fields equal the reference arrays, getindex agrees."""
+    rowptr, colval, nzval, A = sprand_csr(10, 10, 0.5, seed=1)
+    for B in (G.SparseGPUMatrixCSR(10, 10, rowptr, colval, nzval),
+              G.SparseGPUMatrixCSR.from_scipy(A),
+              G.SparseGPUMatrixCSR.from_dense(A.toarray()),
+              G.SparseGPUMatrixCSR(10, 10, dev(rowptr), dev(colval), dev(nzval))):
+        assert B.size() == (10, 10) and B.length() == 100 and B.nnz() == A.nnz
+        assert (host(B.rowptr) == rowptr).all()
+        assert (host(B.colval) == colval).all()
+        assert (host(B.nzval) == nzval).all()
+        D = A.toarray()
+        for i, j in [(1, 1), (3, 7), (10, 10), (5, 2)]:
+            assert B[i, j] == D[i - 1, j - 1]
+        with pytest.raises(G.BoundsError):
+            B[11, 1]
+    E = G.SparseGPUMatrixCSR.empty(0, 0)
+    assert E.size() == (0, 0) and E.nnz() == 0
+
+
+def test_csr_constructor_errors_golden():
+    """test/structs.jl:79-149: every case throws ArgumentError."""
+    for case in golden_json("csr_errors.json")["cases"]:
+        with pytest.raises(G.ArgumentError):
+            G.SparseGPUMatrixCSR(case["m"], case["n"], np.array(case["rowptr"]),
+                                 np.array(case["colval"]), np.array(case["nzval"], np.float32))
+    # device arrays go through the library's own checks
+    case = golden_json("csr_errors.json")["cases"][5]
+    with pytest.raises(G.ArgumentError):
+        G.SparseGPUMatrixCSR(3, 10, dev(np.array(case["rowptr"], np.int32)),
+                             dev(np.array(case["colval"], np.int32)),
+                             dev(np.array(case["nzval"], np.float32)))
+
+
+def test_sell_layout_golden_gpu():
+    """test/structs.jl:176-207 through the device SELL builder."""
+    g = golden_json("sell_4x4.json")
+    D = np.array(g["dense"], np.float32)
+    for S in (G.SparseGPUMatrixSELL(sp.csc_matrix(D)), G.SparseGPUMatrixSELL(D)):
+        assert S.size() == (4, 4) and S.nnz() == g["nnz"] and S.slice_size == 4
+        assert host(S.slice_ptr).tolist() == g["slice_ptr"]
+        assert host(S.colval).tolist() == g["colval"]
+        assert host(S.nzval).tolist() == g["nzval"]
+        for i in range(1, 5):
+            for j in range(1, 5):
+                assert S[i, j] == D[i - 1, j - 1]
+
+
+@pytest.mark.parametrize("C,sigma", [(32, 1), (8, 1), (16, 64), (32, 1024), (7, 3)])
+def test_sell_layout_matches_oracle(C, sigma):
+    rowptr, colval, nzval, A = power_law_csr(600, 2)
+    ref = O.sell_build(600, rowptr, colval, nzval, slice_size=C, sigma=sigma)
+    S = G.SparseGPUMatrixSELL(G.SparseGPUMatrixCSR(600, 600, rowptr, colval, nzval), C, sigma)
+    assert S.n_stored == ref["n_stored"] and S.nslices == ref["nslices"]
+    assert (host(S.slice_ptr) == ref["slice_ptr"]).all()
+    assert (host(S.colval) == ref["colval"]).all()
+    assert (host(S.nzval) == ref["nzval"]).all()
+    assert (host(S.perm) == ref["perm"]).all()
+
+
+# --------------------------------------------------------------------------------
+# plus-times Float32 (the headline path)
+# --------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("m,p,seed", [(10, 0.5, 1), (1000, 0.2, 2)])
+def test_spmv_plus_times_reference_sizes(m, p, seed):
+    """test/spmv.jl:10-70 sizes; short rows are folded in storage order -> bit-exact."""
+    rowptr, colval, nzval, A = sprand_csr(m, m, p, seed=seed)
+    x = np.random.default_rng(seed).random(m, dtype=np.float32)
+    yo = np.zeros(m, np.float32)
+    O.csr_spmv(m, m, rowptr, colval, nzval, yo, x)
+    B = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nzval)
+    S = G.SparseGPUMatrixSELL(B)
+    ref64 = A.astype(np.float64) @ x.astype(np.float64)
+    for M in (B, S):
+        y = torch.zeros(m, dtype=torch.float32, device="cuda")
+        G.gpu_spmv_(y, M, dev(x))
+        yh = host(y)
+        np.testing.assert_allclose(yh, ref64, rtol=RTOL, atol=1e-6)
+        if m <= 1000 and (np.diff(rowptr) <= 256).all():
+            assert (yh == yo).all()
+
+
+def test_spmv_plus_times_long_rows():
+    m = 6000
+    rowptr, colval, nzval, A = power_law_csr(m, 3)
+    x = np.random.default_rng(3).random(m, dtype=np.float32)
+    yo = np.zeros(m, np.float32)
+    O.csr_spmv(m, m, rowptr, colval, nzval, yo, x)
+    ref64 = A.astype(np.float64) @ x.astype(np.float64)
+    B = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nzval)
+    deg = np.diff(rowptr)
+    for rep in range(3):  # the long-row counters reset themselves between launches
+        y = torch.full((m,), -1.0, dtype=torch.float32, device="cuda")
+        G.gpu_spmv_(y, B, dev(x))
+        yh = host(y)
+        short = deg <= 256
+        assert (yh[short] == yo[short]).all()
+        np.testing.assert_allclose(yh, ref64, rtol=RTOL, atol=1e-6)
+    for C, sigma in ((32, 1), (8, 256)):
+        S = G.SparseGPUMatrixSELL(B, C, sigma)
+        y = torch.zeros(m, dtype=torch.float32, device="cuda")
+        G.gpu_spmv_(y, S, dev(x))
+        assert (host(y) == yo).all()  # SELL folds every row in storage order
+
+
+def test_spmv_masked_and_range():
+    """test/spmv.jl:72-170 plus the range variants (CSR.jl:224-313, SELL.jl:176-283)."""
+    m = 1000
+    rowptr, colval, nzval, A = sprand_csr(m, m, 0.2, seed=4)
+    rng = np.random.default_rng(4)
+    x = rng.random(m, dtype=np.float32)
+    mask = rng.random(m) < 0.5
+    B = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nzval)
+    S = G.SparseGPUMatrixSELL(B, 32, 64)
+    ref64 = (A.astype(np.float64) @ x.astype(np.float64))
+    for M in (B, S):
+        for mk, rg in ((mask, None), (None, range(100, 301)), (mask, (5, 900)), (None, range(7, 7))):
+            y = torch.full((m,), -3.0, dtype=torch.float32, device="cuda")
+            G.gpu_spmv_(y, M, dev(x), mask=None if mk is None else dev(mk), range=rg)
+            sel = np.ones(m, bool) if mk is None else mk.copy()
+            if rg is not None:
+                lo, hi = (rg.start, rg.stop - 1) if isinstance(rg, range) else rg
+                r = np.zeros(m, bool)
+                r[lo - 1:hi] = True
+                sel &= r
+            yh = host(y)
+            assert (yh[~sel] == -3.0).all()
+            np.testing.assert_allclose(yh[sel], ref64[sel], rtol=RTOL, atol=1e-6)
+
+
+# --------------------------------------------------------------------------------
+# generic semirings: bit parity with the oracle (status codes included)
+# --------------------------------------------------------------------------------
+
+SEMIRINGS = [
+    (O.MUL, O.ADD, O.SECOND), (O.SAFE_ADD, O.MIN, O.MIN), (O.BAND, O.BOR, O.SECOND),
+    (O.SECONDI, O.ANY, O.SECOND), (O.MUL, O.MAX, O.SECOND), (O.PAIR, O.ADD, O.SECOND),
+    (O.FIRST, O.MIN, O.MAX), (O.SECOND, O.ANY, O.SECOND), (O.MINUS, O.MAX, O.ADD),
+    (O.FIRSTI, O.MIN, O.SECOND), (O.FIRSTJ, O.MAX, O.SECOND), (O.SECONDJ, O.ADD, O.SECOND),
+    (O.LAND, O.LOR, O.SECOND), (O.MUL, O.MUL, O.SECOND), (O.BXOR, O.BAND, O.MIN),
+    (O.ADD, O.SAFE_ADD, O.SECOND), (O.RMINUS, O.MIN, O.FIRST), (O.MUL, O.BXOR, O.SECOND),
+]
+TYPES = [(np.bool_, np.bool_), (np.int32, np.int32), (np.int32, np.bool_),
+         (np.float32, np.float32), (np.int64, np.int32), (np.float64, np.float32),
+         (np.bool_, np.int32), (np.float32, np.int32)]
+OPS = {v.code: v for v in G.algebra.OPERATORS.values()}
+STATUS_EXC = {O.TYPE: G.ArgumentError, O.UNSUPPORTED: G.UnsupportedError}
+
+
+def _values(rng, n, dt):
+    if dt == np.bool_:
+        return rng.random(n) < 0.6
+    if np.issubdtype(dt, np.integer):
+        v = rng.integers(-4, 9, n).astype(dt)
+        v[rng.random(n) < 0.05] = np.iinfo(dt).max
+        return v
+    v = (rng.random(n) * 4 - 1).astype(dt)
+    v[rng.random(n) < 0.05] = np.inf
+    return v
+
+
+def _run_gpu(M, mul, add, accum, y0, x, mask, rng_):
+    y = dev(y0)
+    kw = dict(mul=OPS[mul], add=OPS[add], accum=OPS[accum])
+    if mask is not None:
+        kw["mask"] = dev(mask)
+    if rng_ is not None:
+        kw["range"] = rng_
+    # the C ABI accepts y wider than promote_type; call it directly to test the kernels
+    L = core.lib()
+    mp = core.ptr(kw["mask"]) if mask is not None else None
+    lo, hi = rng_ if rng_ is not None else (0, 0)
+    rc = L.gg_spmv(core.ctx(), M.handle, mul, add, accum, core.ptr(y), core.dtype_code(y),
+                   y.numel(), core.ptr(kw.get("x", dev(x))), core.dtype_code(torch.from_numpy(x)),
+                   x.size, mp, 0 if mask is None else core.dtype_code(torch.from_numpy(mask)),
+                   0 if mask is None else mask.size, lo, hi)
+    return rc, host(y)
+
+
+@pytest.mark.parametrize("fmt", ["csr", "sell"])
+def test_spmv_semiring_grid(fmt):
+    rng = np.random.default_rng(7)
+    m = 180
+    base = sp.random(m, m, density=0.06, random_state=rng, format="csr")
+    base.sort_indices()
+    rowptr = (base.indptr + 1).astype(np.int32)
+    colval = (base.indices + 1).astype(np.int32)
+    mask = rng.random(m) < 0.5
+    fails = []
+    for (tv, tx), (mul, add, accum) in itertools.product(TYPES, SEMIRINGS):
+        nz = _values(rng, len(colval), tv)
+        x = _values(rng, m, tx)
+        ty = np.result_type(tv, tx) if not (tv == np.bool_ and tx == np.bool_) else np.bool_
+        if mul in (O.SECONDI, O.FIRSTJ) and ty == np.bool_:
+            ty = np.int32
+        if mul in (O.FIRSTI, O.SECONDJ) and np.dtype(ty).itemsize < 8:
+            ty = np.int64 if not np.issubdtype(ty, np.floating) else np.float64
+        y0 = _values(rng, m, ty)
+        Bc = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nz)
+        M = Bc if fmt == "csr" else G.SparseGPUMatrixSELL(Bc, 8, 4)
+        S = O.sell_build(m, rowptr, colval, nz, 8, 4)
+        for mk, rg in ((None, None), (mask, None), (None, (20, 150)), (mask, (3, 177))):
+            yo = y0.copy()
+            if fmt == "csr":
+                st = O.csr_spmv(m, m, rowptr, colval, nz, yo, x, mul, add, accum, mk, rg)
+            else:
+                st = O.sell_spmv(S, m, yo, x, mul, add, accum, mk, rg)
+            rc, yg = _run_gpu(M, mul, add, accum, y0, x, mk, rg)
+            tag = (fmt, np.dtype(tv).name, np.dtype(tx).name, mul, add, accum, mk is not None, rg)
+            if rc != st:
+                fails.append(("status", tag, rc, st))
+                continue
+            if st != O.OK:
+                continue
+            float_add = np.issubdtype(np.result_type(tv, tx), np.floating) and add in (O.ADD, O.SAFE_ADD, O.MUL)
+            parallel = fmt == "csr" and (mk is not None or rg is not None or mul == O.FIRSTI)
+            if float_add and parallel:
+                ok = np.allclose(yg.astype(np.float64), yo.astype(np.float64), rtol=RTOL,
+                                 atol=1e-6, equal_nan=True)
+            else:
+                ok = nan_equal(yg, yo)
+            if not ok:
+                fails.append(("value", tag))
+    assert not fails, fails[:10]
+
+
+def test_spmv_errors():
+    """_validate_args (src/spmv/CSR.jl:358-408) error classes."""
+    rowptr, colval, nzval, A = sprand_csr(20, 30, 0.3, seed=5)
+    B = G.SparseGPUMatrixCSR(20, 30, rowptr, colval, nzval)
+    x = torch.ones(30, dtype=torch.float32, device="cuda")
+    y = torch.zeros(20, dtype=torch.float32, device="cuda")
+    with pytest.raises(G.DimensionMismatch):
+        G.gpu_spmv_(y, B, torch.ones(29, device="cuda"))
+    with pytest.raises(G.DimensionMismatch):
+        G.gpu_spmv_(torch.zeros(21, device="cuda"), B, x)
+    with pytest.raises(G.ArgumentError):
+        G.gpu_spmv_(torch.zeros(20, dtype=torch.int32, device="cuda"), B, x)
+    with pytest.raises(G.ArgumentError):
+        G.gpu_spmv_(y, B, torch.ones(30))
+    with pytest.raises(G.DimensionMismatch):
+        G.gpu_spmv_(y, B, x, mask=torch.ones(19, dtype=torch.bool, device="cuda"))
+    with pytest.raises(G.UnsupportedError):
+        G.gpu_spmv_(y, B, x, mul=G.GPUGraphs_band, add=G.GPUGraphs_bor)
+    with pytest.raises(G.ArgumentError):
+        G.gpu_spmv_(y, B, x, mul=lambda *a: 0)
+
+
+# --------------------------------------------------------------------------------
+# SpMM
+# --------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_spmm_plus_times(layout):
+    """test/spmm.jl:10-73 sizes: each (row, column) is folded in storage order, so the
+    result equals the reference's sequential fold bit for bit."""
+    for m, k, p, seed in ((10, 5, 0.5, 1), (1000, 20, 0.2, 2), (700, 40, 0.05, 3)):
+        rowptr, colval, nzval, A = sprand_csr(m, m, p, seed=seed)
+        Bh = np.random.default_rng(seed).random((m, k), dtype=np.float32)
+        Bh = np.asfortranarray(Bh) if layout == 0 else np.ascontiguousarray(Bh)
+        Co = np.zeros((m, k), np.float32, order="F" if layout == 0 else "C")
+        O.csr_spmm(m, rowptr, colval, nzval, Co, Bh, layout=layout)
+        ref64 = A.astype(np.float64) @ Bh.astype(np.float64)
+        Bc = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nzval)
+        for M in (Bc, G.SparseGPUMatrixSELL(Bc)):
+            if layout == 0:
+                Bd = torch.from_numpy(np.ascontiguousarray(Bh.T)).cuda().T
+                Cd = torch.zeros((k, m), dtype=torch.float32, device="cuda").T
+            else:
+                Bd = dev(Bh)
+                Cd = torch.zeros((m, k), dtype=torch.float32, device="cuda")
+            G.gpu_spmm_(Cd, M, Bd)
+            Ch = host(Cd)
+            np.testing.assert_allclose(Ch, ref64, rtol=RTOL, atol=1e-5)
+            assert (Ch == Co).all()
+
+
+def test_spmm_min_plus_masked_range():
+    m, k = 300, 33
+    rng = np.random.default_rng(8)
+    base = sp.random(m, m, density=0.05, random_state=rng, format="csr")
+    base.sort_indices()
+    rowptr = (base.indptr + 1).astype(np.int32)
+    colval = (base.indices + 1).astype(np.int32)
+    nz = rng.integers(1, 20, len(colval)).astype(np.int32)
+    Bh = rng.integers(0, 100, (m, k)).astype(np.int32)
+    Bh[rng.random((m, k)) < 0.3] = np.iinfo(np.int32).max
+    mask = rng.random(m) < 0.5
+    Bc = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nz)
+    S = O.sell_build(m, rowptr, colval, nz, 32, 16)
+    for fmt, M in (("csr", Bc), ("sell", G.SparseGPUMatrixSELL(Bc, 32, 16))):
+        for layout in (0, 1):
+            for mk, rg in ((None, None), (mask, None), (None, (10, 250))):
+                C0 = rng.integers(0, 50, (m, k)).astype(np.int32)
+                C0 = np.asfortranarray(C0) if layout == 0 else np.ascontiguousarray(C0)
+                Bl = np.asfortranarray(Bh) if layout == 0 else np.ascontiguousarray(Bh)
+                Co = C0.copy(order="K")
+                if fmt == "csr":
+                    O.csr_spmm(m, rowptr, colval, nz, Co, Bl, layout, O.SAFE_ADD, O.MIN, O.MIN, mk, rg)
+                else:
+                    O.sell_spmm(S, Co, Bl, layout, O.SAFE_ADD, O.MIN, O.MIN, mk, rg)
+                if layout == 0:
+                    Bd = torch.from_numpy(np.ascontiguousarray(Bl.T)).cuda().T
+                    Cd = torch.from_numpy(np.ascontiguousarray(C0.T)).cuda().T
+                else:
+                    Bd, Cd = dev(Bl), dev(C0)
+                G.gpu_spmm_(Cd, M, Bd, mul=G.GPUGraphs_safe_add, add=G.GPUGraphs_min,
+                            accum=G.GPUGraphs_min, mask=None if mk is None else dev(mk), range=rg)
+                assert (host(Cd) == Co).all(), (fmt, layout, mk is not None, rg)
+
+
+def test_spmm_assertions():
+    rowptr, colval, nzval, A = sprand_csr(20, 30, 0.3, seed=5)
+    B = G.SparseGPUMatrixCSR(20, 30, rowptr, colval, nzval)
+    with pytest.raises(G.SpmmAssertionError):
+        G.gpu_spmm_(torch.zeros((20, 4), device="cuda"), B, torch.zeros((29, 4), device="cuda"))
+    with pytest.raises(G.SpmmAssertionError):
+        G.gpu_spmm_(torch.zeros((20, 4), device="cuda"), B, torch.zeros((30, 5), device="cuda"))
+    with pytest.raises(G.SpmmAssertionError):
+        G.gpu_spmm_(torch.zeros((20, 4), device="cuda"), B, torch.zeros((30, 4), device="cuda"),
+                    mask=torch.ones(20, device="cuda"), range=(1, 3))
