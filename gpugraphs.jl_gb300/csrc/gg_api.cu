@@ -175,6 +175,13 @@ static void free_mat_storage(gg_mat* A) {
     A->blocks = nullptr;
   }
   free_graph_aux(A);
+  if (A->sellplan) {
+    cudaFree(A->sellplan->items);
+    cudaFree(A->sellplan->multi);
+    cudaFree(A->sellplan->partials);
+    delete A->sellplan;
+    A->sellplan = nullptr;
+  }
 }
 
 static int blocks_for(gg_ctx* ctx, int64_t work) {

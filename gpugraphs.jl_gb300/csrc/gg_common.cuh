@@ -306,15 +306,16 @@ template <> __device__ __forceinline__ uint8_t shfl_xor<uint8_t>(uint8_t v, int 
 // ---------------------------------------------------------------------------------
 
 // Row-block partition of a CSR matrix for the SpMV / SpMM row-block kernels.
-// Regular blocks: contiguous rows [first, last) holding at most kBlockNnz stored
-// entries and kBlockRows rows.  Long rows (more than kBlockNnz entries) are cut into
+// Regular blocks: contiguous short rows (at most kShortRow entries each) [first,
+// last) holding at most kBlockNnz stored entries and kBlockRows rows.  Longer rows
+// are handled one warp per segment; rows of more than kSegNnz entries are cut into
 // segments of kSegNnz entries; the warp that finishes a row's last segment combines
 // the partials in segment order.
 struct RowBlocks {
   int64_t nblocks = 0;      // regular blocks
   int64_t nsegs = 0;        // long-row segments
   int64_t nlong = 0;        // long rows
-  int2* blocks = nullptr;   // [nblocks] (first row, last row) 0-based, half-open
+  int4* blocks = nullptr;   // [nblocks] (first row, end row, first entry, end entry) 0-based
   int4* segs = nullptr;     // [nsegs] (row, k_begin, k_end, long-row index) 0-based
   int32_t* long_first_seg = nullptr;  // [nlong + 1] first segment of each long row
   int32_t* long_rows = nullptr;       // [nlong] row id
@@ -325,9 +326,21 @@ struct RowBlocks {
 
 struct GraphAux;  // graph-algorithm analysis (gg_graph.cu)
 
+// Work list of a SELL matrix: slices cut into chunks of at most kSellChunk stored
+// columns.  items: (slice, first column, end column, partial index or -1 when the
+// slice is a single chunk); multi: (slice, first partial index, number of chunks).
+struct SellPlan {
+  int64_t nitems = 0, nmulti = 0;
+  int4* items = nullptr;
+  int4* multi = nullptr;
+  void* partials = nullptr;  // [npartials * C] accumulators (8 bytes each)
+};
+static const int kSellChunk = 512;
+
 static const int kBlockNnz = 256;
+static const int kShortRow = 32;
 static const int kBlockRows = 256;
-static const int kSegNnz = 2048;
+static const int kSegNnz = 4096;
 
 }  // namespace gg
 
@@ -359,6 +372,7 @@ struct gg_mat {
   // lazily built analysis
   gg::RowBlocks* blocks = nullptr;
   gg::GraphAux* aux = nullptr;
+  gg::SellPlan* sellplan = nullptr;
   int64_t max_row_len = -1;
 };
 
@@ -370,5 +384,6 @@ int check_semiring(int tv, int tx, int ty, int mul, int add, int accum, int* tc_
 int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, void* y, int ty,
                   const void* x, int tx, const void* mask, int tmask, int64_t lo, int64_t hi);
 int build_row_blocks(gg_ctx* ctx, gg_mat* A);
+int build_sell_plan(gg_ctx* ctx, gg_mat* A);
 int row_stats(gg_ctx* ctx, gg_mat* A);
 }  // namespace gg

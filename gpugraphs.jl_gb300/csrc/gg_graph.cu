@@ -456,6 +456,20 @@ __global__ void k_queue_to_bitmap(const int32_t* q, int64_t nf, unsigned* bm) {
   }
 }
 
+// light frontier vertices (<= kLightDeg out-edges) are processed kBatch per thread
+// with all their edge loads, then all their atomics, in flight together; heavier
+// vertices go to a warp-per-vertex pass.  This keeps the per-level dependent chain
+// at a few memory round trips, which bounds high-diameter searches.
+static const int kLightDeg = 4;
+static const int kBatch = 4;
+
+__device__ __forceinline__ void small_append(int32_t w, int32_t* nxt, int32_t* qg, int32_t cap,
+                                             int32_t* s_nn) {
+  const int32_t pos = atomicAdd(s_nn, 1);
+  if (pos < cap) nxt[pos] = w;
+  else qg[pos] = w;
+}
+
 // Small-frontier BFS: one CTA runs top-down levels back to back while the frontier
 // fits in shared memory.  qg holds the starting frontier (nf0 <= cap) and receives
 // the overflowing frontier when it grows past cap.  Out: ctr->nf = size of the last
@@ -469,7 +483,7 @@ __global__ void __launch_bounds__(1024)
   int32_t* nxt = smem + cap;
   int32_t* heavy = smem + 2 * cap;
   __shared__ int32_t s_nn, s_nh;
-  __shared__ unsigned long long s_mf;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int32_t i = threadIdx.x; i < nf0; i += blockDim.x) cur[i] = qg[i];
   int32_t nf = nf0, level = level0;
   __syncthreads();
@@ -478,44 +492,57 @@ __global__ void __launch_bounds__(1024)
     if (threadIdx.x == 0) {
       s_nn = 0;
       s_nh = 0;
-      s_mf = 0;
     }
     __syncthreads();
-    // light vertices: one thread each; heavy ones are deferred to the whole block
-    for (int32_t i = threadIdx.x; i < nf; i += blockDim.x) {
-      const int32_t u = cur[i];
-      const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
-      if (k1 - k0 > 32) {
-        heavy[atomicAdd(&s_nh, 1)] = u;
-        continue;
+    for (int32_t i0 = threadIdx.x; i0 < nf; i0 += blockDim.x * kBatch) {
+      int32_t k0[kBatch], k1[kBatch];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int32_t i = i0 + b * (int32_t)blockDim.x;
+        k0[b] = 0;
+        k1[b] = 0;
+        if (i < nf) {
+          const int32_t u = cur[i];
+          k0[b] = __ldg(prow + u);
+          k1[b] = __ldg(prow + u + 1);
+          if (k1[b] - k0[b] > kLightDeg) {
+            heavy[atomicAdd(&s_nh, 1)] = u;
+            k1[b] = k0[b];
+          }
+        }
       }
-      for (int32_t k = k0; k < k1; ++k) {
-        const int32_t w = __ldg(pcol + k);
-        const unsigned bit = 1u << (w & 31);
-        if (__ldcg(visited + (w >> 5)) & bit) continue;
-        if (atomicOr(visited + (w >> 5), bit) & bit) continue;
-        dist[w] = level;
-        const int32_t pos = atomicAdd(&s_nn, 1);
-        if (pos < cap) nxt[pos] = w;
-        else qg[pos] = w;
-        atomicAdd(&s_mf, (unsigned long long)(__ldg(prow + w + 1) - __ldg(prow + w)));
-      }
+      int32_t w[kBatch][kLightDeg];
+      unsigned old[kBatch][kLightDeg];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b)
+#pragma unroll
+        for (int j = 0; j < kLightDeg; ++j)
+          w[b][j] = (k0[b] + j < k1[b]) ? __ldg(pcol + k0[b] + j) : -1;
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b)
+#pragma unroll
+        for (int j = 0; j < kLightDeg; ++j)
+          old[b][j] = (w[b][j] >= 0) ? atomicOr(visited + (w[b][j] >> 5), 1u << (w[b][j] & 31)) : ~0u;
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b)
+#pragma unroll
+        for (int j = 0; j < kLightDeg; ++j)
+          if (w[b][j] >= 0 && !((old[b][j] >> (w[b][j] & 31)) & 1u)) {
+            dist[w[b][j]] = level;
+            small_append(w[b][j], nxt, qg, cap, &s_nn);
+          }
     }
     __syncthreads();
     const int32_t nh = s_nh;
-    for (int32_t h = 0; h < nh; ++h) {
+    for (int32_t h = warp; h < nh; h += nwarps) {
       const int32_t u = heavy[h];
       const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
-      for (int32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+      for (int32_t k = k0 + lane; k < k1; k += 32) {
         const int32_t w = __ldg(pcol + k);
         const unsigned bit = 1u << (w & 31);
-        if (__ldcg(visited + (w >> 5)) & bit) continue;
         if (atomicOr(visited + (w >> 5), bit) & bit) continue;
         dist[w] = level;
-        const int32_t pos = atomicAdd(&s_nn, 1);
-        if (pos < cap) nxt[pos] = w;
-        else qg[pos] = w;
-        atomicAdd(&s_mf, (unsigned long long)(__ldg(prow + w + 1) - __ldg(prow + w)));
+        small_append(w, nxt, qg, cap, &s_nn);
       }
     }
     __syncthreads();
@@ -525,7 +552,7 @@ __global__ void __launch_bounds__(1024)
         for (int32_t i = threadIdx.x; i < cap; i += blockDim.x) qg[i] = nxt[i];
       if (threadIdx.x == 0) {
         ctr->nf = (unsigned long long)nn;
-        ctr->mf = s_mf;
+        ctr->mf = 0;
         ctr->level = (unsigned long long)level;
       }
       return;
@@ -536,6 +563,20 @@ __global__ void __launch_bounds__(1024)
     nf = nn;
     __syncthreads();
   }
+}
+
+// sum of out-degrees of a frontier queue (direction heuristic after the small kernel)
+__global__ void k_queue_degree(const int32_t* __restrict__ prow, const int32_t* __restrict__ q,
+                               int64_t nf, Counters* ctr) {
+  unsigned long long d = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t u = q[i];
+    d += (unsigned long long)(prow[u + 1] - prow[u]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(kFullG, d, o);
+  if ((threadIdx.x & 31) == 0 && d) atomicAdd(&ctr->mf, d);
 }
 
 static const int kSmallCap = 8192;
@@ -595,10 +636,15 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
       GG_CUDA(cudaStreamSynchronize(ctx->stream));
       nf = (int64_t)h->nf;
       level = (int64_t)h->level;
-      mf = (int64_t)h->mf;
       if (nf == 0) break;
+      // the frontier of `level` is in q[cur]; its out-degree sum feeds the heuristic
+      GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+      k_queue_degree<<<gridsz(ctx, nf), 256, 0, ctx->stream>>>(P.rowptr, sc.q[cur], nf, sc.ctr);
+      GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+      GG_CUDA(cudaStreamSynchronize(ctx->stream));
+      mf = (int64_t)h->mf;
       explored += mf;
-      continue;  // frontier of `level` is in q[cur]
+      continue;
     }
     // direction heuristic (Beamer et al.): pull when the frontier's edges outweigh a
     // 1/14 share of the unexplored edges, push again once the frontier is small
@@ -754,6 +800,7 @@ __global__ void __launch_bounds__(1024)
   int32_t* nxt = smem + cap;
   int32_t* heavy = smem + 2 * cap;
   __shared__ int32_t s_nn, s_nh;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int32_t i = threadIdx.x; i < nf0; i += blockDim.x) cur[i] = qg[i];
   int32_t nf = nf0;
   unsigned* ic = inq_a;
@@ -767,43 +814,66 @@ __global__ void __launch_bounds__(1024)
       s_nh = 0;
     }
     __syncthreads();
-    for (int32_t i = threadIdx.x; i < nf; i += blockDim.x) {
-      const int32_t u = cur[i];
-      atomicAnd(ic + (u >> 5), ~(1u << (u & 31)));
-      const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
-      if (k1 - k0 > 32) {
-        heavy[atomicAdd(&s_nh, 1)] = u;
-        continue;
+    for (int32_t i0 = threadIdx.x; i0 < nf; i0 += blockDim.x * kBatch) {
+      int32_t k0[kBatch], k1[kBatch];
+      T du[kBatch];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int32_t i = i0 + b * (int32_t)blockDim.x;
+        k0[b] = 0;
+        k1[b] = 0;
+        du[b] = Lim<T>::max();
+        if (i < nf) {
+          const int32_t u = cur[i];
+          atomicAnd(ic + (u >> 5), ~(1u << (u & 31)));
+          k0[b] = __ldg(prow + u);
+          k1[b] = __ldg(prow + u + 1);
+          if (k1[b] - k0[b] > kLightDeg) {
+            heavy[atomicAdd(&s_nh, 1)] = u;
+            k1[b] = k0[b];
+          } else {
+            du[b] = ld_cg(dist + u);
+          }
+        }
       }
-      const T du = ld_cg(dist + u);
-      for (int32_t k = k0; k < k1; ++k) {
-        const int32_t w = __ldg(pcol + k);
-        const T cand = relax_add(__ldg(pw + k), du);
-        if (!(cand < ld_cg(dist + w))) continue;
-        if (!(cand < atomic_min_t(dist + w, cand))) continue;
-        const unsigned bit = 1u << (w & 31);
-        if (atomicOr(in + (w >> 5), bit) & bit) continue;
-        const int32_t pos = atomicAdd(&s_nn, 1);
-        if (pos < cap) nxt[pos] = w;
-        else qg[pos] = w;
-      }
+      int32_t w[kBatch][kLightDeg];
+      T cand[kBatch][kLightDeg];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b)
+#pragma unroll
+        for (int j = 0; j < kLightDeg; ++j) {
+          const bool ok = k0[b] + j < k1[b];
+          w[b][j] = ok ? __ldg(pcol + k0[b] + j) : -1;
+          cand[b][j] = ok ? relax_add(__ldg(pw + k0[b] + j), du[b]) : Lim<T>::max();
+        }
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b)
+#pragma unroll
+        for (int j = 0; j < kLightDeg; ++j)
+          if (w[b][j] >= 0 && !(cand[b][j] < atomic_min_t(dist + w[b][j], cand[b][j]))) w[b][j] = -1;
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b)
+#pragma unroll
+        for (int j = 0; j < kLightDeg; ++j)
+          if (w[b][j] >= 0) {
+            const unsigned bit = 1u << (w[b][j] & 31);
+            if (!(atomicOr(in + (w[b][j] >> 5), bit) & bit)) small_append(w[b][j], nxt, qg, cap, &s_nn);
+          }
     }
     __syncthreads();
     const int32_t nh = s_nh;
-    for (int32_t h = 0; h < nh; ++h) {
+    for (int32_t h = warp; h < nh; h += nwarps) {
       const int32_t u = heavy[h];
       const T du = ld_cg(dist + u);
       const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
-      for (int32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+      for (int32_t k = k0 + lane; k < k1; k += 32) {
         const int32_t w = __ldg(pcol + k);
         const T cand = relax_add(__ldg(pw + k), du);
         if (!(cand < ld_cg(dist + w))) continue;
         if (!(cand < atomic_min_t(dist + w, cand))) continue;
         const unsigned bit = 1u << (w & 31);
         if (atomicOr(in + (w >> 5), bit) & bit) continue;
-        const int32_t pos = atomicAdd(&s_nn, 1);
-        if (pos < cap) nxt[pos] = w;
-        else qg[pos] = w;
+        small_append(w, nxt, qg, cap, &s_nn);
       }
     }
     __syncthreads();

@@ -99,6 +99,35 @@ struct SRGen {
 };
 
 // ---------------------------------------------------------------------------------
+// streaming loads: read-once matrix data bypasses L1 (keeps L1 for the gathered
+// dense operand) and asks L2 for 256-byte prefetch
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ int32_t ld_stream(const int32_t* p) {
+  int32_t r;
+  asm("ld.global.nc.L1::no_allocate.L2::256B.s32 %0, [%1];" : "=r"(r) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ float ld_stream(const float* p) {
+  float r;
+  asm("ld.global.nc.L1::no_allocate.L2::256B.f32 %0, [%1];" : "=f"(r) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ int4 ld_stream4(const int32_t* p) {
+  int4 r;
+  asm("ld.global.nc.L1::no_allocate.L2::256B.v4.s32 {%0,%1,%2,%3}, [%4];"
+      : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+      : "l"(p));
+  return r;
+}
+__device__ __forceinline__ float4 ld_stream4(const float* p) {
+  float4 r;
+  asm("ld.global.nc.L1::no_allocate.L2::256B.v4.f32 {%0,%1,%2,%3}, [%4];"
+      : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+      : "l"(p));
+  return r;
+}
+
+// ---------------------------------------------------------------------------------
 // (GPUGraphs_mul, GPUGraphs_add, GPUGraphs_second) on Float32: the headline SpMV.
 // The early exit at +Inf follows monoid_absorb(Float32, GPUGraphs_add) (algebra.jl:45).
 // ---------------------------------------------------------------------------------
@@ -111,10 +140,15 @@ struct SRPlusTimesF32 {
   __device__ __forceinline__ T neutral() const { return 0.0f; }
   __device__ __forceinline__ bool is_absorb(T a) const { return a == __int_as_float(0x7f800000); }
   __device__ __forceinline__ T mulk(int64_t k, int32_t col1, int64_t, int64_t = 0) const {
-    return __fmul_rn(__ldcs(nz + k), __ldg(x + (col1 - 1)));
+    return __fmul_rn(ld_stream(nz + k), __ldg(x + (col1 - 1)));
   }
   __device__ __forceinline__ T addv(T acc, T v) const { return __fadd_rn(acc, v); }
   __device__ __forceinline__ void write(int64_t row0, T acc) const { __stcs(y + row0, acc); }
+  // split steps for the pipelined kernel: stream A, gather x, multiply
+  __device__ __forceinline__ float a(int64_t k) const { return ld_stream(nz + k); }
+  __device__ __forceinline__ float4 a4(int64_t k) const { return ld_stream4(nz + k); }
+  __device__ __forceinline__ float xg(int32_t col1) const { return __ldg(x + (col1 - 1)); }
+  __device__ __forceinline__ T mul(float av, float xv) const { return __fmul_rn(av, xv); }
 };
 
 }  // namespace gg

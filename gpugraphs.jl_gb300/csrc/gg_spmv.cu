@@ -2,21 +2,24 @@
 // src/spmv/SELL.jl of GPUGraphs.jl).
 //
 // Kernels
-//  * k_csr_rowblock<SR>: unmasked CSR.  One warp per regular row block (<= 256
-//    stored entries): the warp computes mul(A[k], x[col[k]]) for the whole block
-//    with coalesced loads into shared memory, then every lane folds one row from
-//    shared memory in storage order -- the reference's sequential order, so these
-//    rows are bit-identical to it.  Long rows are cut into 2048-entry segments;
-//    each segment is reduced by one warp (lane partials + shuffle tree) and the warp
-//    that finishes a row's last segment combines the partials in order.  One launch
-//    covers both kinds of work item.
-//    Mask / range variants use the same kernel with a row filter, so every row with
-//    at most 256 entries is folded in storage order whatever the variant.
+//  * k_csr_rowblock<SR>: any semiring / element type, optional row filter (mask,
+//    range).  Short rows (<= 32 entries) are grouped into blocks of <= 256 entries;
+//    one warp computes mul(A[k], x[col[k]]) for a block with coalesced loads into
+//    shared memory, then every lane folds one row from shared memory in storage
+//    order -- the reference's sequential order, so these rows are bit-identical to
+//    it, early exit included.  Longer rows are reduced by one warp per segment
+//    (<= 4096 entries; lane partials + shuffle tree); for rows of several segments
+//    the warp that finishes the last one combines the partials in order.  Mask and
+//    range variants use the same kernel with a row filter.
+//  * k_spmv_pipe<SR>: the same work items for the fixed-type plus-times Float32
+//    semiring, software pipelined (next block's loads in flight during the current
+//    block's gathers), A streamed past L1, long segments read with 128-bit loads.
 //  * k_csr_first_hit<TC>: add == GPUGraphs_any with a mask on CSR: the first stored
 //    column whose x is nonzero (any_dense_masked_csr_spmv_kernel!, CSR.jl:147-171).
-//  * k_sell<SR>: one thread per stored SELL row walking its slice with stride C
-//    (slice-column-major, so a warp reads C consecutive words), stopping at the
-//    first -1 padding column like sell_spmv_kernel! (SELL.jl:31-63).
+//  * k_sell<SR>: one thread per (stored SELL row, chunk of <= 512 slice columns)
+//    walking with stride C (slice-column-major, so a warp reads C consecutive
+//    words), stopping at the first -1 padding column like sell_spmv_kernel!
+//    (SELL.jl:31-63); rows of multi-chunk slices are combined by k_sell_combine.
 #include <vector>
 
 #include "gg_semiring.cuh"
@@ -72,7 +75,7 @@ __device__ __forceinline__ int64_t row_of(const int32_t* rowptr, int32_t r0, int
 template <class SR, bool kFiltered, bool kNeedsRow>
 __global__ void __launch_bounds__(kRBWarps * 32)
     k_csr_rowblock(SR sr, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colval,
-                   const int2* __restrict__ blocks, int64_t nblocks, const int4* __restrict__ segs,
+                   const int4* __restrict__ blocks, int64_t nblocks, const int4* __restrict__ segs,
                    int64_t nsegs, const int32_t* __restrict__ long_first_seg,
                    const int32_t* __restrict__ long_rows, unsigned int* long_count,
                    typename SR::T* partials, RowFilter flt) {
@@ -83,10 +86,9 @@ __global__ void __launch_bounds__(kRBWarps * 32)
   T* st = stage[warp];
   for (int64_t item = (int64_t)blockIdx.x * kRBWarps + warp; item < nblocks + nsegs; item += nw) {
     if (item < nblocks) {
-      const int2 b = blocks[item];
+      const int4 b = blocks[item];
       if (kFiltered && (b.y <= flt.lo || b.x >= flt.hi)) continue;
-      const int32_t k0 = __ldg(rowptr + b.x) - 1;
-      const int32_t k1 = __ldg(rowptr + b.y) - 1;
+      const int32_t k0 = b.z, k1 = b.w;
       // stage products: 8 independent coalesced loads in flight per lane
       T v[kBlockNnz / 32];
 #pragma unroll
@@ -130,6 +132,11 @@ __global__ void __launch_bounds__(kRBWarps * 32)
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) acc = sr.addv(acc, shfl_xor_m<T>(kFull, acc, off, 32));
+      const int32_t f0 = long_first_seg[sg.w], f1 = long_first_seg[sg.w + 1];
+      if (f1 - f0 == 1) {  // the whole row in one segment
+        if (lane == 0) sr.write(sg.x, acc);
+        continue;
+      }
       unsigned prev = 0;
       if (lane == 0) {
         partials[si] = acc;
@@ -137,7 +144,6 @@ __global__ void __launch_bounds__(kRBWarps * 32)
         prev = atomicAdd(long_count + sg.w, 1u);
       }
       prev = __shfl_sync(kFull, prev, 0);
-      const int32_t f0 = long_first_seg[sg.w], f1 = long_first_seg[sg.w + 1];
       if (prev == (unsigned)(f1 - f0 - 1)) {  // this warp completed the row
         __threadfence();
         if (lane == 0) {
@@ -146,6 +152,178 @@ __global__ void __launch_bounds__(kRBWarps * 32)
           sr.write(long_rows[sg.w], tot);
           long_count[sg.w] = 0;  // ready for the next launch
         }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// pipelined row-block kernel for fixed-type semirings (no mask / range)
+//
+// Same work items as k_csr_rowblock, with the memory chain shortened and overlapped:
+// block descriptors carry their entry range; each warp issues the column / value
+// loads of its next block before gathering x for the current one, and prefetches
+// the rowptr pair of the current block's first 32 rows.  Long-row segments are read
+// with 128-bit loads, double buffered.  Rows of regular blocks are still folded in
+// storage order.
+// ---------------------------------------------------------------------------------
+static const int kPipeWarps = 8;
+static const int kPU = kBlockNnz / 32;  // entries per lane of a regular block
+
+template <class SR>
+struct BlockRegs {
+  int32_t col[kPU];
+  float val[kPU];
+  int32_t rp0, rp1;  // rowptr[r0 + lane], rowptr[r0 + lane + 1]
+};
+
+template <class SR>
+__device__ __forceinline__ void load_block(const SR& sr, const int32_t* __restrict__ rowptr,
+                                           const int32_t* __restrict__ colval, const int4& d,
+                                           int lane, BlockRegs<SR>& R) {
+#pragma unroll
+  for (int u = 0; u < kPU; ++u) {
+    const int32_t k = d.z + u * 32 + lane;
+    if (k < d.w) {
+      R.col[u] = ld_stream(colval + k);
+      R.val[u] = sr.a(k);
+    }
+  }
+  if (d.x + lane < d.y) {
+    R.rp0 = __ldg(rowptr + d.x + lane);
+    R.rp1 = __ldg(rowptr + d.x + lane + 1);
+  }
+}
+
+template <class SR>
+__global__ void __launch_bounds__(kPipeWarps * 32)
+    k_spmv_pipe(SR sr, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colval,
+                const int4* __restrict__ blocks, int64_t nblocks, const int4* __restrict__ segs,
+                int64_t nsegs, const int32_t* __restrict__ long_first_seg,
+                const int32_t* __restrict__ long_rows, unsigned int* long_count,
+                typename SR::T* partials) {
+  typedef typename SR::T T;
+  __shared__ T stage[kPipeWarps][kBlockNnz];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)gridDim.x * kPipeWarps;
+  const int64_t gw = (int64_t)blockIdx.x * kPipeWarps + warp;
+  T* st = stage[warp];
+  const int4 empty = make_int4(0, 0, 0, 0);
+
+  // ---- regular blocks ----
+  int64_t it = gw;
+  int4 dc = it < nblocks ? blocks[it] : empty;
+  int4 dn = it + nw < nblocks ? blocks[it + nw] : empty;
+  BlockRegs<SR> cur, nxt;
+  load_block(sr, rowptr, colval, dc, lane, cur);
+  while (it < nblocks) {
+    const int64_t itn = it + nw;
+    const int4 dnn = itn + nw < nblocks ? blocks[itn + nw] : empty;
+    // gathers for the current block (its columns are already in registers)
+    T p[kPU];
+#pragma unroll
+    for (int u = 0; u < kPU; ++u) {
+      const int32_t k = dc.z + u * 32 + lane;
+      if (k < dc.w) p[u] = sr.mul(cur.val[u], sr.xg(cur.col[u]));
+    }
+    // loads of the next block go out while the gathers are in flight
+    load_block(sr, rowptr, colval, dn, lane, nxt);
+#pragma unroll
+    for (int u = 0; u < kPU; ++u) {
+      const int32_t k = dc.z + u * 32 + lane;
+      if (k < dc.w) st[u * 32 + lane] = p[u];
+    }
+    __syncwarp();
+    for (int32_t r = dc.x + lane; r < dc.y; r += 32) {
+      const int32_t s = (r == dc.x + lane ? cur.rp0 : __ldg(rowptr + r)) - 1 - dc.z;
+      const int32_t e = (r == dc.x + lane ? cur.rp1 : __ldg(rowptr + r + 1)) - 1 - dc.z;
+      // Fold in storage order.  Without NaN / -Inf terms, a sum that reaches +Inf
+      // stays +Inf, which equals the reference's stop at the absorbing +Inf
+      // (CSR.jl:49-51); a NaN result is folded again with that stop.
+      T acc = sr.neutral();
+#pragma unroll 4
+      for (int32_t i = s; i < e; ++i) acc = sr.addv(acc, st[i]);
+      if (acc != acc) {
+        acc = sr.neutral();
+        for (int32_t i = s; i < e; ++i) {
+          acc = sr.addv(acc, st[i]);
+          if (sr.is_absorb(acc)) break;
+        }
+      }
+      sr.write(r, acc);
+    }
+    __syncwarp();
+    it = itn;
+    dc = dn;
+    dn = dnn;
+    cur = nxt;
+  }
+
+  // ---- long-row segments: 128-bit loads, next chunk prefetched ----
+  for (int64_t si = gw; si < nsegs; si += nw) {
+    const int4 sg = segs[si];  // row, k_begin, k_end, long-row index
+    T acc = sr.neutral();
+    const int32_t kb = sg.y, ke = sg.z;
+    int32_t ka = (kb + 3) & ~3;  // first 16-byte aligned entry
+    if (ka > ke) ka = ke;
+    if (kb + lane < ka) acc = sr.addv(acc, sr.mul(sr.a(kb + lane), sr.xg(ld_stream(colval + kb + lane))));
+    // body in chunks of 256 entries: 2 x (int4 + float4) per lane
+    int32_t k = ka;
+    const int32_t kend = ka + ((ke - ka) & ~255);
+    int4 c0, c1;
+    float4 v0, v1;
+    if (k < kend) {
+      c0 = ld_stream4(colval + k + lane * 4);
+      c1 = ld_stream4(colval + k + 128 + lane * 4);
+      v0 = sr.a4(k + lane * 4);
+      v1 = sr.a4(k + 128 + lane * 4);
+    }
+    while (k < kend) {
+      const int32_t kn = k + 256;
+      int4 nc0 = c0, nc1 = c1;
+      float4 nv0 = v0, nv1 = v1;
+      if (kn < kend) {
+        nc0 = ld_stream4(colval + kn + lane * 4);
+        nc1 = ld_stream4(colval + kn + 128 + lane * 4);
+        nv0 = sr.a4(kn + lane * 4);
+        nv1 = sr.a4(kn + 128 + lane * 4);
+      }
+      const float x0 = sr.xg(c0.x), x1 = sr.xg(c0.y), x2 = sr.xg(c0.z), x3 = sr.xg(c0.w);
+      const float x4 = sr.xg(c1.x), x5 = sr.xg(c1.y), x6 = sr.xg(c1.z), x7 = sr.xg(c1.w);
+      acc = sr.addv(acc, sr.mul(v0.x, x0));
+      acc = sr.addv(acc, sr.mul(v0.y, x1));
+      acc = sr.addv(acc, sr.mul(v0.z, x2));
+      acc = sr.addv(acc, sr.mul(v0.w, x3));
+      acc = sr.addv(acc, sr.mul(v1.x, x4));
+      acc = sr.addv(acc, sr.mul(v1.y, x5));
+      acc = sr.addv(acc, sr.mul(v1.z, x6));
+      acc = sr.addv(acc, sr.mul(v1.w, x7));
+      c0 = nc0; c1 = nc1; v0 = nv0; v1 = nv1;
+      k = kn;
+    }
+    for (int32_t kk = kend + lane; kk < ke; kk += 32)
+      acc = sr.addv(acc, sr.mul(sr.a(kk), sr.xg(ld_stream(colval + kk))));
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc = sr.addv(acc, shfl_xor_m<T>(kFull, acc, off, 32));
+    const int32_t f0 = long_first_seg[sg.w], f1 = long_first_seg[sg.w + 1];
+    if (f1 - f0 == 1) {  // the whole row in one segment
+      if (lane == 0) sr.write(sg.x, acc);
+      continue;
+    }
+    unsigned prev = 0;
+    if (lane == 0) {
+      partials[si] = acc;
+      __threadfence();
+      prev = atomicAdd(long_count + sg.w, 1u);
+    }
+    prev = __shfl_sync(kFull, prev, 0);
+    if (prev == (unsigned)(f1 - f0 - 1)) {
+      __threadfence();
+      if (lane == 0) {
+        T tot = sr.neutral();
+        for (int32_t q = f0; q < f1; ++q) tot = sr.addv(tot, __ldcg(partials + q));
+        sr.write(long_rows[sg.w], tot);
+        long_count[sg.w] = 0;
       }
     }
   }
@@ -192,30 +370,127 @@ __global__ void k_csr_first_hit(SRGen<TC> sr, const int32_t* __restrict__ rowptr
 }
 
 // ---------------------------------------------------------------------------------
-// SELL: one thread per stored row
+// SELL: one thread per (stored row, chunk of its slice).  Every thread walks at most
+// kSellChunk columns with stride C, so hub slices no longer serialise on one thread;
+// a row spread over several chunks is combined in chunk order by k_sell_combine.
 // ---------------------------------------------------------------------------------
 template <class SR>
 __global__ void k_sell(SR sr, const int32_t* __restrict__ slice_ptr,
                        const int32_t* __restrict__ colval, const int32_t* __restrict__ perm,
-                       int64_t C, int64_t sr_lo, int64_t sr_hi, int64_t range_lo, int64_t range_hi,
+                       int64_t C, int64_t m, const int4* __restrict__ items, int64_t nitems,
+                       typename SR::T* partials, int64_t range_lo, int64_t range_hi,
                        const void* mask, int tmask) {
   typedef typename SR::T T;
-  for (int64_t t = sr_lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sr_hi;
+  const int64_t total = nitems * C;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t s = t / C, o = t - s * C;
-    const int64_t r1 = perm ? (int64_t)perm[t] : t + 1;  // original row, 1-based
+    const int64_t it = t / C, o = t - it * C;
+    const int4 d = items[it];  // slice, first column, end column, partial index
+    const int64_t srow = (int64_t)d.x * C + o;
+    if (srow >= m) continue;
+    const int64_t r1 = perm ? (int64_t)perm[srow] : srow + 1;  // original row, 1-based
     if (range_lo > 0 && (r1 < range_lo || r1 > range_hi)) continue;
     if (mask && raw_is_zero(load_raw(mask, tmask, r1 - 1), tmask)) continue;
-    const int64_t i0 = (int64_t)slice_ptr[s] - 1 + o, i1 = (int64_t)slice_ptr[s + 1] - 1;
+    int64_t i = (int64_t)slice_ptr[d.x] - 1 + o + (int64_t)d.y * C;
     T acc = sr.neutral();
-    for (int64_t i = i0; i < i1; i += C) {
-      const int32_t col = __ldcs(colval + i);
+    int32_t j = d.y;
+    bool done = false;
+    for (; j + 4 <= d.z && !done; j += 4, i += 4 * C) {
+      int32_t c[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) c[u] = ld_stream(colval + i + u * C);
+      T p[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) p[u] = (c[u] != -1) ? sr.mulk(i + u * C, c[u], r1) : sr.neutral();
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (c[u] == -1) { done = true; break; }
+        acc = sr.addv(acc, p[u]);
+      }
+    }
+    for (; j < d.z && !done; ++j, i += C) {
+      const int32_t col = ld_stream(colval + i);
       if (col == -1) break;
       acc = sr.addv(acc, sr.mulk(i, col, r1));
     }
+    if (d.w < 0) sr.write(r1 - 1, acc);
+    else partials[(int64_t)d.w * C + o] = acc;
+  }
+}
+
+template <class SR>
+__global__ void k_sell_combine(SR sr, const int32_t* __restrict__ perm, int64_t C, int64_t m,
+                               const int4* __restrict__ multi, int64_t nmulti,
+                               const typename SR::T* __restrict__ partials, int64_t range_lo,
+                               int64_t range_hi, const void* mask, int tmask) {
+  typedef typename SR::T T;
+  const int64_t total = nmulti * C;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = t / C, o = t - q * C;
+    const int4 d = multi[q];  // slice, first partial, chunks
+    const int64_t srow = (int64_t)d.x * C + o;
+    if (srow >= m) continue;
+    const int64_t r1 = perm ? (int64_t)perm[srow] : srow + 1;
+    if (range_lo > 0 && (r1 < range_lo || r1 > range_hi)) continue;
+    if (mask && raw_is_zero(load_raw(mask, tmask, r1 - 1), tmask)) continue;
+    T acc = sr.neutral();
+    for (int32_t c = 0; c < d.z; ++c) acc = sr.addv(acc, partials[(int64_t)(d.y + c) * C + o]);
     sr.write(r1 - 1, acc);
   }
 }
+
+int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
+  if (A->sellplan) return GG_OK;
+  const int64_t ns = A->nslices, C = A->slice_size;
+  std::vector<int32_t> sp(ns + 1);
+  GG_CUDA(cudaMemcpyAsync(sp.data(), A->slice_ptr, (ns + 1) * sizeof(int32_t),
+                          cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<int4> items, multi;
+  int32_t np = 0;
+  for (int64_t s = 0; s < ns; ++s) {
+    const int64_t L = C > 0 ? ((int64_t)sp[s + 1] - sp[s]) / C : 0;
+    if (L <= kSellChunk) {
+      items.push_back(make_int4((int)s, 0, (int)L, -1));
+      continue;
+    }
+    const int32_t nch = (int32_t)((L + kSellChunk - 1) / kSellChunk);
+    multi.push_back(make_int4((int)s, np, nch, 0));
+    for (int32_t c = 0; c < nch; ++c) {
+      const int64_t jb = (int64_t)c * kSellChunk;
+      const int64_t je = jb + kSellChunk < L ? jb + kSellChunk : L;
+      items.push_back(make_int4((int)s, (int)jb, (int)je, np + c));
+    }
+    np += nch;
+  }
+  SellPlan* P = new SellPlan();
+  P->nitems = (int64_t)items.size();
+  P->nmulti = (int64_t)multi.size();
+  cudaError_t e = cudaMalloc((void**)&P->items, (items.size() + 1) * sizeof(int4));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&P->multi, (multi.size() + 1) * sizeof(int4));
+  if (e == cudaSuccess) e = cudaMalloc(&P->partials, ((int64_t)np * C + 1) * 8);
+  if (e == cudaSuccess && !items.empty())
+    e = cudaMemcpyAsync(P->items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                        ctx->stream);
+  if (e == cudaSuccess && !multi.empty())
+    e = cudaMemcpyAsync(P->multi, multi.data(), multi.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                        ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(P->items);
+    cudaFree(P->multi);
+    cudaFree(P->partials);
+    delete P;
+    return cuda_error(e, "SELL analysis");
+  }
+  A->sellplan = P;
+  return GG_OK;
+}
+
+template <class SR>
+static int launch_sell(gg_ctx* ctx, gg_mat* A, const SR& sr, const void* mask, int tmask,
+                       int64_t lo, int64_t hi);
 
 // ---------------------------------------------------------------------------------
 // analysis: row blocks and long-row segments (built once per matrix, on first use)
@@ -227,14 +502,14 @@ int build_row_blocks(gg_ctx* ctx, gg_mat* A) {
   GG_CUDA(cudaMemcpyAsync(rp.data(), A->rowptr, (m + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost,
                           ctx->stream));
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
-  std::vector<int2> blocks;
+  std::vector<int4> blocks;
   std::vector<int4> segs;
   std::vector<int32_t> first_seg, long_rows;
   blocks.reserve(m / 8 + 16);
   int64_t r = 0;
   while (r < m) {
     int64_t len = rp[r + 1] - rp[r];
-    if (len > kBlockNnz) {
+    if (len > kShortRow) {
       int32_t li = (int32_t)long_rows.size();
       long_rows.push_back((int32_t)r);
       first_seg.push_back((int32_t)segs.size());
@@ -248,11 +523,11 @@ int build_row_blocks(gg_ctx* ctx, gg_mat* A) {
     int64_t first = r, cnt = 0;
     while (r < m && r - first < kBlockRows) {
       int64_t l = rp[r + 1] - rp[r];
-      if (l > kBlockNnz || cnt + l > kBlockNnz) break;
+      if (l > kShortRow || cnt + l > kBlockNnz) break;
       cnt += l;
       ++r;
     }
-    blocks.push_back(make_int2((int)first, (int)r));
+    blocks.push_back(make_int4((int)first, (int)r, rp[first] - 1, rp[r] - 1));
   }
   first_seg.push_back((int32_t)segs.size());
 
@@ -268,7 +543,7 @@ int build_row_blocks(gg_ctx* ctx, gg_mat* A) {
     if (e == cudaSuccess && bytes > 0)
       e = cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
   };
-  up((void**)&rb->blocks, blocks.data(), blocks.size() * sizeof(int2));
+  up((void**)&rb->blocks, blocks.data(), blocks.size() * sizeof(int4));
   up((void**)&rb->segs, segs.data(), segs.size() * sizeof(int4));
   up((void**)&rb->long_first_seg, first_seg.data(), first_seg.size() * sizeof(int32_t));
   up((void**)&rb->long_rows, long_rows.data(), long_rows.size() * sizeof(int32_t));
@@ -312,8 +587,14 @@ int launch_rowblock_t(gg_ctx* ctx, gg_mat* A, const SR& sr, const RowFilter& flt
   RowBlocks* rb = A->blocks;
   const int64_t items = rb->nblocks + rb->nsegs;
   if (items == 0) return GG_OK;
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, k_csr_rowblock<SR, kFiltered, kNeedsRow>, kRBWarps * 32, 0));
+    if (per_sm < 1) per_sm = 1;
+  }
   int64_t grid = (items + kRBWarps - 1) / kRBWarps;
-  const int64_t cap = (int64_t)ctx->num_sms * 8;  // 8 CTAs x 8 warps = 64 warps per SM
+  const int64_t cap = (int64_t)ctx->num_sms * per_sm;  // one resident wave
   if (grid > cap) grid = cap;
   k_csr_rowblock<SR, kFiltered, kNeedsRow><<<(int)grid, kRBWarps * 32, 0, ctx->stream>>>(
       sr, A->rowptr, A->colval, rb->blocks, rb->nblocks, rb->segs, rb->nsegs, rb->long_first_seg,
@@ -362,20 +643,7 @@ static int spmv_generic(gg_ctx* ctx, gg_mat* A, int mul, int add, int accum, voi
   const int64_t m = A->m;
   if (A->format == GG_FMT_SELL) {
     sr.has_absorb = false;  // the SELL kernels never stop early (SELL.jl:54-60)
-    int64_t s_lo = 0, s_hi = m;
-    if (lo > 0) {
-      // stored rows of original rows lo..hi lie in the sigma windows covering them
-      const int64_t w = A->sigma > 1 ? A->sigma : 1;
-      s_lo = ((lo - 1) / w) * w;
-      s_hi = ((hi + w - 1) / w) * w;
-      if (s_hi > m) s_hi = m;
-    }
-    if (s_hi <= s_lo) return GG_OK;
-    k_sell<SRGen<TC>><<<grid_for(ctx, s_hi - s_lo, 256), 256, 0, ctx->stream>>>(
-        sr, A->slice_ptr, A->colval, A->sigma > 1 ? A->perm : nullptr, A->slice_size, s_lo, s_hi,
-        lo, hi, mask, tmask);
-    GG_CUDA(cudaGetLastError());
-    return GG_OK;
+    return launch_sell(ctx, A, sr, mask, tmask, lo, hi);
   }
   const int G = group_width(A);
   if (add == GG_OP_ANY && mask != nullptr && lo == 0) {
@@ -385,6 +653,25 @@ static int spmv_generic(gg_ctx* ctx, gg_mat* A, int mul, int add, int accum, voi
     return GG_OK;
   }
   return launch_rowblock(ctx, A, sr, mask, tmask, lo, hi, mul == GG_OP_FIRSTI);
+}
+
+template <class SR>
+static int launch_sell(gg_ctx* ctx, gg_mat* A, const SR& sr, const void* mask, int tmask,
+                       int64_t lo, int64_t hi) {
+  GG_CHECK(build_sell_plan(ctx, A));
+  SellPlan* P = A->sellplan;
+  const int64_t C = A->slice_size;
+  typedef typename SR::T T;
+  if (P->nitems > 0)
+    k_sell<SR><<<grid_for(ctx, P->nitems * C, 256), 256, 0, ctx->stream>>>(
+        sr, A->slice_ptr, A->colval, A->sigma > 1 ? A->perm : nullptr, C, A->m, P->items,
+        P->nitems, static_cast<T*>(P->partials), lo, hi, mask, tmask);
+  if (P->nmulti > 0)
+    k_sell_combine<SR><<<grid_for(ctx, P->nmulti * C, 256), 256, 0, ctx->stream>>>(
+        sr, A->sigma > 1 ? A->perm : nullptr, C, A->m, P->multi, P->nmulti,
+        static_cast<const T*>(P->partials), lo, hi, mask, tmask);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
 }
 
 // dispatch of gg_spmv after validation (gg_api.cu); tc = accumulator type
@@ -398,12 +685,27 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
     sr.nz = static_cast<const float*>(A->nzval);
     sr.x = static_cast<const float*>(x);
     sr.y = static_cast<float*>(y);
-    if (A->format == GG_FMT_CSR) return launch_rowblock(ctx, A, sr);
-    k_sell<SRPlusTimesF32><<<grid_for(ctx, A->m, 256), 256, 0, ctx->stream>>>(
-        sr, A->slice_ptr, A->colval, A->sigma > 1 ? A->perm : nullptr, A->slice_size, 0, A->m, 0,
-        0, nullptr, 0);
-    GG_CUDA(cudaGetLastError());
-    return GG_OK;
+    if (A->format == GG_FMT_CSR) {
+      GG_CHECK(build_row_blocks(ctx, A));
+      RowBlocks* rb = A->blocks;
+      const int64_t items = rb->nblocks > rb->nsegs ? rb->nblocks : rb->nsegs;
+      if (items == 0) return GG_OK;
+      static int per_sm = 0;
+      if (per_sm == 0) {
+        GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_spmv_pipe<SRPlusTimesF32>, kPipeWarps * 32, 0));
+        if (per_sm < 1) per_sm = 1;
+      }
+      int64_t grid = (items + kPipeWarps - 1) / kPipeWarps;
+      const int64_t cap = (int64_t)ctx->num_sms * per_sm;  // one resident wave
+      if (grid > cap) grid = cap;
+      k_spmv_pipe<SRPlusTimesF32><<<(int)grid, kPipeWarps * 32, 0, ctx->stream>>>(
+          sr, A->rowptr, A->colval, rb->blocks, rb->nblocks, rb->segs, rb->nsegs,
+          rb->long_first_seg, rb->long_rows, rb->long_count, static_cast<float*>(rb->partials));
+      GG_CUDA(cudaGetLastError());
+      return GG_OK;
+    }
+    return launch_sell(ctx, A, sr, nullptr, 0, 0, 0);
   }
   switch (tc) {
     case GG_BOOL: return spmv_generic<GG_BOOL>(ctx, A, mul, add, accum, y, ty, x, tx, mask, tmask, lo, hi);
