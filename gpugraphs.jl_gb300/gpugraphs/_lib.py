@@ -36,6 +36,7 @@ SIGNATURES = {
     "gg_bfs_levels": [P, P, I64, P, I64, PI64],
     "gg_bfs_parents": [P, P, I64, P, I64, I, PI64],
     "gg_sssp": [P, P, P, I64, P, P, I, I64, PI64],
+    "gg_bfs_levels_noalloc": [P, P, P, I, I64, I64, I64, P, P, PI64],
     "gg_gen_rmat_edges": [P, I, I64, D, D, D, U64, I, P, P, P],
     "gg_gen_er_edges": [P, I64, I64, U64, I, P, P, P],
     "gg_gen_grid_edges": [P, I64, I64, U64, I, P, P, P],

@@ -227,6 +227,25 @@ int gg_bfs_parents(gg_ctx* ctx, const gg_mat* A_T, int64_t source, int32_t* pare
 int gg_sssp(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, int64_t nsources, void* dist,
             void* next, int dist_dtype, int64_t ld, int64_t* rounds_out);
 
+/*
+ * BFS levels for callers that cannot allocate device memory (no counterpart in the
+ * reference).  Same result as gg_bfs_levels -- dist[v] = hop level along edges with
+ * odd / true stored values (all stored edges when nzval is NULL), dist[source] = 0,
+ * unreached entries untouched -- computed from plain device pointers to the 1-based
+ * CSR arrays of A_T (rowptr n+1, colval nnz, nzval nnz of type dtype) on the current
+ * device, on `stream` (NULL = legacy default stream).  Calls no cudaMalloc /
+ * cudaFree: its working state lives in a fixed array of the library sized for at
+ * most 4,194,304 vertices (1.5 MiB, held by every GPU that loads the library until
+ * exit); larger n returns GG_ERR_ARGUMENT.  The first call on a device looks up that
+ * array's device address, so make it before any stream capture.  All calls share
+ * the one array: calls whose work overlaps on the GPU race and must be ordered by
+ * the caller.  Bottom-up only: O(levels * (n + nnz)) work.  The CSR arrays are not
+ * validated.  Synchronous.
+ */
+int gg_bfs_levels_noalloc(const int32_t* rowptr, const int32_t* colval, const void* nzval,
+                          int dtype, int64_t n, int64_t nnz, int64_t source, int32_t* dist,
+                          void* stream, int64_t* levels_out);
+
 /* ---- seeded synthetic inputs (no reference counterpart: the reference's benchmark
  *      draws its inputs with Julia's sprand / Graphs.jl generators,
  *      benchmark/benchmarks.jl:57-63,100-104) ------------------------------------ */
