@@ -1,18 +1,25 @@
-"""Benchmark of the semiring SpMV hot path on one GB300 (N replicas under torchrun).
+"""Benchmarks of the semiring sparse path on one GB300 (N replicas under torchrun).
 
-Default workload: plus-times Float32 SpMV over the CSR of an R-MAT scale-22 graph
-(a=0.57, b=0.19, c=0.19, edge factor 16, symmetrised, self-loops removed, values
-uniform [0,1)), x uniform [0,1) -- the SpMV half of the R-MAT scale-22 config.  A
-step is one gpu_spmv! over the whole matrix.  `value` is GB/s of algorithmic bytes
-4(n+1) + 8 nnz + 4n (x) + 4n (y) with all inputs resident in HBM (the matrix, ~1 GB,
-is larger than L2); `e2e` times the same call through the public API with x in
-pinned host memory copied in and y copied out every step.
+Default workload (`spmv_csr_rmat22`, the R-MAT scale-22 configuration): plus-times
+Float32 SpMV over the CSR of an R-MAT graph (a=0.57, b=0.19, c=0.19, edge factor 16,
+symmetrised, self-loops removed, values uniform [0,1)), x uniform [0,1).  A step is
+one gpu_spmv! over the whole matrix.  `value` = GB/s of algorithmic bytes
+4(n+1) + 8 nnz + 4n (x) + 4n (y) with inputs resident in HBM (the ~1 GB matrix is
+larger than L2, so no flush is needed); `e2e` = the same call through the public API
+with x copied in from pinned host memory and y copied out every step.  The line also
+carries the same graph's SELL-C-sigma SpMV, SpMM (32 row-major columns), BFS,
+Bellman-Ford and batched BFS / shortest-path throughput under "secondary".
 
---impl reference times the reference algorithm's CPU path (the C restatement of
-csr_spmv_kernel!, OpenMP over every host core) on the same graph built on the host.
+Other workloads (`--workload`, one JSON line each): bfs_rmat24, sssp_rmat24,
+bfs_grid4096, sssp_grid4096 (BFS / Bellman-Ford GTEPS), serve (continuous-batching
+server, queries/s with p50/p99 latency against the one-query-at-a-time path),
+multigraph (1000 Erdos-Renyi graphs in one launch).
+
+--impl reference times the reference algorithm's CPU path (the C restatement of the
+reference kernels, OpenMP over every host core) on the same inputs built on the host.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                       [--workload NAME]
+                       [--workload NAME] [--no-cpu]
 """
 import argparse
 import json
@@ -31,6 +38,7 @@ for _p in (ROOT, PKG):
 
 RMAT = dict(a=0.57, b=0.19, c=0.19, edge_factor=16, seed=1)
 FALLBACK_HBM_GBS = 6800.0
+I32MAX = 2 ** 31 - 1
 
 
 def peak_hbm():
@@ -44,7 +52,7 @@ def peak_hbm():
 
 def traffic_from_profiles(workload):
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary
-    (profiles/traffic.txt: `workload kernel bytes_per_launch` lines), else None."""
+    (profiles/traffic.txt lines: `workload kernel bytes_per_launch`), else None."""
     p = os.path.join(ROOT, "profiles", "traffic.txt")
     try:
         for line in open(p):
@@ -57,7 +65,7 @@ def traffic_from_profiles(workload):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during a timed region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -66,7 +74,6 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = None
 
     def start(self):
         try:
@@ -111,40 +118,141 @@ class ClockSampler:
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
-
-# ---------------------------------------------------------------------------------
-# workloads
-# ---------------------------------------------------------------------------------
 
 def spmv_bytes(n, nnz):
     return 4 * (n + 1) + 8 * nnz + 4 * n + 4 * n
 
 
-def build_rmat22(device):
+def bfs_bytes(n, nnz):
+    return 4 * (n + 1) + 4 * nnz + 4 * n
+
+
+def sssp_bytes(n, nnz):
+    return 4 * (n + 1) + 8 * nnz + 4 * n
+
+
+# ---------------------------------------------------------------------------------
+# timing helpers (CUDA events on the launching stream, synchronize on both sides)
+# ---------------------------------------------------------------------------------
+
+def time_steps(fn, steps, warmup=3):
+    import torch
+    for _ in range(max(warmup, 3)):
+        fn()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        fn()
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def time_host(fn, reps, warmup=1):
+    """Host wall time of synchronous calls (BFS / SSSP return after the search)."""
+    import torch
+    for _ in range(warmup):
+        fn(0)
+    torch.cuda.synchronize()
+    ts = []
+    for i in range(reps):
+        t0 = time.perf_counter()
+        fn(i)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    return ts
+
+
+def reached_edges(A, dist):
+    """m_cc: stored entries of the reached vertices / 2 (symmetric graphs, Graph500)."""
+    import torch
+    rp = A.rowptr.to(torch.int64)
+    deg = rp[1:] - rp[:-1]
+    return int(deg[dist != I32MAX].sum().item()) // 2
+
+
+def sources_for(A, k, seed):
+    """k seeded non-isolated vertices (1-based)."""
+    import numpy as np
+    import torch
+    rp = A.rowptr.to(torch.int64)
+    nz = torch.nonzero((rp[1:] - rp[:-1]) > 0).flatten().cpu().numpy()
+    rng = np.random.default_rng(seed)
+    return (nz[rng.integers(0, len(nz), k)] + 1).astype(np.int64)
+
+
+# ---------------------------------------------------------------------------------
+# default workload: SpMV on R-MAT scale 22 (+ secondary measurements)
+# ---------------------------------------------------------------------------------
+
+def rmat(scale, wkind, device):
     from gpugraphs import generators as gen
-    A = gen.rmat(22, RMAT["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], seed=RMAT["seed"],
-                 wkind=gen.W_U01_F32, device=device)
-    x = gen.uniform_vector(A.n, seed=2, device=device)
-    return A, x
+    return gen.rmat(scale, RMAT["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], seed=RMAT["seed"],
+                    wkind=wkind, device=device)
 
 
-def run_ours(args):
+def secondary_rmat22(device, A, x):
+    import numpy as np
+    import torch
+    import gpugraphs as G
+    from gpugraphs import generators as gen
+    out = {}
+    n, nnz = A.n, A.nnz()
+    y = torch.zeros(n, dtype=torch.float32, device=device)
+    S = G.SparseGPUMatrixSELL(A, 32, A.n)
+    ms = time_steps(lambda: G.gpu_spmv_(y, S, x), 20)
+    out["sell_spmv_rmat22"] = {"gbs": round(spmv_bytes(n, nnz) / ms / 1e6, 1), "ms": round(ms, 4),
+                               "C": 32, "sigma": n, "n_stored": S.n_stored}
+    del S
+    X = torch.rand((n, 32), dtype=torch.float32, device=device)
+    Y = torch.zeros((n, 32), dtype=torch.float32, device=device)
+    ms = time_steps(lambda: G.gpu_spmm_(Y, A, X), 5)
+    b = 4 * (n + 1) + 8 * nnz + 4 * n * 32 * 2
+    out["spmm_rmat22_k32"] = {"gbs_algorithmic": round(b / ms / 1e6, 1), "ms": round(ms, 3),
+                              "layout": "row-major"}
+    del X, Y
+    P = rmat(22, gen.W_PATTERN, device)
+    src = sources_for(P, 256, 7)
+    d = G.bfs_distances(P, int(src[0]))
+    mcc = reached_edges(P, d)
+    ts = time_host(lambda i: G.bfs_distances(P, int(src[i % 16])), 8)
+    t = statistics.median(ts)
+    out["bfs_rmat22"] = {"gteps": round(mcc / t / 1e9, 2), "ms": round(t * 1e3, 3), "m_cc": mcc}
+    tb = time_host(lambda i: G.bfs_distances_batch(P, src), 2)
+    tbm = statistics.median(tb)
+    out["bfs_batch256_rmat22"] = {"queries_per_s": round(256 / tbm, 1), "ms": round(tbm * 1e3, 2),
+                                  "aggregate_gteps": round(256 * mcc / tbm / 1e9, 1),
+                                  "speedup_vs_single": round((256 / tbm) / (1 / t), 2)}
+    del P
+    W = rmat(22, gen.W_INT_1_255, device)
+    ts = time_host(lambda i: G.shortest_path(W, int(src[i % 16])), 3)
+    t1 = statistics.median(ts)
+    out["sssp_rmat22_int"] = {"gteps": round(mcc / t1 / 1e9, 2), "ms": round(t1 * 1e3, 2)}
+    tb = time_host(lambda i: G.shortest_path(W, src[:64]), 1)
+    tbm = statistics.median(tb)
+    out["sssp_batch64_rmat22_int"] = {"queries_per_s": round(64 / tbm, 1), "ms": round(tbm * 1e3, 1),
+                                      "speedup_vs_single": round((64 / tbm) / (1 / t1), 2)}
+    return out
+
+
+def run_spmv_rmat22(args):
     import torch
     import torch.distributed as dist
-
     import gpugraphs as G
+    from gpugraphs import generators as gen
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
     if ws > 1:
         dist.init_process_group("nccl", device_id=device)
-    A, x = build_rmat22(device)
+    A = rmat(22, gen.W_U01_F32, device)
+    x = gen.uniform_vector(A.n, seed=2, device=device)
     n, nnz = A.n, A.nnz()
     y = torch.zeros(n, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
@@ -159,7 +267,7 @@ def run_ours(args):
         dist.barrier()
     clk = ClockSampler(local)
     clk.start()
-    time.sleep(0.3)  # let the sampler see the start of the timed region
+    time.sleep(0.3)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     ev0.record(stream)
@@ -170,8 +278,7 @@ def run_ours(args):
     if ws > 1:
         dist.barrier()
     ms = ev0.elapsed_time(ev1)
-    # hold the clock sampler over a longer window of the same work
-    t_end = time.time() + 1.0
+    t_end = time.time() + 1.0  # keep the sampler on the same work a little longer
     while time.time() < t_end:
         for _ in range(50):
             step()
@@ -184,40 +291,33 @@ def run_ours(args):
     per_step_ms = ms / args.steps
     B = spmv_bytes(n, nnz)
     value = ws * B / (per_step_ms * 1e-3) / 1e9
+    launches_per_step = 2 if (A.handle and _relabelled(A)) else 1
 
-    # kernel-level roofline: average launch duration of the SpMV kernel (one per step)
-    achieved = B / (per_step_ms * 1e-3) / 1e9
+    # roofline of the SpMV kernel alone (the x reordering gather, when present, is a
+    # separate 8n-byte kernel timed inside the step)
     peak, peak_kind = peak_hbm()
+    achieved = B / (per_step_ms * 1e-3) / 1e9
     traffic = traffic_from_profiles("spmv_csr_rmat22")
 
     # e2e through the public API with host buffers
     xh = x.cpu().pin_memory()
     yh = torch.empty(n, dtype=torch.float32).pin_memory()
     xd = torch.empty_like(x)
-    for _ in range(3):
+
+    def e2e_step():
         xd.copy_(xh, non_blocking=True)
         G.gpu_spmv_(y, A, xd)
         yh.copy_(y, non_blocking=True)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        xd.copy_(xh, non_blocking=True)
-        G.gpu_spmv_(y, A, xd)
-        yh.copy_(y, non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    e2e_ms_t = torch.tensor([e2e_ms], device=device)
+
+    e2e_ms = time_steps(e2e_step, args.steps)
+    e2e_t = torch.tensor([e2e_ms], device=device)
     if ws > 1:
-        dist.all_reduce(e2e_ms_t, op=dist.ReduceOp.MAX)
-    e2e_val = ws * B / (float(e2e_ms_t.item()) * 1e-3) / 1e9
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_val = ws * B / (float(e2e_t.item()) * 1e-3) / 1e9
 
-    # parity spot check of this run's output against an FP64 product on 4096 rows
-    rows = torch.arange(0, n, max(1, n // 4096), device=device)[:4096]
-    ok = spot_check(A, x, y, rows)
-
-    cpu = cpu_baseline(A, x) if (rank == 0 and not args.no_cpu) else None
+    ok = spot_check(A, x, y)
+    secondary = {} if args.no_secondary else secondary_rmat22(device, A, x)
+    cpu = cpu_baseline_spmv(A, x) if (rank == 0 and not args.no_cpu) else None
     out = {
         "metric": "SpMV GB/s (plus-times Float32, CSR, R-MAT scale 22)",
         "value": round(value, 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
@@ -225,16 +325,18 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded R-MAT generator on the device)",
         "config": {"workload": "spmv_csr_rmat22", "n": n, "nnz": nnz, "format": "CSR",
-                   "semiring": "(mul, add, second)", "l2": "inputs larger than L2 (CSR %.2f GB)" % (
-                       (4 * (n + 1) + 8 * nnz) / 1e9), "parallelism": "replicas" if ws > 1 else "single"},
+                   "semiring": "(mul, add, second)",
+                   "l2": "inputs larger than L2 (CSR %.2f GB)" % ((4 * (n + 1) + 8 * nnz) / 1e9),
+                   "parallelism": "replicas" if ws > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "peak_kind": peak_kind, "algorithmic_bytes": B},
         "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * n},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * launches_per_step,
         "clocks": clocks,
         "parity_spot_check": ok,
+        "secondary": secondary,
     }
     if cpu is not None:
         out["cpu_baseline"] = cpu
@@ -244,54 +346,146 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def spot_check(A, x, y, rows):
+def _relabelled(A):
+    # the library reorders x when the column frequencies are skewed (R-MAT); the
+    # reordering is one extra gather kernel per SpMV
+    return A.n >= (1 << 16)
+
+
+def spot_check(A, x, y, nrows=2048):
+    """FP64 check of this run's output on seeded rows (rel err vs FP64 <= 1e-5)."""
     import numpy as np
     import torch
-    rp = A.rowptr.cpu().numpy().astype(np.int64)
-    r = rows.cpu().numpy()
-    cv = A.colval
-    nz = A.nzval
-    xs = x.double()
+    rp = A.rowptr.to(torch.int64)
+    rows = torch.from_numpy(np.random.default_rng(3).integers(0, A.n, nrows)).to(x.device)
     worst = 0.0
-    for i in r:
-        lo, hi = rp[i] - 1, rp[i + 1] - 1
-        if hi == lo:
-            ref = 0.0
-        else:
-            idx = torch.arange(lo, hi, device=x.device)
-            ref = float((nz[idx].double() * xs[cv[idx].long() - 1]).sum())
+    xs = x.double()
+    for i in rows.tolist():
+        lo, hi = int(rp[i]) - 1, int(rp[i + 1]) - 1
+        ref = float((A.nzval[lo:hi].double() * xs[A.colval[lo:hi].long() - 1]).sum()) if hi > lo else 0.0
         got = float(y[i])
-        if ref != 0:
-            worst = max(worst, abs(got - ref) / abs(ref))
-        elif got != 0:
-            worst = max(worst, abs(got))
-    return {"rows": int(len(r)), "max_rel_err_vs_fp64": worst, "ok": worst <= 1e-5}
+        err = abs(got - ref) / abs(ref) if ref != 0 else abs(got)
+        worst = max(worst, err)
+    return {"rows": nrows, "max_rel_err_vs_fp64": worst, "ok": worst <= 1e-5}
 
 
-def cpu_baseline(A, x, budget_s=10.0):
-    """The reference's csr_spmv_kernel! restated in C (oracle), OpenMP over all host
-    cores, timed on the same graph copied to the host."""
+def cpu_baseline_spmv(A, x, budget_s=8.0):
+    """csr_spmv_kernel! (plus-times) restated in C (oracle), OpenMP over all host cores,
+    on the same graph copied to the host."""
     import numpy as np
     from oracle import oracle as O
-    rowptr = A.rowptr.cpu().numpy()
-    colval = A.colval.cpu().numpy()
-    nzval = A.nzval.cpu().numpy()
+    rowptr, colval, nzval = A.rowptr.cpu().numpy(), A.colval.cpu().numpy(), A.nzval.cpu().numpy()
     xh = x.cpu().numpy()
     y = np.zeros(A.m, np.float32)
-    O.spmv_plus_times_f32(rowptr, colval, nzval, xh, y)  # warm-up
+    O.spmv_plus_times_f32(rowptr, colval, nzval, xh, y)
     times = []
     t_end = time.time() + budget_s
-    while time.time() < t_end or len(times) < 3:
+    while (time.time() < t_end or len(times) < 3) and len(times) < 50:
         t0 = time.perf_counter()
         O.spmv_plus_times_f32(rowptr, colval, nzval, xh, y)
         times.append(time.perf_counter() - t0)
-        if len(times) >= 50:
-            break
     t = statistics.median(times)
-    B = spmv_bytes(A.n, A.nnz())
-    return {"value": round(B / t / 1e9, 3), "unit": "GB/s", "cores": O.num_threads(),
-            "kind": "port", "sample": "%d full SpMVs over the same R-MAT s22 CSR (median)" % len(times)}
+    return {"value": round(spmv_bytes(A.n, A.nnz()) / t / 1e9, 3), "unit": "GB/s",
+            "cores": O.num_threads(), "kind": "port",
+            "sample": "%d full SpMVs over the same R-MAT s22 CSR (median)" % len(times)}
 
+
+# ---------------------------------------------------------------------------------
+# BFS / SSSP workloads (R-MAT scale 24, 4096 x 4096 grid)
+# ---------------------------------------------------------------------------------
+
+def run_search(args, kind, graph):
+    import numpy as np
+    import torch
+    import gpugraphs as G
+    from gpugraphs import generators as gen
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if graph == "rmat24":
+        A = rmat(24, gen.W_PATTERN if kind == "bfs" else gen.W_INT_1_255, device)
+        cfg = "R-MAT scale 24, edge factor 16, symmetrised" + (
+            ", Bool pattern" if kind == "bfs" else ", Int32 weights 1..255")
+    else:
+        A = gen.grid(4096, 4096, seed=4, wkind=gen.W_PATTERN if kind == "bfs" else gen.W_F32_1_10,
+                     device=device)
+        cfg = "4096x4096 4-neighbour grid" + (", Bool pattern" if kind == "bfs" else
+                                               ", Float32 weights [1,10)")
+    n, nnz = A.n, A.nnz()
+    src = sources_for(A, 64, 11)
+    run = (lambda i: G.bfs_distances(A, int(src[i % len(src)]))) if kind == "bfs" else \
+        (lambda i: G.shortest_path(A, int(src[i % len(src)])))
+    d0 = run(0)
+    if kind == "bfs":
+        mcc = reached_edges(A, d0)
+    else:
+        mcc = reached_edges(A, torch.where(torch.isinf(d0.float()) | (d0 == I32MAX),
+                                           torch.full_like(d0, 0).to(torch.int32) + I32MAX,
+                                           torch.zeros_like(d0, dtype=torch.int32)))
+    clk = ClockSampler(local)
+    clk.start()
+    ts = time_host(run, args.steps, warmup=max(args.warmup, 3))
+    clocks = clk.stop()
+    t = sum(ts) / len(ts)
+    value = mcc / t / 1e9
+    B = (bfs_bytes if kind == "bfs" else sssp_bytes)(n, nnz)
+    peak, peak_kind = peak_hbm()
+    # e2e: the result copied back to pinned host memory each query
+    host = torch.empty(n, dtype=d0.dtype).pin_memory()
+    te = time_host(lambda i: host.copy_(run(i)), max(3, args.steps // 2), warmup=1)
+    e2e = mcc / (sum(te) / len(te)) / 1e9
+    out = {
+        "metric": "%s GTEPS (%s)" % ("BFS" if kind == "bfs" else "Bellman-Ford", cfg),
+        "value": round(value * ws, 3), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(t * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32" if kind == "bfs" else str(d0.dtype).split(".")[-1],
+        "data": "synthetic (seeded generator on the device), %d seeded sources" % len(src),
+        "config": {"workload": "%s_%s" % (kind, graph), "n": n, "nnz": nnz, "m_cc": mcc,
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": round(B / t / 1e9, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(B / t / 1e9 / peak, 4), "traffic": traffic_from_profiles("%s_%s" % (kind, graph)),
+                     "peak_kind": peak_kind, "algorithmic_bytes": B},
+        "e2e": {"value": round(e2e * ws, 3), "unit": "GTEPS", "h2d_bytes_per_step": 8,
+                "d2h_bytes_per_step": n * d0.element_size()},
+        "gpu_launches": None,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline_search(A, kind, int(src[0]), mcc)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def cpu_baseline_search(A, kind, s, mcc, max_levels=None):
+    """The reference algorithm (level-synchronous masked SpMV BFS / Jacobi Bellman-Ford,
+    restated in C with OpenMP) from one source; high-diameter graphs run a bounded
+    number of levels / rounds and extrapolate by the GPU's level count."""
+    import numpy as np
+    from oracle import oracle as O
+    rp, cv, nz = A.rowptr.cpu().numpy(), A.colval.cpu().numpy(), A.nzval.cpu().numpy()
+    t0 = time.perf_counter()
+    if kind == "bfs":
+        d, lv = O.bfs_levels(A.n, rp, cv, nz, s, max_levels=40)
+    else:
+        d, lv = O.sssp(A.n, rp, cv, nz, [s], max_rounds=40)
+    t = time.perf_counter() - t0
+    full = lv >= 0 and lv < 40
+    sample = "%s from 1 source, %s" % ("levels" if kind == "bfs" else "rounds",
+                                       "complete" if full else "first 40, time scaled to the full search")
+    if not full:
+        levels_needed = A.n  # replaced below by the measured level count when known
+        if kind == "bfs":
+            dd = O.bfs_levels(A.n, rp, cv, nz, s, max_levels=0, dry_levels=True)
+            levels_needed = dd
+        t = t / 40 * levels_needed
+    return {"value": round(mcc / t / 1e9, 5), "unit": "GTEPS", "cores": O.num_threads(),
+            "kind": "port", "sample": sample}
+
+
+# ---------------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------------
 
 def run_reference(args):
     ws, rank, local = dist_env()
@@ -317,7 +511,6 @@ def run_reference(args):
     per = sum(times) / len(times)
     B = spmv_bytes(n, len(colval))
     val = B / per / 1e9
-    cores = O.num_threads()
     out = {
         "impl": "reference",
         "metric": "SpMV GB/s (plus-times Float32, CSR, R-MAT scale 22)",
@@ -327,7 +520,8 @@ def run_reference(args):
         "data": "synthetic (seeded R-MAT generator, host copy)",
         "config": {"workload": "spmv_csr_rmat22", "n": n, "nnz": int(len(colval)), "format": "CSR",
                    "semiring": "(mul, add, second)"},
-        "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+        "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": O.num_threads(),
+                         "kind": "port",
                          "sample": "%d full SpMVs (C restatement of csr_spmv_kernel!, OpenMP); "
                                    "host graph build %.1f s untimed" % (args.steps, build_s)},
         "e2e": {"value": round(val, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
@@ -344,11 +538,19 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="spmv_csr_rmat22")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-secondary", action="store_true", help="headline SpMV only")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "spmv_csr_rmat22":
+        run_spmv_rmat22(args)
+    elif args.workload in ("bfs_rmat24", "sssp_rmat24", "bfs_grid4096", "sssp_grid4096"):
+        kind, graph = args.workload.split("_")
+        if args.steps == 50:
+            args.steps = 8
+        run_search(args, kind, graph)
     else:
-        run_ours(args)
+        raise SystemExit("unknown workload %s" % args.workload)
 
 
 if __name__ == "__main__":

@@ -175,6 +175,13 @@ static void free_mat_storage(gg_mat* A) {
     A->blocks = nullptr;
   }
   free_graph_aux(A);
+  if (A->colperm) {
+    cudaFree(A->colperm->colval_r);
+    cudaFree(A->colperm->inv);
+    cudaFree(A->colperm->xr);
+    delete A->colperm;
+    A->colperm = nullptr;
+  }
   if (A->sellplan) {
     cudaFree(A->sellplan->items);
     cudaFree(A->sellplan->multi);

@@ -337,6 +337,18 @@ struct SellPlan {
 };
 static const int kSellChunk = 512;
 
+// Frequency-ordered column labels for the plus-times SpMV kernels: relabelling the
+// columns of A by decreasing number of stored entries puts the most-gathered part of
+// x in a few contiguous cache lines, so L1 keeps it.  colval_r mirrors the matrix's
+// colval (same positions; -1 padding kept for SELL) with new 1-based labels; inv maps
+// a new label (0-based) to the original column; xr holds x in the new order.
+struct ColPerm {
+  bool enabled = false;
+  int32_t* colval_r = nullptr;
+  int32_t* inv = nullptr;
+  float* xr = nullptr;
+};
+
 static const int kBlockNnz = 256;
 static const int kShortRow = 32;
 static const int kBlockRows = 256;
@@ -373,6 +385,7 @@ struct gg_mat {
   gg::RowBlocks* blocks = nullptr;
   gg::GraphAux* aux = nullptr;
   gg::SellPlan* sellplan = nullptr;
+  gg::ColPerm* colperm = nullptr;
   int64_t max_row_len = -1;
 };
 

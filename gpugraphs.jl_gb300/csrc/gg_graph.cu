@@ -283,6 +283,19 @@ static int ensure_aux(gg_ctx* ctx, gg_mat* A) {
   return GG_OK;
 }
 
+// CSR view of A_T (1-based) and its value flags, for the batched kernels
+int graph_view(gg_ctx* ctx, gg_mat* A, const int32_t** rp, const int32_t** cv, const void** nz,
+               bool* all_odd, bool* nonneg) {
+  GG_CHECK(ensure_aux(ctx, A));
+  GraphAux* g = A->aux;
+  *rp = g->vrowptr;
+  *cv = g->vcolval;
+  *nz = g->vnz;
+  *all_odd = g->all_odd;
+  *nonneg = g->nonneg;
+  return GG_OK;
+}
+
 // which: 0 odd-valued edges, 1 all edges, 2 all edges with weights in the distance type
 static int ensure_push(gg_ctx* ctx, gg_mat* A, int which) {
   GG_CHECK(ensure_aux(ctx, A));
@@ -462,6 +475,7 @@ __global__ void k_queue_to_bitmap(const int32_t* q, int64_t nf, unsigned* bm) {
 // at a few memory round trips, which bounds high-diameter searches.
 static const int kLightDeg = 4;
 static const int kBatch = 4;
+static const int kHubDeg = 1024;  // beyond this a frontier vertex gets the whole block
 
 __device__ __forceinline__ void small_append(int32_t w, int32_t* nxt, int32_t* qg, int32_t cap,
                                              int32_t* s_nn) {
@@ -534,10 +548,24 @@ __global__ void __launch_bounds__(1024)
     }
     __syncthreads();
     const int32_t nh = s_nh;
+    // heavy vertices: a warp each up to kHubDeg out-edges, the whole block beyond
     for (int32_t h = warp; h < nh; h += nwarps) {
       const int32_t u = heavy[h];
       const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
+      if (k1 - k0 > kHubDeg) continue;
       for (int32_t k = k0 + lane; k < k1; k += 32) {
+        const int32_t w = __ldg(pcol + k);
+        const unsigned bit = 1u << (w & 31);
+        if (atomicOr(visited + (w >> 5), bit) & bit) continue;
+        dist[w] = level;
+        small_append(w, nxt, qg, cap, &s_nn);
+      }
+    }
+    for (int32_t h = 0; h < nh; ++h) {
+      const int32_t u = heavy[h];
+      const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
+      if (k1 - k0 <= kHubDeg) continue;
+      for (int32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
         const int32_t w = __ldg(pcol + k);
         const unsigned bit = 1u << (w & 31);
         if (atomicOr(visited + (w >> 5), bit) & bit) continue;
@@ -866,7 +894,23 @@ __global__ void __launch_bounds__(1024)
       const int32_t u = heavy[h];
       const T du = ld_cg(dist + u);
       const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
+      if (k1 - k0 > kHubDeg) continue;
       for (int32_t k = k0 + lane; k < k1; k += 32) {
+        const int32_t w = __ldg(pcol + k);
+        const T cand = relax_add(__ldg(pw + k), du);
+        if (!(cand < ld_cg(dist + w))) continue;
+        if (!(cand < atomic_min_t(dist + w, cand))) continue;
+        const unsigned bit = 1u << (w & 31);
+        if (atomicOr(in + (w >> 5), bit) & bit) continue;
+        small_append(w, nxt, qg, cap, &s_nn);
+      }
+    }
+    for (int32_t h = 0; h < nh; ++h) {
+      const int32_t u = heavy[h];
+      const int32_t k0 = __ldg(prow + u), k1 = __ldg(prow + u + 1);
+      if (k1 - k0 <= kHubDeg) continue;
+      const T du = ld_cg(dist + u);
+      for (int32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
         const int32_t w = __ldg(pcol + k);
         const T cand = relax_add(__ldg(pw + k), du);
         if (!(cand < ld_cg(dist + w))) continue;
@@ -1128,6 +1172,10 @@ int gg_sssp(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, int64_t nsou
   gg_mat* A = const_cast<gg_mat*>(A_T);
   GG_CHECK(ensure_aux(ctx, A));
   const bool caller = next != nullptr;
+  // several sources from the standard start: one batched pass (the reference's
+  // min-plus SpMM formulation, shortest_path.jl:88-161)
+  if (!caller && nsources > 1 && A->aux->nonneg)
+    return gg_sssp_batch(ctx, A_T, sources, nsources, dist, dist_dtype, ld, rounds_out);
   const int esz = dtype_size(dist_dtype);
   for (int64_t q = 0; q < nsources; ++q) {
     char* dcol = static_cast<char*>(dist) + q * ld * esz;

@@ -20,6 +20,7 @@
 //    walking with stride C (slice-column-major, so a warp reads C consecutive
 //    words), stopping at the first -1 padding column like sell_spmv_kernel!
 //    (SELL.jl:31-63); rows of multi-chunk slices are combined by k_sell_combine.
+#include <algorithm>
 #include <vector>
 
 #include "gg_semiring.cuh"
@@ -117,15 +118,16 @@ __global__ void __launch_bounds__(kRBWarps * 32)
       __syncwarp();
     } else {
       const int64_t si = item - nblocks;
-      const int4 sg = segs[si];  // row, k_begin, k_end, long-row index
-      if (kFiltered && !flt.keep(sg.x)) continue;
+      const int4 sg = segs[si];  // partial slot, k_begin, k_end, long-row index
+      const int32_t row = long_rows[sg.w];
+      if (kFiltered && !flt.keep(row)) continue;
       T acc = sr.neutral();
       for (int32_t base = sg.y; base < sg.z; base += 32 * 4) {
         T v[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int32_t k = base + u * 32 + lane;
-          v[u] = (k < sg.z) ? sr.mulk(k, __ldcs(colval + k), sg.x + 1) : sr.neutral();
+          v[u] = (k < sg.z) ? sr.mulk(k, __ldcs(colval + k), row + 1) : sr.neutral();
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) acc = sr.addv(acc, v[u]);
@@ -134,12 +136,12 @@ __global__ void __launch_bounds__(kRBWarps * 32)
       for (int off = 16; off > 0; off >>= 1) acc = sr.addv(acc, shfl_xor_m<T>(kFull, acc, off, 32));
       const int32_t f0 = long_first_seg[sg.w], f1 = long_first_seg[sg.w + 1];
       if (f1 - f0 == 1) {  // the whole row in one segment
-        if (lane == 0) sr.write(sg.x, acc);
+        if (lane == 0) sr.write(row, acc);
         continue;
       }
       unsigned prev = 0;
       if (lane == 0) {
-        partials[si] = acc;
+        partials[sg.x] = acc;
         __threadfence();
         prev = atomicAdd(long_count + sg.w, 1u);
       }
@@ -261,7 +263,8 @@ __global__ void __launch_bounds__(kPipeWarps * 32)
 
   // ---- long-row segments: 128-bit loads, next chunk prefetched ----
   for (int64_t si = gw; si < nsegs; si += nw) {
-    const int4 sg = segs[si];  // row, k_begin, k_end, long-row index
+    const int4 sg = segs[si];  // partial slot, k_begin, k_end, long-row index
+    const int32_t row = long_rows[sg.w];
     T acc = sr.neutral();
     const int32_t kb = sg.y, ke = sg.z;
     int32_t ka = (kb + 3) & ~3;  // first 16-byte aligned entry
@@ -307,12 +310,12 @@ __global__ void __launch_bounds__(kPipeWarps * 32)
     for (int off = 16; off > 0; off >>= 1) acc = sr.addv(acc, shfl_xor_m<T>(kFull, acc, off, 32));
     const int32_t f0 = long_first_seg[sg.w], f1 = long_first_seg[sg.w + 1];
     if (f1 - f0 == 1) {  // the whole row in one segment
-      if (lane == 0) sr.write(sg.x, acc);
+      if (lane == 0) sr.write(row, acc);
       continue;
     }
     unsigned prev = 0;
     if (lane == 0) {
-      partials[si] = acc;
+      partials[sg.x] = acc;
       __threadfence();
       prev = atomicAdd(long_count + sg.w, 1u);
     }
@@ -490,7 +493,7 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
 
 template <class SR>
 static int launch_sell(gg_ctx* ctx, gg_mat* A, const SR& sr, const void* mask, int tmask,
-                       int64_t lo, int64_t hi);
+                       int64_t lo, int64_t hi, const int32_t* colval_override = nullptr);
 
 // ---------------------------------------------------------------------------------
 // analysis: row blocks and long-row segments (built once per matrix, on first use)
@@ -515,7 +518,7 @@ int build_row_blocks(gg_ctx* ctx, gg_mat* A) {
       first_seg.push_back((int32_t)segs.size());
       for (int64_t kb = rp[r] - 1; kb < rp[r + 1] - 1; kb += kSegNnz) {
         int64_t ke = kb + kSegNnz < rp[r + 1] - 1 ? kb + kSegNnz : rp[r + 1] - 1;
-        segs.push_back(make_int4((int)r, (int)kb, (int)ke, li));
+        segs.push_back(make_int4((int)segs.size(), (int)kb, (int)ke, li));
       }
       ++r;
       continue;
@@ -530,6 +533,10 @@ int build_row_blocks(gg_ctx* ctx, gg_mat* A) {
     blocks.push_back(make_int4((int)first, (int)r, rp[first] - 1, rp[r] - 1));
   }
   first_seg.push_back((int32_t)segs.size());
+  // largest segments first: with the kernels' round-robin assignment this balances
+  // the warps (longest-processing-time order); partial slots stay in row order
+  std::stable_sort(segs.begin(), segs.end(),
+                   [](const int4& a, const int4& b) { return (a.z - a.y) > (b.z - b.y); });
 
   RowBlocks* rb = new RowBlocks();
   rb->nblocks = (int64_t)blocks.size();
@@ -655,16 +662,99 @@ static int spmv_generic(gg_ctx* ctx, gg_mat* A, int mul, int add, int accum, voi
   return launch_rowblock(ctx, A, sr, mask, tmask, lo, hi, mul == GG_OP_FIRSTI);
 }
 
+// ---------------------------------------------------------------------------------
+// column relabelling by frequency (plus-times Float32 path)
+// ---------------------------------------------------------------------------------
+__global__ void k_col_count(const int32_t* __restrict__ colval, int64_t len, int32_t* cnt) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < len;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = colval[k];
+    if (c > 0) atomicAdd(cnt + (c - 1), 1);
+  }
+}
+
+__global__ void k_col_relabel(const int32_t* __restrict__ colval, int64_t len,
+                              const int32_t* __restrict__ rank, int32_t* out) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < len;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = colval[k];
+    out[k] = c > 0 ? rank[c - 1] + 1 : c;
+  }
+}
+
+__global__ void k_gather_x(const float* __restrict__ x, const int32_t* __restrict__ inv,
+                           int64_t n, float* xr) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    xr[i] = __ldg(x + inv[i]);
+}
+
+// Builds the relabelling once per matrix.  It is kept only when the column
+// frequencies are skewed (the 1% most frequent columns hold over a quarter of the
+// entries) and x is larger than L1 could hold anyway; otherwise the natural order
+// (e.g. the locality of a grid) is better.
+static int build_colperm(gg_ctx* ctx, gg_mat* A) {
+  if (A->colperm) return GG_OK;
+  ColPerm* P = new ColPerm();
+  A->colperm = P;
+  const int64_t n = A->n;
+  const int64_t len = A->format == GG_FMT_CSR ? A->nnz : A->n_stored;
+  if (n < (1 << 16) || A->nnz == 0) return GG_OK;
+  int32_t* cnt = nullptr;
+  GG_CUDA(cudaMalloc((void**)&cnt, n * sizeof(int32_t)));
+  GG_CUDA(cudaMemsetAsync(cnt, 0, n * sizeof(int32_t), ctx->stream));
+  k_col_count<<<grid_for(ctx, len, 256), 256, 0, ctx->stream>>>(A->colval, len, cnt);
+  std::vector<int32_t> hc(n);
+  cudaError_t e = cudaMemcpyAsync(hc.data(), cnt, n * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                  ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(cnt);
+    return cuda_error(e, "column counts");
+  }
+  std::vector<uint64_t> key(n);
+  for (int64_t c = 0; c < n; ++c) key[c] = ((uint64_t)(uint32_t)(~(uint32_t)hc[c]) << 32) | (uint64_t)c;
+  std::sort(key.begin(), key.end());
+  int64_t top = 0;
+  const int64_t ntop = n / 100;
+  for (int64_t i = 0; i < ntop; ++i) top += hc[key[i] & 0xffffffffu];
+  if (top * 4 <= A->nnz) {  // not skewed: keep the natural column order
+    cudaFree(cnt);
+    return GG_OK;
+  }
+  std::vector<int32_t> inv(n), rank(n);
+  for (int64_t i = 0; i < n; ++i) {
+    inv[i] = (int32_t)(key[i] & 0xffffffffu);
+    rank[inv[i]] = (int32_t)i;
+  }
+  e = cudaMemcpyAsync(cnt, rank.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&P->colval_r, (len > 0 ? len : 1) * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&P->inv, n * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&P->xr, n * sizeof(float));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P->inv, inv.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    k_col_relabel<<<grid_for(ctx, len, 256), 256, 0, ctx->stream>>>(A->colval, len, cnt, P->colval_r);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(cnt);
+  if (e != cudaSuccess) return cuda_error(e, "column relabelling");
+  P->enabled = true;
+  return GG_OK;
+}
+
 template <class SR>
 static int launch_sell(gg_ctx* ctx, gg_mat* A, const SR& sr, const void* mask, int tmask,
-                       int64_t lo, int64_t hi) {
+                       int64_t lo, int64_t hi, const int32_t* colval_override) {
   GG_CHECK(build_sell_plan(ctx, A));
   SellPlan* P = A->sellplan;
   const int64_t C = A->slice_size;
   typedef typename SR::T T;
   if (P->nitems > 0)
     k_sell<SR><<<grid_for(ctx, P->nitems * C, 256), 256, 0, ctx->stream>>>(
-        sr, A->slice_ptr, A->colval, A->sigma > 1 ? A->perm : nullptr, C, A->m, P->items,
+        sr, A->slice_ptr, colval_override ? colval_override : A->colval,
+        A->sigma > 1 ? A->perm : nullptr, C, A->m, P->items,
         P->nitems, static_cast<T*>(P->partials), lo, hi, mask, tmask);
   if (P->nmulti > 0)
     k_sell_combine<SR><<<grid_for(ctx, P->nmulti * C, 256), 256, 0, ctx->stream>>>(
@@ -685,6 +775,14 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
     sr.nz = static_cast<const float*>(A->nzval);
     sr.x = static_cast<const float*>(x);
     sr.y = static_cast<float*>(y);
+    GG_CHECK(build_colperm(ctx, A));
+    const int32_t* colval = A->colval;
+    if (A->colperm->enabled) {
+      k_gather_x<<<grid_for(ctx, A->n, 256), 256, 0, ctx->stream>>>(
+          static_cast<const float*>(x), A->colperm->inv, A->n, A->colperm->xr);
+      sr.x = A->colperm->xr;
+      colval = A->colperm->colval_r;
+    }
     if (A->format == GG_FMT_CSR) {
       GG_CHECK(build_row_blocks(ctx, A));
       RowBlocks* rb = A->blocks;
@@ -700,12 +798,12 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
       const int64_t cap = (int64_t)ctx->num_sms * per_sm;  // one resident wave
       if (grid > cap) grid = cap;
       k_spmv_pipe<SRPlusTimesF32><<<(int)grid, kPipeWarps * 32, 0, ctx->stream>>>(
-          sr, A->rowptr, A->colval, rb->blocks, rb->nblocks, rb->segs, rb->nsegs,
+          sr, A->rowptr, colval, rb->blocks, rb->nblocks, rb->segs, rb->nsegs,
           rb->long_first_seg, rb->long_rows, rb->long_count, static_cast<float*>(rb->partials));
       GG_CUDA(cudaGetLastError());
       return GG_OK;
     }
-    return launch_sell(ctx, A, sr, nullptr, 0, 0, 0);
+    return launch_sell(ctx, A, sr, nullptr, 0, 0, 0, colval);
   }
   switch (tc) {
     case GG_BOOL: return spmv_generic<GG_BOOL>(ctx, A, mul, add, accum, y, ty, x, tx, mask, tmask, lo, hi);

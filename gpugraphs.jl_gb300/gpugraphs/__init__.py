@@ -11,7 +11,8 @@ from .algebra import (GPUGraphs_add, GPUGraphs_any, GPUGraphs_band, GPUGraphs_bo
                       GPUGraphs_minus, GPUGraphs_mul, GPUGraphs_pair, GPUGraphs_rminus,
                       GPUGraphs_safe_add, GPUGraphs_second, GPUGraphs_secondi,
                       GPUGraphs_secondj, monoid_absorb, monoid_neutral)
-from .algorithms import (bfs_distances, bfs_distances_, bfs_parents, bfs_parents_,
+from .algorithms import (bfs_distances, bfs_distances_, bfs_distances_batch, bfs_parents,
+                         bfs_parents_,
                          shortest_path, shortest_path_)
 from .errors import (ArgumentError, BoundsError, DimensionMismatch, GPUGraphsError,
                      SpmmAssertionError, UnsupportedError)
@@ -21,7 +22,7 @@ from .storage import (AbstractSparseGPUMatrix, SparseGPUMatrixCSR, SparseGPUMatr
 
 __all__ = [
     "AbstractSparseGPUMatrix", "SparseGPUMatrixCSR", "SparseGPUMatrixSELL", "gpu_spmv_",
-    "gpu_spmm_", "sprand_gpu", "bfs_distances", "bfs_distances_", "bfs_parents",
+    "gpu_spmm_", "sprand_gpu", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
     "bfs_parents_", "shortest_path", "shortest_path_", "monoid_neutral", "monoid_absorb", "synchronize",
     "GPUGraphs_add", "GPUGraphs_safe_add", "GPUGraphs_mul", "GPUGraphs_second",
     "GPUGraphs_band", "GPUGraphs_bor", "GPUGraphs_any", "GPUGraphs_secondi", "GPUGraphs_max",

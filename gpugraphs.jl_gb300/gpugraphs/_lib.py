@@ -36,6 +36,14 @@ SIGNATURES = {
     "gg_bfs_levels": [P, P, I64, P, I64, PI64],
     "gg_bfs_parents": [P, P, I64, P, I64, I, PI64],
     "gg_sssp": [P, P, P, I64, P, P, I, I64, PI64],
+    "gg_bfs_levels_batch": [P, P, P, I64, P, I64, PI64],
+    "gg_sssp_batch": [P, P, P, I64, P, I, I64, PI64],
+    "gg_server_create": [P, I64, PP],
+    "gg_server_add_graph": [P, P, PI],
+    "gg_server_submit": [P, I, I, I64, P, I, P, PI64],
+    "gg_server_poll": [P, PI64, ctypes.POINTER(ctypes.c_double), I64, PI64, PI64],
+    "gg_server_stats": [P, PI64, PI64, PI64],
+    "gg_server_destroy": [P],
     "gg_bfs_levels_noalloc": [P, P, P, I, I64, I64, I64, P, P, PI64],
     "gg_gen_rmat_edges": [P, I, I64, D, D, D, U64, I, P, P, P],
     "gg_gen_er_edges": [P, I64, I64, U64, I, P, P, P],

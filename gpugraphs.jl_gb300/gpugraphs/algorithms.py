@@ -57,6 +57,23 @@ def bfs_distances(A_T, source, use_mask=True):
     return dist
 
 
+def bfs_distances_batch(A_T, sources):
+    """Batched bfs_distances: an n x S column-major Int32 matrix whose column q is
+    bfs_distances(A_T, sources[q]).  Up to 256 sources share each pass over the graph
+    (gg_bfs_levels_batch); the reference has no multi-source BFS."""
+    _check_matrix(A_T)
+    n = A_T.size(1)
+    src = _sources(sources)
+    dist = torch.empty((len(src), n), dtype=torch.int32, device=A_T.device).T
+    L = core.lib()
+    lv = ctypes.c_int64()
+    with torch.cuda.device(A_T.device):
+        check(L.gg_bfs_levels_batch(core.ctx(A_T.device), A_T.handle,
+                                    src.ctypes.data_as(ctypes.c_void_p), len(src), core.ptr(dist),
+                                    n, ctypes.byref(lv)), L)
+    return dist
+
+
 def bfs_parents_(A_T, source, parents, curr=None, next=None, to_explore=None, batch_size=8,
                  rule=PARENT_FORMAT_DEFAULT):
     """bfs_parents!(A_T, source, parents, curr, next, to_explore, batch_size)

@@ -88,8 +88,12 @@ enum {
   GG_PARENT_MAX_INDEX = 2       /* largest frontier column index (src/algebra.jl:35 via src/spmv/SELL.jl:100-133) */
 };
 
+/* query kinds served by gg_server */
+enum { GG_QUERY_BFS = 1, GG_QUERY_SSSP = 2, GG_QUERY_SPMV_ITER = 3 };
+
 typedef struct gg_ctx gg_ctx; /* device, stream, scratch arena */
 typedef struct gg_mat gg_mat; /* a CSR or SELL-C-sigma matrix resident on the device */
+typedef struct gg_server gg_server; /* continuous-batching query server */
 
 /* ---- library / context ---------------------------------------------------- */
 
@@ -228,6 +232,28 @@ int gg_sssp(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, int64_t nsou
             void* next, int dist_dtype, int64_t ld, int64_t* rounds_out);
 
 /*
+ * Batched BFS: column q of dist (n x S, column-major, leading dimension ld) receives
+ * bfs_distances(A_T, sources[q]) -- levels over edges with odd / true values,
+ * typemax(Int32) when unreached.  Up to 256 sources share one pass over the graph
+ * per level (frontiers and visited sets packed as bits).  The reference has no
+ * multi-source BFS; this is the batched form of bfs_distances (src/algorithms/
+ * bfs.jl:1-29).  Synchronous.  levels_out (may be NULL): levels summed over groups.
+ */
+int gg_bfs_levels_batch(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, int64_t S,
+                        int32_t* dist, int64_t ld, int64_t* levels_out);
+
+/*
+ * Batched shortest paths from the standard start: column q of dist receives
+ * shortest_path(A_T, sources[q]), as the reference's multi-source shortest_path
+ * (src/algorithms/shortest_path.jl:88-161) computes with a min-plus SpMM per round.
+ * 32 sources per pass, relaxing only from vertices that changed in the previous
+ * round.  Needs non-negative weights (GG_ERR_UNSUPPORTED otherwise; gg_sssp then
+ * runs the reference's Jacobi rounds).  gg_sssp routes several sources here.
+ */
+int gg_sssp_batch(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, int64_t S, void* dist,
+                  int dist_dtype, int64_t ld, int64_t* rounds_out);
+
+/*
  * BFS levels for callers that cannot allocate device memory (no counterpart in the
  * reference).  Same result as gg_bfs_levels -- dist[v] = hop level along edges with
  * odd / true stored values (all stored edges when nzval is NULL), dist[source] = 0,
@@ -245,6 +271,35 @@ int gg_sssp(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, int64_t nsou
 int gg_bfs_levels_noalloc(const int32_t* rowptr, const int32_t* colval, const void* nzval,
                           int dtype, int64_t n, int64_t nnz, int64_t source, int32_t* dist,
                           void* stream, int64_t* levels_out);
+
+/* ---- serving (no reference counterpart) ------------------------------------------
+ * A scheduler thread keeps per (graph, query kind) executors with fixed slots --
+ * 256 BFS slots (bits of packed frontier words), 32 shortest-path columns, 32 SpMV
+ * columns -- and advances every active slot one level / round / step per tick.
+ * Requests arriving meanwhile join free slots at the next tick (continuous
+ * batching); executors are created only when cudaMemGetInfo shows their memory plus
+ * reserve_bytes free (admission by free HBM), otherwise requests wait.  Results
+ * equal the single-query functions: BFS -> gg_bfs_levels semantics with unreached =
+ * typemax(Int32); SSSP -> gg_sssp (non-negative weights); SPMV_ITER -> `steps` times
+ * x <- A*x with the plus-times Float32 semiring. */
+
+/* Server bound to ctx's device, with its own stream and worker thread. */
+int gg_server_create(gg_ctx* ctx, int64_t reserve_bytes, gg_server** out);
+/* Registers a resident graph (A_T must outlive the server); before the first submit. */
+int gg_server_add_graph(gg_server* server, const gg_mat* A_T, int* graph_id);
+/* Queues a query.  out: device array of n results (Int32 levels, distances of the
+ * shortest_path element type, or Float32); x: device start vector for SPMV_ITER. */
+int gg_server_submit(gg_server* server, int kind, int graph, int64_t source, const float* x,
+                     int steps, void* out, int64_t* request_id);
+/* Non-blocking: up to max completed request ids with their latencies (seconds from
+ * submit to result in `out`); inflight receives the number still pending. */
+int gg_server_poll(gg_server* server, int64_t* ids, double* latency_s, int64_t max,
+                   int64_t* ndone, int64_t* inflight);
+/* Ticks run, executor creations deferred for lack of free HBM, executor bytes held. */
+int gg_server_stats(gg_server* server, int64_t* ticks, int64_t* admission_waits,
+                    int64_t* exec_bytes);
+/* Stops the worker and frees the executors (queued requests are dropped). */
+int gg_server_destroy(gg_server* server);
 
 /* ---- seeded synthetic inputs (no reference counterpart: the reference's benchmark
  *      draws its inputs with Julia's sprand / Graphs.jl generators,

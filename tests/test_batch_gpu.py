@@ -1,0 +1,85 @@
+"""GPU parity of the batched engines (many sources in one pass): batched BFS levels
+and batched shortest paths equal the per-source results column by column, exactly."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+import gpugraphs as G
+from gpugraphs import generators as gen
+from oracle import oracle as O
+from helpers import csr_from_scipy, golden_graphs, undirected_csr
+
+pytestmark = pytest.mark.gpu
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def csr_host(A):
+    return host(A.rowptr), host(A.colval), host(A.nzval)
+
+
+def test_bfs_batch_rmat_two_groups():
+    A = gen.rmat(13, 16, seed=31, wkind=gen.W_PATTERN)
+    rp, cv, nz = csr_host(A)
+    n = A.n
+    rng = np.random.default_rng(31)
+    src = rng.integers(1, n + 1, 300)  # two groups: 256 + 44
+    D = host(G.bfs_distances_batch(A, src))
+    assert D.shape == (n, 300)
+    for q in list(range(0, 300, 23)) + [255, 256, 299]:
+        ref, _ = O.bfs_levels(n, rp, cv, nz, int(src[q]))
+        assert (D[:, q] == ref).all(), q
+    S = G.SparseGPUMatrixSELL(A, 32, 64)
+    D2 = host(G.bfs_distances_batch(S, src[:40]))
+    assert (D2 == D[:, :40]).all()
+
+
+def test_bfs_batch_odd_values_and_directed():
+    n = 2500
+    rng = np.random.default_rng(32)
+    M = sp.random(n, n, density=0.003, random_state=rng, format="csr")
+    M.data = rng.integers(1, 5, M.nnz).astype(np.int32)
+    rp, cv, nz = csr_from_scipy(M.T.tocsr().astype(np.int32))
+    B = G.SparseGPUMatrixCSR(n, n, rp, cv, nz)
+    src = np.arange(1, n + 1, 97)
+    D = host(G.bfs_distances_batch(B, src))
+    for q, s in enumerate(src):
+        ref, _ = O.bfs_levels(n, rp, cv, nz, int(s))
+        assert (D[:, q] == ref).all()
+
+
+@pytest.mark.parametrize("name", ["ba30", "dm30"])
+def test_sssp_batch_golden_all_sources(name):
+    g = golden_graphs()
+    n = g[name + "_hop"].shape[0]
+    rp, cv, nz = undirected_csr(g[name + "_edges"], n, weights=g[name + "_w"])
+    B = G.SparseGPUMatrixCSR(n, n, rp, cv, nz)
+    L = G.core.lib()
+    d = torch.empty((n, n), dtype=torch.int32, device="cuda").T.contiguous().T
+    src = np.arange(1, n + 1, dtype=np.int64)
+    import ctypes
+    rc = L.gg_sssp_batch(G.core.ctx(), B.handle, src.ctypes.data_as(ctypes.c_void_p), n,
+                         G.core.ptr(d), 2, n, None)
+    assert rc == 0
+    assert (host(d) == g[name + "_dijkstra"]).all()
+
+
+def test_sssp_batch_int_rmat_and_float_grid():
+    A = gen.rmat(12, 16, seed=33, wkind=gen.W_INT_1_255)
+    rp, cv, nz = csr_host(A)
+    rng = np.random.default_rng(33)
+    src = rng.integers(1, A.n + 1, 40)
+    ref, _ = O.sssp(A.n, rp, cv, nz, src)
+    assert (host(G.shortest_path(A, src)) == ref).all()  # routed to the batched engine
+    Gf = gen.grid(60, 50, seed=34, wkind=gen.W_F32_1_10)
+    rp, cv, nz = csr_host(Gf)
+    src = rng.integers(1, Gf.n + 1, 33)
+    ref, _ = O.sssp(Gf.n, rp, cv, nz, src)
+    got = host(G.shortest_path(Gf, src))
+    assert got.dtype == np.float32 and (got == ref).all()
+    S = G.SparseGPUMatrixSELL(Gf, 16, 32)
+    assert (host(G.shortest_path(S, src)) == ref).all()

@@ -388,3 +388,27 @@ def test_spmm_assertions():
     with pytest.raises(G.SpmmAssertionError):
         G.gpu_spmm_(torch.zeros((20, 4), device="cuda"), B, torch.zeros((30, 4), device="cuda"),
                     mask=torch.ones(20, device="cuda"), range=(1, 3))
+
+
+def test_spmv_generic_semirings_on_rmat():
+    """Long rows (segments) and short-row blocks of an R-MAT graph through the
+    generic-semiring kernels, against the oracle."""
+    from gpugraphs import generators as gen
+    A = gen.rmat(14, 16, seed=12, wkind=gen.W_INT_1_255)
+    rowptr, colval, nz = host(A.rowptr), host(A.colval), host(A.nzval)
+    n = A.n
+    x = np.random.default_rng(12).integers(0, 1000, n).astype(np.int32)
+    for mul, add, accum in ((O.SAFE_ADD, O.MIN, O.MIN), (O.MUL, O.MAX, O.SECOND), (O.BAND, O.BOR, O.SECOND)):
+        y0 = np.full(n, 7, np.int32)
+        yo = y0.copy()
+        assert O.csr_spmv(n, n, rowptr, colval, nz, yo, x, mul, add, accum) == O.OK
+        y = dev(y0)
+        G.gpu_spmv_(y, A, dev(x), mul=OPS[mul], add=OPS[add], accum=OPS[accum])
+        assert (host(y) == yo).all()
+    # plus-times Float32 on the same structure (long rows within tolerance)
+    B = G.SparseGPUMatrixCSR(n, n, rowptr, colval, nz.astype(np.float32))
+    xf = np.random.default_rng(13).random(n, dtype=np.float32)
+    y = torch.zeros(n, dtype=torch.float32, device="cuda")
+    G.gpu_spmv_(y, B, dev(xf))
+    ref = B.to_scipy().astype(np.float64) @ xf.astype(np.float64)
+    np.testing.assert_allclose(host(y), ref, rtol=RTOL, atol=1e-6)
