@@ -156,6 +156,7 @@ __global__ void k_invert_perm(int64_t m, const int32_t* perm, int32_t* iperm) {
     iperm[perm[t] - 1] = (int32_t)t;
 }
 
+static void free_mat_storage(gg_mat* A);
 static void free_mat_storage(gg_mat* A) {
   cudaFree(A->rowptr);
   cudaFree(A->colval);
@@ -175,12 +176,31 @@ static void free_mat_storage(gg_mat* A) {
     A->blocks = nullptr;
   }
   free_graph_aux(A);
+  if (A->sell_copy) {
+    free_mat_storage(A->sell_copy);
+    delete A->sell_copy;
+    A->sell_copy = nullptr;
+  }
   if (A->colperm) {
     cudaFree(A->colperm->colval_r);
     cudaFree(A->colperm->inv);
     cudaFree(A->colperm->xr);
     delete A->colperm;
     A->colperm = nullptr;
+  }
+  if (A->hubplan) {
+    cudaFree(A->hubplan->hubs);
+    cudaFree(A->hubplan->pieces);
+    cudaFree(A->hubplan->acc);
+    delete A->hubplan;
+    A->hubplan = nullptr;
+  }
+  if (A->mmplan) {
+    cudaFree(A->mmplan->segs);
+    cudaFree(A->mmplan->first);
+    cudaFree(A->mmplan->rows);
+    delete A->mmplan;
+    A->mmplan = nullptr;
   }
   if (A->sellplan) {
     cudaFree(A->sellplan->items);

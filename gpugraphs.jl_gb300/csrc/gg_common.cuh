@@ -335,7 +335,33 @@ struct SellPlan {
   int4* multi = nullptr;
   void* partials = nullptr;  // [npartials * C] accumulators (8 bytes each)
 };
-static const int kSellChunk = 512;
+static const int kSellChunk = 128;
+
+// SpMM long-row segments.  Rows (CSR) or slices (SELL) longer than kSegMM entries
+// are cut into pieces of kSegMM; one warp folds one piece for all dense columns into
+// partials[slot * k + j] and a second pass folds a row's pieces in order.
+// segs: (row, first entry, end entry, slot) for CSR -- entries 0-based positions in
+// colval; (stored row, first slice column, end slice column, slot) for SELL.
+// first[li] .. first[li + 1] are the slots of long row li = rows[li].
+struct MMPlan {
+  int64_t nseg = 0, nlong = 0;
+  int4* segs = nullptr;
+  int32_t* first = nullptr;
+  int32_t* rows = nullptr;
+};
+static const int kSegMM = 256;
+
+// Hub vertices of a graph's CSR view for the batched searches: rows longer than
+// kHubDegB entries, cut into pieces of kHubPieceB entries (0-based positions in
+// colval).  pieces: (hub index, first entry, end entry, 0); hubs: vertex (0-based).
+struct HubPlan {
+  int64_t nhub = 0, npiece = 0;
+  int32_t* hubs = nullptr;
+  int4* pieces = nullptr;
+  void* acc = nullptr;  // per-hub accumulators of the batched BFS (8 words per hub)
+};
+static const int kHubDegB = 2048;
+static const int kHubPieceB = 2048;
 
 // Frequency-ordered column labels for the plus-times SpMV kernels: relabelling the
 // columns of A by decreasing number of stored entries puts the most-gathered part of
@@ -386,7 +412,15 @@ struct gg_mat {
   gg::GraphAux* aux = nullptr;
   gg::SellPlan* sellplan = nullptr;
   gg::ColPerm* colperm = nullptr;
+  gg::MMPlan* mmplan = nullptr;
+  gg::HubPlan* hubplan = nullptr;
+  gg_mat* sell_copy = nullptr;  // CSR handles: SELL-32 copy (rows sorted by length) for plus-times
   int64_t max_row_len = -1;
+  // tuned choices (gg_tune): plus-times SpMV kernel (0 = built-in rule, 1 = CSR row
+  // blocks, 2 = the SELL copy), rows per row block, SpMM columns per lane (0 = 1)
+  int tuned_spmv = 0;
+  int block_rows = 0;
+  int mm_cpl = 0;
 };
 
 namespace gg {

@@ -6,8 +6,13 @@
 // broadcasts them by shuffle; every lane folds its (row, j) sequentially in storage
 // order -- the order of csr_spmm_kernel! (src/spmm/CSR.jl:3-35), so results equal
 // the reference's bit for bit, including its early exit on the absorbing value.
+// Rows longer than kSegMM entries (hubs of power-law graphs) are cut into pieces
+// folded by separate warps and combined in order by a second pass: exact for every
+// associative monoid, within rounding for Float32/Float64 sums.
 // With a row-major dense operand (the batched-query layout) each gathered B row is
 // one contiguous 128-byte read.
+#include <vector>
+
 #include "gg_semiring.cuh"
 
 namespace gg {
@@ -32,85 +37,186 @@ struct SRPlusTimesF32MM {
   }
 };
 
-// CSR: one warp per row of [row_lo, row_lo + nrows)
-template <class SR>
-__global__ void __launch_bounds__(256)
-    k_csr_spmm(SR sr, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colval,
-               int64_t row_lo, int64_t nrows, int64_t kcols, const void* mask, int tmask) {
+// Fold entries [k0, k1) of row r1 (1-based) for dense columns j0 + 32 c (c < CPL) in
+// storage order, stopping at the absorbing value like csr_spmm_kernel!
+// (src/spmm/CSR.jl:3-35).  The warp loads 32 column indices at a time and broadcasts
+// them; each lane keeps 8 x CPL gathers in flight.
+template <class SR, int CPL>
+__device__ __forceinline__ void fold_csr(const SR& sr, const int32_t* __restrict__ colval,
+                                         int32_t k0, int32_t k1, int64_t r1, int64_t j0,
+                                         int64_t jn_abs, int lane, typename SR::T (&acc)[CPL]) {
   typedef typename SR::T T;
-  const int lane = threadIdx.x & 31;
-  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t t = w0; t < nrows; t += nw) {
-    const int64_t r = row_lo + t;
-    if (mask && raw_is_zero(load_raw(mask, tmask, r), tmask)) continue;
-    const int32_t k0 = __ldg(rowptr + r) - 1, k1 = __ldg(rowptr + r + 1) - 1;
-    for (int64_t jb = 0; jb < kcols; jb += 32) {
-      const int64_t j = jb + lane;
-      const bool active = j < kcols;
-      T acc = sr.neutral();
-      bool done = !active;
-      for (int32_t base = k0; base < k1; base += 32) {
-        const int32_t kk = base + lane;
-        const int32_t col_l = kk < k1 ? __ldg(colval + kk) : 1;
-        const int n = (k1 - base) < 32 ? (k1 - base) : 32;
-        int i = 0;
-        for (; i + 4 <= n; i += 4) {
-          const int32_t c0 = __shfl_sync(kFullMM, col_l, i);
-          const int32_t c1 = __shfl_sync(kFullMM, col_l, i + 1);
-          const int32_t c2 = __shfl_sync(kFullMM, col_l, i + 2);
-          const int32_t c3 = __shfl_sync(kFullMM, col_l, i + 3);
-          if (!done) {
-            const T v0 = sr.mulk(base + i, c0, r + 1, j);
-            const T v1 = sr.mulk(base + i + 1, c1, r + 1, j);
-            const T v2 = sr.mulk(base + i + 2, c2, r + 1, j);
-            const T v3 = sr.mulk(base + i + 3, c3, r + 1, j);
-            acc = sr.addv(acc, v0);
-            if (sr.is_absorb(acc)) done = true;
-            if (!done) { acc = sr.addv(acc, v1); if (sr.is_absorb(acc)) done = true; }
-            if (!done) { acc = sr.addv(acc, v2); if (sr.is_absorb(acc)) done = true; }
-            if (!done) { acc = sr.addv(acc, v3); if (sr.is_absorb(acc)) done = true; }
-          }
-        }
-        for (; i < n; ++i) {
-          const int32_t c = __shfl_sync(kFullMM, col_l, i);
-          if (!done) {
-            acc = sr.addv(acc, sr.mulk(base + i, c, r + 1, j));
-            if (sr.is_absorb(acc)) done = true;
+  bool done[CPL];
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) {
+    acc[c] = sr.neutral();
+    done[c] = j0 + 32 * c >= jn_abs;
+  }
+  for (int32_t base = k0; base < k1; base += 32) {
+    const int32_t kk = base + lane;
+    const int32_t col_l = kk < k1 ? __ldg(colval + kk) : 1;
+    const int n = (k1 - base) < 32 ? (k1 - base) : 32;
+    int i = 0;
+    for (; i + 8 <= n; i += 8) {
+      int32_t cidx[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) cidx[u] = __shfl_sync(kFullMM, col_l, i + u);
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        if (done[c]) continue;
+        T v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = sr.mulk(base + i + u, cidx[u], r1, j0 + 32 * c);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (!done[c]) {
+            acc[c] = sr.addv(acc[c], v[u]);
+            if (sr.is_absorb(acc[c])) done[c] = true;
           }
         }
       }
-      if (active) sr.write_mm(r, j, acc);
+    }
+    for (; i < n; ++i) {
+      const int32_t cc = __shfl_sync(kFullMM, col_l, i);
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        if (!done[c]) {
+          acc[c] = sr.addv(acc[c], sr.mulk(base + i, cc, r1, j0 + 32 * c));
+          if (sr.is_absorb(acc[c])) done[c] = true;
+        }
+      }
     }
   }
 }
 
-// SELL: one warp per stored row, walking its slice with stride C
-template <class SR>
+// CSR: items [0, nseg) are pieces of rows longer than kSegMM (their partials go to
+// partials[slot * jn + j - jlo]); items [nseg, nseg + nrows) are the rows of
+// [row_lo, row_lo + nrows), one warp per row, lane per dense column (CPL columns per
+// lane and pass), rows longer than kSegMM skipped.  Columns [jlo, jlo + jn).
+template <class SR, int CPL>
 __global__ void __launch_bounds__(256)
-    k_sell_spmm(SR sr, const int32_t* __restrict__ slice_ptr, const int32_t* __restrict__ colval,
-                const int32_t* __restrict__ perm, int64_t C, int64_t s_lo, int64_t s_hi,
-                int64_t kcols, int64_t range_lo, int64_t range_hi, const void* mask, int tmask) {
+    k_csr_spmm(SR sr, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colval,
+               int64_t row_lo, int64_t nrows, int64_t jlo, int64_t jn, const void* mask, int tmask,
+               const int4* __restrict__ segs, int64_t nseg, typename SR::T* partials) {
   typedef typename SR::T T;
   const int lane = threadIdx.x & 31;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t t = s_lo + w0; t < s_hi; t += nw) {
+  for (int64_t t = w0; t < nseg + nrows; t += nw) {
+    int64_t r;
+    int32_t k0, k1, slot = -1;
+    if (t < nseg) {
+      const int4 sg = segs[t];
+      r = sg.x;
+      if (r < row_lo || r >= row_lo + nrows) continue;
+      k0 = sg.y;
+      k1 = sg.z;
+      slot = sg.w;
+    } else {
+      r = row_lo + (t - nseg);
+      k0 = __ldg(rowptr + r) - 1;
+      k1 = __ldg(rowptr + r + 1) - 1;
+      if (k1 - k0 > kSegMM) continue;
+    }
+    if (mask && raw_is_zero(load_raw(mask, tmask, r), tmask)) continue;
+    for (int64_t jb = 0; jb < jn; jb += 32 * CPL) {
+      T acc[CPL];
+      fold_csr<SR, CPL>(sr, colval, k0, k1, r + 1, jlo + jb + lane, jlo + jn, lane, acc);
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        const int64_t jj = jb + lane + 32 * c;
+        if (jj >= jn) continue;
+        if (slot >= 0) partials[(int64_t)slot * jn + jj] = acc[c];
+        else sr.write_mm(r, jlo + jj, acc[c]);
+      }
+    }
+  }
+}
+
+// SELL: fold stored row t over slice columns [c0, c1) with stride C, stopping at the
+// first -1 padding column or the absorbing value
+template <class SR>
+__device__ __forceinline__ typename SR::T fold_sell(const SR& sr, const int32_t* __restrict__ colval,
+                                                    int64_t i0, int64_t i1, int64_t C, int64_t r1,
+                                                    int64_t j) {
+  typename SR::T acc = sr.neutral();
+  for (int64_t i = i0; i < i1; i += C) {
+    const int32_t col = __ldg(colval + i);
+    if (col == -1 || sr.is_absorb(acc)) break;
+    acc = sr.addv(acc, sr.mulk(i, col, r1, j));
+  }
+  return acc;
+}
+
+// SELL: items [0, nseg) are pieces of the rows of slices wider than kSegMM, items
+// [nseg, nseg + s_hi - s_lo) one warp per stored row (rows of wide slices skipped)
+template <class SR>
+__global__ void __launch_bounds__(256)
+    k_sell_spmm(SR sr, const int32_t* __restrict__ slice_ptr, const int32_t* __restrict__ colval,
+                const int32_t* __restrict__ perm, int64_t C, int64_t s_lo, int64_t s_hi,
+                int64_t jlo, int64_t jn, int64_t range_lo, int64_t range_hi, const void* mask,
+                int tmask, const int4* __restrict__ segs, int64_t nseg, typename SR::T* partials) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t it = w0; it < nseg + (s_hi - s_lo); it += nw) {
+    int64_t t, cb, ce;
+    int slot = -1;
+    if (it < nseg) {
+      const int4 sg = segs[it];
+      t = sg.x;
+      cb = sg.y;
+      ce = sg.z;
+      slot = sg.w;
+      if (t < s_lo || t >= s_hi) continue;
+    } else {
+      t = s_lo + (it - nseg);
+      const int64_t s = t / C;
+      ce = ((int64_t)slice_ptr[s + 1] - slice_ptr[s]) / C;
+      if (ce > kSegMM) continue;
+      cb = 0;
+    }
     const int64_t s = t / C, o = t - s * C;
     const int64_t r1 = perm ? (int64_t)perm[t] : t + 1;
     if (range_lo > 0 && (r1 < range_lo || r1 > range_hi)) continue;
     if (mask && raw_is_zero(load_raw(mask, tmask, r1 - 1), tmask)) continue;
-    const int64_t i0 = (int64_t)slice_ptr[s] - 1 + o, i1 = (int64_t)slice_ptr[s + 1] - 1;
-    for (int64_t jb = 0; jb < kcols; jb += 32) {
-      const int64_t j = jb + lane;
-      if (j >= kcols) continue;
+    const int64_t base = (int64_t)slice_ptr[s] - 1 + o;
+    for (int64_t jb = 0; jb < jn; jb += 32) {
+      const int64_t jj = jb + lane;
+      if (jj >= jn) continue;
+      const typename SR::T acc = fold_sell(sr, colval, base + cb * C, base + ce * C, C, r1, jlo + jj);
+      if (slot >= 0) partials[(int64_t)slot * jn + jj] = acc;
+      else sr.write_mm(r1 - 1, jlo + jj, acc);
+    }
+  }
+}
+
+// second pass over long rows: fold each row's piece partials in order
+template <class SR>
+__global__ void __launch_bounds__(256)
+    k_spmm_combine(SR sr, const int32_t* __restrict__ rows, const int32_t* __restrict__ first,
+                   int64_t nlong, const int32_t* __restrict__ perm, bool sell, int64_t row_lo,
+                   int64_t row_hi, int64_t jlo, int64_t jn, const void* mask, int tmask,
+                   const typename SR::T* __restrict__ partials) {
+  typedef typename SR::T T;
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t li = w0; li < nlong; li += nw) {
+    const int64_t t = rows[li];
+    const int64_t r0 = sell ? (perm ? (int64_t)perm[t] - 1 : t) : t;  // original row, 0-based
+    if (r0 < row_lo || r0 >= row_hi) continue;
+    if (mask && raw_is_zero(load_raw(mask, tmask, r0), tmask)) continue;
+    const int32_t q0 = first[li], q1 = first[li + 1];
+    for (int64_t jb = 0; jb < jn; jb += 32) {
+      const int64_t jj = jb + lane;
+      if (jj >= jn) continue;
       T acc = sr.neutral();
-      for (int64_t i = i0; i < i1; i += C) {
-        const int32_t col = __ldg(colval + i);
-        if (col == -1 || sr.is_absorb(acc)) break;
-        acc = sr.addv(acc, sr.mulk(i, col, r1, j));
+      for (int32_t q = q0; q < q1; ++q) {
+        acc = sr.addv(acc, partials[(int64_t)q * jn + jj]);
+        if (sr.is_absorb(acc)) break;
       }
-      sr.write_mm(r1 - 1, j, acc);
+      sr.write_mm(r0, jlo + jj, acc);
     }
   }
 }
@@ -122,28 +228,127 @@ static int grid_mm(gg_ctx* ctx, int64_t warps) {
   return (int)(g < 1 ? 1 : g);
 }
 
+// long-row pieces, built once per matrix from rowptr (CSR) or slice_ptr (SELL)
+static int build_mm_plan(gg_ctx* ctx, gg_mat* A) {
+  if (A->mmplan) return GG_OK;
+  std::vector<int4> segs;
+  std::vector<int32_t> first, rows;
+  if (A->format == GG_FMT_CSR) {
+    const int64_t m = A->m;
+    std::vector<int32_t> rp(m + 1);
+    GG_CUDA(cudaMemcpyAsync(rp.data(), A->rowptr, (m + 1) * sizeof(int32_t),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int64_t r = 0; r < m; ++r) {
+      const int64_t k0 = rp[r] - 1, k1 = rp[r + 1] - 1;
+      if (k1 - k0 <= kSegMM) continue;
+      rows.push_back((int32_t)r);
+      first.push_back((int32_t)segs.size());
+      for (int64_t kb = k0; kb < k1; kb += kSegMM) {
+        const int64_t ke = kb + kSegMM < k1 ? kb + kSegMM : k1;
+        segs.push_back(make_int4((int)r, (int)kb, (int)ke, (int)segs.size()));
+      }
+    }
+  } else {
+    const int64_t ns = A->nslices, C = A->slice_size;
+    std::vector<int32_t> sp(ns + 1);
+    GG_CUDA(cudaMemcpyAsync(sp.data(), A->slice_ptr, (ns + 1) * sizeof(int32_t),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int64_t s = 0; s < ns; ++s) {
+      const int64_t L = C > 0 ? ((int64_t)sp[s + 1] - sp[s]) / C : 0;
+      if (L <= kSegMM) continue;
+      for (int64_t o = 0; o < C && s * C + o < A->m; ++o) {
+        const int64_t t = s * C + o;
+        rows.push_back((int32_t)t);
+        first.push_back((int32_t)segs.size());
+        for (int64_t cb = 0; cb < L; cb += kSegMM) {
+          const int64_t ce = cb + kSegMM < L ? cb + kSegMM : L;
+          segs.push_back(make_int4((int)t, (int)cb, (int)ce, (int)segs.size()));
+        }
+      }
+    }
+  }
+  first.push_back((int32_t)segs.size());
+  MMPlan* P = new MMPlan();
+  P->nseg = (int64_t)segs.size();
+  P->nlong = (int64_t)rows.size();
+  cudaError_t e = cudaSuccess;
+  auto up = [&](void** dst, const void* src, size_t bytes) {
+    if (e != cudaSuccess) return;
+    e = cudaMalloc(dst, bytes > 0 ? bytes : 16);
+    if (e == cudaSuccess && bytes > 0)
+      e = cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  };
+  up((void**)&P->segs, segs.data(), segs.size() * sizeof(int4));
+  up((void**)&P->first, first.data(), first.size() * sizeof(int32_t));
+  up((void**)&P->rows, rows.data(), rows.size() * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(P->segs);
+    cudaFree(P->first);
+    cudaFree(P->rows);
+    delete P;
+    return cuda_error(e, "SpMM long-row analysis");
+  }
+  A->mmplan = P;
+  return GG_OK;
+}
+
+// partial buffers are bounded: wide dense operands run in column windows
+static const int64_t kMMPartialBytes = (int64_t)256 << 20;
+
 template <class SR>
 static int launch_mm(gg_ctx* ctx, gg_mat* A, const SR& sr, int64_t k, const void* mask, int tmask,
                      int64_t lo, int64_t hi) {
+  typedef typename SR::T T;
   const int64_t m = A->m;
-  if (A->format == GG_FMT_CSR) {
-    const int64_t row_lo = lo > 0 ? lo - 1 : 0;
-    const int64_t nrows = lo > 0 ? hi - lo + 1 : m;
-    k_csr_spmm<SR><<<grid_mm(ctx, nrows), 256, 0, ctx->stream>>>(sr, A->rowptr, A->colval, row_lo,
-                                                                 nrows, k, mask, tmask);
-  } else {
-    int64_t s_lo = 0, s_hi = m;
-    if (lo > 0) {
-      const int64_t w = A->sigma > 1 ? A->sigma : 1;
-      s_lo = ((lo - 1) / w) * w;
-      s_hi = ((hi + w - 1) / w) * w;
-      if (s_hi > m) s_hi = m;
-    }
-    k_sell_spmm<SR><<<grid_mm(ctx, s_hi - s_lo), 256, 0, ctx->stream>>>(
-        sr, A->slice_ptr, A->colval, A->sigma > 1 ? A->perm : nullptr, A->slice_size, s_lo, s_hi, k,
-        lo, hi, mask, tmask);
+  GG_CHECK(build_mm_plan(ctx, A));
+  const MMPlan* P = A->mmplan;
+  int64_t jwin = k;
+  if (P->nseg > 0) {
+    const int64_t per_col = P->nseg * (int64_t)sizeof(T);
+    const int64_t cap = kMMPartialBytes / per_col;
+    if (jwin > cap) jwin = cap < 32 ? 32 : (cap / 32) * 32;
+    GG_CHECK(ensure_scratch(ctx, (size_t)(per_col * jwin)));
   }
-  GG_CUDA(cudaGetLastError());
+  T* partials = static_cast<T*>(ctx->scratch);
+  const int64_t row_lo = lo > 0 ? lo - 1 : 0;
+  const int64_t row_hi = lo > 0 ? hi : m;
+  for (int64_t jlo = 0; jlo < k; jlo += jwin) {
+    const int64_t jn = k - jlo < jwin ? k - jlo : jwin;
+    if (A->format == GG_FMT_CSR) {
+      const int64_t nrows = row_hi - row_lo;
+      const int cpl = A->mm_cpl == 4 && jn >= 128 ? 4 : (A->mm_cpl >= 2 && jn >= 64 ? 2 : 1);
+      if (cpl == 4)
+        k_csr_spmm<SR, 4><<<grid_mm(ctx, P->nseg + nrows), 256, 0, ctx->stream>>>(
+            sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials);
+      else if (cpl == 2)
+        k_csr_spmm<SR, 2><<<grid_mm(ctx, P->nseg + nrows), 256, 0, ctx->stream>>>(
+            sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials);
+      else
+        k_csr_spmm<SR, 1><<<grid_mm(ctx, P->nseg + nrows), 256, 0, ctx->stream>>>(
+            sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials);
+    } else {
+      int64_t s_lo = 0, s_hi = m;
+      if (lo > 0) {
+        const int64_t w = A->sigma > 1 ? A->sigma : 1;
+        s_lo = ((lo - 1) / w) * w;
+        s_hi = ((hi + w - 1) / w) * w;
+        if (s_hi > m) s_hi = m;
+      }
+      k_sell_spmm<SR><<<grid_mm(ctx, P->nseg + s_hi - s_lo), 256, 0, ctx->stream>>>(
+          sr, A->slice_ptr, A->colval, A->sigma > 1 ? A->perm : nullptr, A->slice_size, s_lo, s_hi,
+          jlo, jn, lo, hi, mask, tmask, P->segs, P->nseg, partials);
+    }
+    GG_CUDA(cudaGetLastError());
+    if (P->nlong > 0) {
+      k_spmm_combine<SR><<<grid_mm(ctx, P->nlong), 256, 0, ctx->stream>>>(
+          sr, P->rows, P->first, P->nlong, A->sigma > 1 ? A->perm : nullptr,
+          A->format != GG_FMT_CSR, row_lo, row_hi, jlo, jn, mask, tmask, partials);
+      GG_CUDA(cudaGetLastError());
+    }
+  }
   return GG_OK;
 }
 

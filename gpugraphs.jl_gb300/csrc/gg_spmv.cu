@@ -14,9 +14,11 @@
 //  * k_spmv_pipe<SR>: the same work items for the fixed-type plus-times Float32
 //    semiring, software pipelined (next block's loads in flight during the current
 //    block's gathers), A streamed past L1, long segments read with 128-bit loads.
+//    Used for CSR matrices of fewer than 65536 rows; larger ones run plus-times on a
+//    SELL-32 copy with rows sorted by length (built once per matrix).
 //  * k_csr_first_hit<TC>: add == GPUGraphs_any with a mask on CSR: the first stored
 //    column whose x is nonzero (any_dense_masked_csr_spmv_kernel!, CSR.jl:147-171).
-//  * k_sell<SR>: one thread per (stored SELL row, chunk of <= 512 slice columns)
+//  * k_sell<SR>: one thread per (stored SELL row, chunk of <= 128 slice columns)
 //    walking with stride C (slice-column-major, so a warp reads C consecutive
 //    words), stopping at the first -1 padding column like sell_spmv_kernel!
 //    (SELL.jl:31-63); rows of multi-chunk slices are combined by k_sell_combine.
@@ -398,15 +400,15 @@ __global__ void k_sell(SR sr, const int32_t* __restrict__ slice_ptr,
     T acc = sr.neutral();
     int32_t j = d.y;
     bool done = false;
-    for (; j + 4 <= d.z && !done; j += 4, i += 4 * C) {
-      int32_t c[4];
+    for (; j + 8 <= d.z && !done; j += 8, i += 8 * C) {
+      int32_t c[8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) c[u] = ld_stream(colval + i + u * C);
-      T p[4];
+      for (int u = 0; u < 8; ++u) c[u] = ld_stream(colval + i + u * C);
+      T p[8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) p[u] = (c[u] != -1) ? sr.mulk(i + u * C, c[u], r1) : sr.neutral();
+      for (int u = 0; u < 8; ++u) p[u] = (c[u] != -1) ? sr.mulk(i + u * C, c[u], r1) : sr.neutral();
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < 8; ++u) {
         if (c[u] == -1) { done = true; break; }
         acc = sr.addv(acc, p[u]);
       }
@@ -775,6 +777,12 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
     sr.nz = static_cast<const float*>(A->nzval);
     sr.x = static_cast<const float*>(x);
     sr.y = static_cast<float*>(y);
+    if (A->format == GG_FMT_CSR && A->m >= (1 << 16)) {
+      // plus-times over a large CSR runs on a SELL-32 copy with rows sorted by length
+      // (built once): slices of equal-length rows give every thread the same work
+      if (!A->sell_copy) GG_CHECK(gg_sell_create(ctx, A, 32, A->m, &A->sell_copy));
+      return spmv_dispatch(ctx, A->sell_copy, tc, mul, add, accum, y, ty, x, tx, mask, tmask, lo, hi);
+    }
     GG_CHECK(build_colperm(ctx, A));
     const int32_t* colval = A->colval;
     if (A->colperm->enabled) {

@@ -44,6 +44,11 @@ SIGNATURES = {
     "gg_server_poll": [P, PI64, ctypes.POINTER(ctypes.c_double), I64, PI64, PI64],
     "gg_server_stats": [P, PI64, PI64, PI64],
     "gg_server_destroy": [P],
+    "gg_multigraph_create": [P, P, I64, PP],
+    "gg_multigraph_destroy": [P],
+    "gg_multigraph_info": [P, PI64, PI64, PI64, PI64],
+    "gg_multigraph_spmv": [P, P, P, P],
+    "gg_multigraph_bfs": [P, P, P, P, PI64],
     "gg_bfs_levels_noalloc": [P, P, P, I, I64, I64, I64, P, P, PI64],
     "gg_gen_rmat_edges": [P, I, I64, D, D, D, U64, I, P, P, P],
     "gg_gen_er_edges": [P, I64, I64, U64, I, P, P, P],

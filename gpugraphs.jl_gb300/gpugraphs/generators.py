@@ -91,11 +91,12 @@ def rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, wkind=W_U01_F32,
     return _csr(n, s, d, w, symmetrize, drop_loops)
 
 
-def erdos_renyi(n, avg_degree=16, seed=1, wkind=W_U01_F32, device="cuda"):
-    """Directed Erdos-Renyi graph with avg_degree * n uniform edges, duplicates merged
-    (first kept), self-loops kept."""
+def erdos_renyi(n, avg_degree=16, seed=1, wkind=W_U01_F32, symmetric=False, device="cuda"):
+    """Erdos-Renyi graph with avg_degree * n uniform edges, duplicates merged (first
+    kept): directed with self-loops kept, or (symmetric=True) undirected -- each edge
+    mirrored, self-loops dropped, about 2 * avg_degree entries per row."""
     s, d, w = er_edges(n, avg_degree * n, seed, wkind, device)
-    return _csr(n, s, d, w, False, False)
+    return _csr(n, s, d, w, symmetric, symmetric)
 
 
 def grid(H, W, seed=1, wkind=W_F32_1_10, device="cuda"):

@@ -94,6 +94,7 @@ enum { GG_QUERY_BFS = 1, GG_QUERY_SSSP = 2, GG_QUERY_SPMV_ITER = 3 };
 typedef struct gg_ctx gg_ctx; /* device, stream, scratch arena */
 typedef struct gg_mat gg_mat; /* a CSR or SELL-C-sigma matrix resident on the device */
 typedef struct gg_server gg_server; /* continuous-batching query server */
+typedef struct gg_multigraph gg_multigraph; /* many graphs in one block-diagonal structure */
 
 /* ---- library / context ---------------------------------------------------- */
 
@@ -300,6 +301,29 @@ int gg_server_stats(gg_server* server, int64_t* ticks, int64_t* admission_waits,
                     int64_t* exec_bytes);
 /* Stops the worker and frees the executors (queued requests are dropped). */
 int gg_server_destroy(gg_server* server);
+
+/* ---- many graphs per launch (no reference counterpart) ---------------------------
+ * G square CSR graphs (one element type) concatenated with 64-bit offsets: vertex v
+ * of graph g has the global id row_offsets[g] + v - 1 in the concatenated vectors. */
+
+/* Copies the graphs into one structure (the handles may be destroyed afterwards). */
+int gg_multigraph_create(gg_ctx* ctx, const gg_mat* const* graphs, int64_t ngraphs,
+                         gg_multigraph** out);
+int gg_multigraph_destroy(gg_multigraph* mg);
+/* Graph count, total vertices, total entries, and (if not NULL) the G+1 offsets. */
+int gg_multigraph_info(const gg_multigraph* mg, int64_t* ngraphs, int64_t* total_n,
+                       int64_t* total_nnz, int64_t* row_offsets);
+/* y_g = A_g * x_g (plus-times Float32) for every graph in one kernel launch;
+ * x, y: concatenated device vectors of total_n entries.  Asynchronous. */
+int gg_multigraph_spmv(gg_ctx* ctx, const gg_multigraph* mg, const float* x, float* y);
+/* One BFS per graph (sources[g], 1-based within graph g, host array) in one
+ * persistent cooperative launch captured in a CUDA graph (re-captured when dist
+ * changes).  dist: concatenated Int32 device vector, levels as bfs_distances of
+ * each graph with rows of A_T used as out-edges (exact for symmetric graphs),
+ * typemax(Int32) when unreached.  Synchronous; GG_ERR_TIMEOUT if the grid barrier's
+ * bounded wait ran out.  levels_out: levels run (deepest graph). */
+int gg_multigraph_bfs(gg_ctx* ctx, gg_multigraph* mg, const int64_t* sources, int32_t* dist,
+                      int64_t* levels_out);
 
 /* ---- seeded synthetic inputs (no reference counterpart: the reference's benchmark
  *      draws its inputs with Julia's sprand / Graphs.jl generators,

@@ -555,10 +555,12 @@ static int edge_odd(const void* nzval, int tv, int64_t k) {
  * masked (band, bor) SpMV per level over unvisited rows; a row joins level `iter`
  * when an in-neighbour in the current frontier has an odd (true) stored value.
  * dist is filled with typemax(Int32) first (bfs.jl:16-18).  Returns the number of
- * levels run (iterations of bfs.jl:50-71).  Parallel over rows.
+ * levels run (iterations of bfs.jl:50-71), or minus that number when max_levels > 0
+ * stopped the search early (bounded CPU samples).  Parallel over rows.
  */
 int64_t orc_bfs_levels(int64_t n, const int32_t* rowptr, const int32_t* colval,
-                       const void* nzval, int tv, int64_t source, int32_t* dist) {
+                       const void* nzval, int tv, int64_t source, int32_t* dist,
+                       int64_t max_levels) {
   uint8_t* curr = (uint8_t*)calloc((size_t)n, 1);
   uint8_t* next = (uint8_t*)calloc((size_t)n, 1);
   uint8_t* to_explore = (uint8_t*)malloc((size_t)n);
@@ -570,6 +572,7 @@ int64_t orc_bfs_levels(int64_t n, const int32_t* rowptr, const int32_t* colval,
   int32_t iter = 0;
   int64_t levels = 0;
   for (;;) {
+    if (max_levels > 0 && levels >= max_levels) { levels = -levels; break; }
     ++iter;
     ++levels;
     int any = 0;

@@ -44,7 +44,7 @@ def lib():
                              I32, I32, I32],
             "orc_sell_spmm": [I64, I64, I64, P, P, P, I32, P, P, I32, I64, P, I32, I64, I64, I32, P,
                               I32, I64, I64, I32, I32, I32],
-            "orc_bfs_levels": [I64, P, P, P, I32, I64, P],
+            "orc_bfs_levels": [I64, P, P, P, I32, I64, P, I64],
             "orc_bfs_parents": [I64, P, P, I64, I32, P],
             "orc_sssp": [I64, P, P, P, I32, P, I64, P, I32, I64],
             "orc_csr_spmv_plus_times_f32": [I64, P, P, P, P, P],
@@ -172,12 +172,13 @@ def sell_spmm(S, Cm, B, layout=0, mul=MUL, add=ADD, accum=SECOND, mask=None, ran
                                0 if mask is None else tcode(mask), lo, hi, mul, add, accum)
 
 
-def bfs_levels(n, rowptr, colval, nzval, source):
-    """bfs_distances(A_T, source) (src/algorithms/bfs.jl:1-73) -> (dist Int32, levels)."""
+def bfs_levels(n, rowptr, colval, nzval, source, max_levels=0):
+    """bfs_distances(A_T, source) (src/algorithms/bfs.jl:1-73) -> (dist Int32, levels);
+    max_levels > 0 stops early and returns -levels."""
     rowptr, colval, nzval = _c(rowptr, np.int32), _c(colval, np.int32), _c(nzval)
     dist = np.empty(n, np.int32)
     lv = lib().orc_bfs_levels(n, _p(rowptr), _p(colval), _p(nzval), tcode(nzval), source,
-                              _p(dist))
+                              _p(dist), max_levels)
     return dist, lv
 
 

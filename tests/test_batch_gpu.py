@@ -83,3 +83,49 @@ def test_sssp_batch_int_rmat_and_float_grid():
     assert got.dtype == np.float32 and (got == ref).all()
     S = G.SparseGPUMatrixSELL(Gf, 16, 32)
     assert (host(G.shortest_path(S, src)) == ref).all()
+
+
+def hub_graph(n, seed, dtype):
+    """Directed graph with two hubs of 6000 and 9000 in-edges (split into pieces), a
+    vertex of 1500 in-edges (whole-warp scan) and a sparse random remainder."""
+    rng = np.random.default_rng(seed)
+    M = sp.random(n, n, density=3.0 / n, random_state=rng, format="coo")
+    rows, cols = [M.row], [M.col]
+    for v, d in ((0, 6000), (1, 9000), (2, 1500)):
+        rows.append(np.full(d, v))
+        cols.append(rng.choice(n, d, replace=False))
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    if dtype == np.float32:
+        vals = rng.uniform(1, 10, len(rows)).astype(np.float32)
+    else:
+        vals = rng.integers(1, 6, len(rows)).astype(dtype)
+    A_T = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))  # row v lists in-neighbours
+    A_T.sum_duplicates()
+    A_T.sort_indices()
+    return csr_from_scipy(A_T)
+
+
+def test_bfs_batch_hubs():
+    n = 12000
+    rp, cv, nz = hub_graph(n, 41, np.int32)
+    assert np.diff(rp).max() > 2048
+    B = G.SparseGPUMatrixCSR(n, n, rp, cv, nz)
+    rng = np.random.default_rng(41)
+    src = np.concatenate([[1, 2, 3], rng.integers(1, n + 1, 97)])
+    for rep in range(2):  # hub accumulators are cleared for the next call
+        D = host(G.bfs_distances_batch(B, src))
+        for q in list(range(0, 100, 7)) + [0, 1, 2, 99]:
+            ref, _ = O.bfs_levels(n, rp, cv, nz, int(src[q]))
+            assert (D[:, q] == ref).all(), (rep, q)
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.float32])
+def test_sssp_batch_hubs(dtype):
+    n = 12000
+    rp, cv, nz = hub_graph(n, 42, dtype)
+    B = G.SparseGPUMatrixCSR(n, n, rp, cv, nz)
+    rng = np.random.default_rng(42)
+    src = np.concatenate([[1, 2, 3], rng.integers(1, n + 1, 37)]).astype(np.int64)
+    ref, _ = O.sssp(n, rp, cv, nz, src)
+    got = host(G.shortest_path(B, src))
+    assert (got == ref).all()

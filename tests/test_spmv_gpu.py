@@ -2,8 +2,8 @@
 the reference's golden vectors and an FP64 oracle.
 
 Tolerance: integer, Bool, min/max/any/or semirings and every row folded in storage
-order (CSR rows of at most 32 entries, SELL rows of at most 512, every SpMM
-element) are compared bit for bit.  Float32 plus-times rows that the kernels reduce in parallel
+order (CSR rows of at most 32 entries, SELL rows of at most 128, SpMM rows of at
+most 256) are compared bit for bit.  Float32 plus-times rows that the kernels reduce in parallel
 (CSR rows longer than 32 entries) are compared with rtol 1e-5 against the FP64
 product (the reference's own isapprox tests use rtol ~3.4e-4)."""
 import itertools
@@ -20,6 +20,8 @@ from helpers import csr_from_scipy, golden_json, sprand_csr
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-5
+SELL_CHUNK = 128  # slice columns one SELL thread folds in storage order
+SEG_MM = 256  # SpMM rows longer than this are folded in pieces
 
 
 def dev(a):
@@ -126,8 +128,8 @@ def test_sell_layout_matches_oracle(C, sigma):
 
 @pytest.mark.parametrize("m,p,seed", [(10, 0.5, 1), (1000, 0.2, 2)])
 def test_spmv_plus_times_reference_sizes(m, p, seed):
-    """test/spmv.jl:10-70 sizes; rows of <= 32 entries are folded in storage order ->
-    bit-exact (every SELL row too)."""
+    """test/spmv.jl:10-70 sizes; CSR rows of <= 32 entries and SELL rows of <= 128
+    are folded in storage order -> bit-exact."""
     rowptr, colval, nzval, A = sprand_csr(m, m, p, seed=seed)
     x = np.random.default_rng(seed).random(m, dtype=np.float32)
     yo = np.zeros(m, np.float32)
@@ -140,7 +142,7 @@ def test_spmv_plus_times_reference_sizes(m, p, seed):
         G.gpu_spmv_(y, M, dev(x))
         yh = host(y)
         np.testing.assert_allclose(yh, ref64, rtol=RTOL, atol=1e-6)
-        exact = np.ones(m, bool) if M is S else np.diff(rowptr) <= 32
+        exact = np.diff(rowptr) <= (SELL_CHUNK if M is S else 32)
         assert (yh[exact] == yo[exact]).all()
 
 
@@ -165,9 +167,9 @@ def test_spmv_plus_times_long_rows():
         y = torch.zeros(m, dtype=torch.float32, device="cuda")
         G.gpu_spmv_(y, S, dev(x))
         yh = host(y)
-        # SELL folds each row in storage order within chunks of 512 slice columns;
+        # SELL folds each row in storage order within chunks of 128 slice columns;
         # longer rows combine the chunk sums in order
-        exact = deg <= 512
+        exact = deg <= SELL_CHUNK
         assert (yh[exact] == yo[exact]).all()
         np.testing.assert_allclose(yh, ref64, rtol=RTOL, atol=1e-6)
 
@@ -376,6 +378,57 @@ def test_spmm_min_plus_masked_range():
                 G.gpu_spmm_(Cd, M, Bd, mul=G.GPUGraphs_safe_add, add=G.GPUGraphs_min,
                             accum=G.GPUGraphs_min, mask=None if mk is None else dev(mk), range=rg)
                 assert (host(Cd) == Co).all(), (fmt, layout, mk is not None, rg)
+
+
+def test_spmm_long_rows_power_law():
+    """Hub rows (up to m/2 entries) are folded in pieces of 256 by separate warps and
+    combined in order: exact for min-plus on Int32, exact for Float32 plus-times rows
+    of <= 256 entries, within rtol 1e-5 of FP64 for the others."""
+    m, k = 3000, 40
+    rowptr, colval, nzval, A = power_law_csr(m, 11)
+    deg = np.diff(rowptr)
+    assert deg.max() > 4 * SEG_MM
+    rng = np.random.default_rng(11)
+    Bf = rng.random((m, k), dtype=np.float32)
+    ref64 = A.astype(np.float64) @ Bf.astype(np.float64)
+    Bc = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nzval)
+    for M in (Bc, G.SparseGPUMatrixSELL(Bc, 32, m), G.SparseGPUMatrixSELL(Bc, 8, 1)):
+        for layout in (0, 1):
+            Bl = np.asfortranarray(Bf) if layout == 0 else np.ascontiguousarray(Bf)
+            Co = np.zeros((m, k), np.float32, order="F" if layout == 0 else "C")
+            O.csr_spmm(m, rowptr, colval, nzval, Co, Bl, layout=layout)
+            if layout == 0:
+                Bd = torch.from_numpy(np.ascontiguousarray(Bf.T)).cuda().T
+                Cd = torch.zeros((k, m), dtype=torch.float32, device="cuda").T
+            else:
+                Bd = dev(Bf)
+                Cd = torch.zeros((m, k), dtype=torch.float32, device="cuda")
+            for rep in range(2):
+                G.gpu_spmm_(Cd, M, Bd)
+                Ch = host(Cd)
+                np.testing.assert_allclose(Ch, ref64, rtol=RTOL, atol=1e-5)
+                short = deg <= SEG_MM
+                assert (Ch[short] == Co[short]).all()
+    # min-plus on Int32 with a mask and a row range: exact on every row
+    nzi = rng.integers(1, 50, len(colval)).astype(np.int32)
+    Bi = rng.integers(0, 1000, (m, k)).astype(np.int32)
+    Bi[rng.random((m, k)) < 0.2] = np.iinfo(np.int32).max
+    mask = rng.random(m) < 0.6
+    mask[:3] = True
+    Ci = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nzi)
+    S = O.sell_build(m, rowptr, colval, nzi, 32, m)
+    for fmt, M in (("csr", Ci), ("sell", G.SparseGPUMatrixSELL(Ci, 32, m))):
+        for mk, rg in ((None, None), (mask, None), (None, (1, 2000))):
+            C0 = rng.integers(0, 5000, (m, k)).astype(np.int32)
+            Co = C0.copy()
+            if fmt == "csr":
+                O.csr_spmm(m, rowptr, colval, nzi, Co, Bi, 1, O.SAFE_ADD, O.MIN, O.MIN, mk, rg)
+            else:
+                O.sell_spmm(S, Co, Bi, 1, O.SAFE_ADD, O.MIN, O.MIN, mk, rg)
+            Cd = dev(C0)
+            G.gpu_spmm_(Cd, M, dev(Bi), mul=G.GPUGraphs_safe_add, add=G.GPUGraphs_min,
+                        accum=G.GPUGraphs_min, mask=None if mk is None else dev(mk), range=rg)
+            assert (host(Cd) == Co).all(), (fmt, mk is not None, rg)
 
 
 def test_spmm_assertions():
