@@ -257,7 +257,49 @@ int gg_destroy(gg_ctx* ctx) {
   cudaFree(ctx->scratch);
   cudaFree(ctx->d_flags);
   cudaFreeHost(ctx->h_flags);
+  if (ctx->trace_ev) {
+    for (int i = 0; i < 2 * kTraceMax; ++i) cudaEventDestroy(ctx->trace_ev[i]);
+    delete[] ctx->trace_ev;
+  }
   delete ctx;
+  return GG_OK;
+}
+
+int gg_trace_begin(gg_ctx* ctx) {
+  if (!ctx) return set_error(GG_ERR_ARGUMENT, "ctx is NULL");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  if (!ctx->trace_ev) {
+    ctx->trace_ev = new cudaEvent_t[2 * kTraceMax]();
+    for (int i = 0; i < 2 * kTraceMax; ++i) {
+      cudaError_t e = cudaEventCreate(&ctx->trace_ev[i]);
+      if (e != cudaSuccess) {
+        for (int j = 0; j < i; ++j) cudaEventDestroy(ctx->trace_ev[j]);
+        delete[] ctx->trace_ev;
+        ctx->trace_ev = nullptr;
+        return cuda_error(e, "gg_trace_begin");
+      }
+    }
+  }
+  ctx->trace_on = true;
+  ctx->trace_launches = 0;
+  ctx->trace_used = 0;
+  return GG_OK;
+}
+
+int gg_trace_end(gg_ctx* ctx, int64_t* launches, int64_t* timed, double* timed_ms) {
+  if (!ctx) return set_error(GG_ERR_ARGUMENT, "ctx is NULL");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  double tot = 0.0;
+  for (int i = 0; i < ctx->trace_used; ++i) {
+    float ms = 0.f;
+    GG_CUDA(cudaEventElapsedTime(&ms, ctx->trace_ev[2 * i], ctx->trace_ev[2 * i + 1]));
+    tot += ms;
+  }
+  if (launches) *launches = ctx->trace_launches;
+  if (timed) *timed = ctx->trace_used;
+  if (timed_ms) *timed_ms = tot;
+  ctx->trace_on = false;
   return GG_OK;
 }
 

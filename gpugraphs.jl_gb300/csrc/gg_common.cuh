@@ -391,7 +391,31 @@ struct gg_ctx {
   size_t scratch_bytes = 0;
   unsigned int* d_flags = nullptr;  // small device word array for status flags
   unsigned int* h_flags = nullptr;  // pinned mirror
+  // launch tracing (gg_trace_begin / gg_trace_end): kernel launches of the SpMV /
+  // SpMM paths are counted and their main kernel bracketed by events from a pool
+  bool trace_on = false;
+  int64_t trace_launches = 0;
+  int trace_used = 0;
+  cudaEvent_t* trace_ev = nullptr;  // 2 * kTraceMax events
 };
+
+namespace gg {
+static const int kTraceMax = 4096;
+// count n kernel launches of the current call
+inline void trace_count(gg_ctx* c, int n) {
+  if (c->trace_on) c->trace_launches += n;
+}
+// bracket the main kernel of a call: returns the event pair index or -1
+inline int trace_main_begin(gg_ctx* c) {
+  if (!c->trace_on || c->trace_used >= kTraceMax) return -1;
+  const int i = c->trace_used++;
+  cudaEventRecord(c->trace_ev[2 * i], c->stream);
+  return i;
+}
+inline void trace_main_end(gg_ctx* c, int i) {
+  if (i >= 0) cudaEventRecord(c->trace_ev[2 * i + 1], c->stream);
+}
+}  // namespace gg
 
 struct gg_mat {
   int format = GG_FMT_CSR;

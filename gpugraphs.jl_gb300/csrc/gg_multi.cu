@@ -12,8 +12,15 @@
 //    wait is bounded: on timeout it records an error, every block returns, and the
 //    call reports GG_ERR_TIMEOUT.  The launch (with its resets) is captured once in
 //    a CUDA graph and replayed by later calls.
+//  * gg_multigraph_sssp: one single-source shortest-path search per graph in one
+//    persistent cooperative launch (frontier Bellman-Ford, atomic min, bounded grid
+//    barrier), captured in a CUDA graph the same way.
 // Levels follow bfs_distances (src/algorithms/bfs.jl:1-73): edges with odd / true
-// stored values, dist = hop level, typemax(Int32) when unreached.
+// stored values (every stored entry of a floating-point graph, i.e. its Bool
+// pattern), dist = hop level, typemax(Int32) when unreached.  Distances follow
+// shortest_path (src/algorithms/shortest_path.jl:12-83) for non-negative weights.
+// Both searches use the rows of A_T as out-edges, which equals the reference for
+// symmetric graphs.
 #include <algorithm>
 #include <vector>
 
@@ -39,6 +46,11 @@ struct gg_multigraph {
   int32_t* dist_bound = nullptr;      // dist pointer captured in the graph
   cudaGraphExec_t gexec = nullptr;
   int grid = 0;
+  // persistent shortest-path state (allocated on first use)
+  unsigned* inq[2] = {nullptr, nullptr};
+  void* sssp_dist_bound = nullptr;
+  cudaGraphExec_t sssp_gexec = nullptr;
+  int nonneg = -1;  // all stored values >= 0 (and not NaN)? -1: not yet checked
 };
 
 namespace gg {
@@ -181,6 +193,140 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+template <typename T> __device__ __forceinline__ T mg_atomic_min(T* p, T v);
+template <> __device__ __forceinline__ int32_t mg_atomic_min<int32_t>(int32_t* p, int32_t v) {
+  return atomicMin(p, v);
+}
+template <> __device__ __forceinline__ int64_t mg_atomic_min<int64_t>(int64_t* p, int64_t v) {
+  return (int64_t)atomicMin((long long*)p, (long long)v);
+}
+// distances are non-negative and never -0.0 (+0.0 + w), so floats order like their bits
+template <> __device__ __forceinline__ float mg_atomic_min<float>(float* p, float v) {
+  return __int_as_float(atomicMin((int*)p, __float_as_int(v)));
+}
+template <> __device__ __forceinline__ double mg_atomic_min<double>(double* p, double v) {
+  return __longlong_as_double(atomicMin((long long*)p, __double_as_longlong(v)));
+}
+
+template <typename T>
+__device__ __forceinline__ T mg_weight(const void* nz, int tv, int64_t k) {
+  switch (tv) {
+    case GG_BOOL: return static_cast<T>(static_cast<const uint8_t*>(nz)[k]);
+    case GG_INT32: return static_cast<T>(static_cast<const int32_t*>(nz)[k]);
+    case GG_INT64: return static_cast<T>(static_cast<const int64_t*>(nz)[k]);
+    case GG_FLOAT32: return static_cast<T>(static_cast<const float*>(nz)[k]);
+  }
+  return static_cast<T>(static_cast<const double*>(nz)[k]);
+}
+
+template <typename T>
+__global__ void k_mg_fill_t(T* d, int64_t n, T v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    d[i] = v;
+}
+
+template <typename T>
+__global__ void k_mg_sssp_seed(int64_t G, const int64_t* src, T* dist, unsigned* inq, int32_t* q,
+                               unsigned long long* ctr) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < G;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = src[g];
+    dist[v] = T(0);
+    atomicOr(inq + (v >> 5), 1u << (v & 31));
+    q[g] = (int32_t)v;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctr[0] = (unsigned long long)G;
+    ctr[1] = 0;
+    ctr[2] = 0;
+  }
+}
+
+// all graphs' Bellman-Ford rounds in one persistent launch (warp per frontier
+// vertex, push over its row); inq_cur / inq_next mark queued vertices
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_mg_sssp(int64_t G, const int64_t* __restrict__ row_off, const int64_t* __restrict__ rp,
+              const int32_t* __restrict__ colval, const void* nz, int tv, T* dist, unsigned* inq_a,
+              unsigned* inq_b, int32_t* qa, int32_t* qb, unsigned long long* ctr, unsigned* bar,
+              int64_t max_rounds) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int32_t* cur = qa;
+  int32_t* nxt = qb;
+  unsigned* icur = inq_a;
+  unsigned* inxt = inq_b;
+  for (int64_t round = 1;; ++round) {
+    const int r = (int)(round % 3);
+    const int64_t nf = (int64_t)*((volatile unsigned long long*)(ctr + (r + 2) % 3));
+    if (nf == 0 || round > max_rounds) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        bar[3] = (unsigned)(round - 1);
+        if (nf != 0) atomicExch(bar + 2, 2u);  // still improving after max_rounds
+      }
+      return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr[(r + 1) % 3] = 0;
+    for (int64_t i = gw; i < nf; i += nw) {
+      const int64_t u = cur[i];
+      if (lane == 0) atomicAnd(icur + (u >> 5), ~(1u << (u & 31)));
+      const T du = __ldcg(dist + u);
+      const int g = graph_of(row_off, G, u);
+      const int64_t base = row_off[g] - 1;
+      const int64_t k0 = rp[u], k1 = rp[u + 1];
+      for (int64_t kb = k0; kb < k1; kb += 32) {
+        const int64_t k = kb + lane;
+        bool add = false;
+        int64_t v = 0;
+        if (k < k1) {
+          v = base + __ldg(colval + k);
+          const T w = mg_weight<T>(nz, tv, k);
+          const T cand = (w == Lim<T>::max() || du == Lim<T>::max()) ? Lim<T>::max() : w_add(w, du);
+          if (cand < __ldcg(dist + v)) {
+            const T old = mg_atomic_min<T>(dist + v, cand);
+            if (cand < old) {
+              const unsigned bit = 1u << (v & 31);
+              add = !(atomicOr(inxt + (v >> 5), bit) & bit);
+            }
+          }
+        }
+        const unsigned b = __ballot_sync(kFullM, add);
+        if (b) {
+          const int leader = __ffs(b) - 1;
+          unsigned long long pos = 0;
+          if (lane == leader) pos = atomicAdd(ctr + r, (unsigned long long)__popc(b));
+          pos = __shfl_sync(kFullM, pos, leader);
+          if (add) nxt[pos + __popc(b & ((1u << lane) - 1u))] = (int32_t)v;
+        }
+      }
+    }
+    if (!mg_grid_sync(bar, gridDim.x)) return;
+    int32_t* t = cur;
+    cur = nxt;
+    nxt = t;
+    unsigned* tb = icur;
+    icur = inxt;
+    inxt = tb;
+  }
+}
+
+__global__ void k_mg_nonneg(const void* nz, int tv, int64_t nnz, unsigned* bad) {
+  unsigned b = 0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    switch (tv) {
+      case GG_INT32: b |= static_cast<const int32_t*>(nz)[k] < 0; break;
+      case GG_INT64: b |= static_cast<const int64_t*>(nz)[k] < 0; break;
+      case GG_FLOAT32: { const float w = static_cast<const float*>(nz)[k]; b |= !(w >= 0.0f); break; }
+      case GG_FLOAT64: { const double w = static_cast<const double*>(nz)[k]; b |= !(w >= 0.0); break; }
+      default: break;
+    }
+  }
+  if (__syncthreads_or(b) && threadIdx.x == 0) atomicOr(bad, 1u);
+}
+
 __global__ void k_mg_fill(int32_t* d, int64_t n, int32_t v) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -275,6 +421,9 @@ int gg_multigraph_destroy(gg_multigraph* M) {
   if (!M) return GG_OK;
   cudaSetDevice(M->device);
   if (M->gexec) cudaGraphExecDestroy(M->gexec);
+  if (M->sssp_gexec) cudaGraphExecDestroy(M->sssp_gexec);
+  cudaFree(M->inq[0]);
+  cudaFree(M->inq[1]);
   cudaFree(M->row_off);
   cudaFree(M->rp64);
   cudaFree(M->colval);
@@ -314,8 +463,6 @@ int gg_multigraph_spmv(gg_ctx* ctx, const gg_multigraph* M, const float* x, floa
 int gg_multigraph_bfs(gg_ctx* ctx, gg_multigraph* M, const int64_t* sources, int32_t* dist,
                       int64_t* levels_out) {
   if (!ctx || !M || !sources || !dist) return set_error(GG_ERR_ARGUMENT, "NULL argument");
-  if (dtype_is_float(M->dtype))
-    return set_error(GG_ERR_UNSUPPORTED, "GPUGraphs_band has no method for floating-point matrices");
   GG_CUDA(cudaSetDevice(ctx->device));
   std::vector<int64_t> gsrc(M->ngraphs);
   for (int64_t g = 0; g < M->ngraphs; ++g) {
@@ -341,7 +488,7 @@ int gg_multigraph_bfs(gg_ctx* ctx, gg_multigraph* M, const int64_t* sources, int
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     const int64_t nw = M->total_n / 32 + 2;
-    const int odd_only = 1;
+    const int odd_only = dtype_is_float(M->dtype) ? 0 : 1;  // floats: the Bool pattern
     int64_t G = M->ngraphs;
     if (e == cudaSuccess) e = cudaMemsetAsync(M->visited, 0, nw * sizeof(unsigned), cs);
     if (e == cudaSuccess) e = cudaMemsetAsync(M->bar, 0, 4 * sizeof(unsigned), cs);
@@ -371,6 +518,104 @@ int gg_multigraph_bfs(gg_ctx* ctx, gg_multigraph* M, const int64_t* sources, int
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
   if (hb[2]) return set_error(GG_ERR_TIMEOUT, "multigraph BFS barrier wait ran out");
   if (levels_out) *levels_out = hb[3];
+  return GG_OK;
+}
+
+}  // extern "C"
+
+template <typename T>
+static int mg_sssp_capture(gg_ctx* ctx, gg_multigraph* M, T* dist) {
+  int per_sm = 0;
+  GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mg_sssp<T>, 256, 0));
+  if (per_sm < 1) return set_error(GG_ERR_CUDA, "k_mg_sssp cannot be resident");
+  const int grid = ctx->num_sms * per_sm;  // every block resident: the barrier is safe
+  cudaStream_t cs = nullptr;
+  GG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  const int64_t nw = M->total_n / 32 + 2;
+  int64_t G = M->ngraphs;
+  int64_t max_rounds = M->total_n + 1;
+  if (e == cudaSuccess) e = cudaMemsetAsync(M->inq[0], 0, nw * sizeof(unsigned), cs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(M->inq[1], 0, nw * sizeof(unsigned), cs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(M->bar, 0, 4 * sizeof(unsigned), cs);
+  if (e == cudaSuccess) {
+    k_mg_fill_t<T><<<mg_grid(ctx->num_sms, M->total_n), 256, 0, cs>>>(dist, M->total_n, Lim<T>::max());
+    k_mg_sssp_seed<T><<<mg_grid(ctx->num_sms, G), 256, 0, cs>>>(G, M->d_src, dist, M->inq[0],
+                                                                M->q[0], M->ctr);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    int tv = M->dtype;
+    void* args[] = {&G, &M->row_off, &M->rp64, &M->colval, &M->nzval, &tv, &dist, &M->inq[0],
+                    &M->inq[1], &M->q[0], &M->q[1], &M->ctr, &M->bar, &max_rounds};
+    e = cudaLaunchCooperativeKernel((const void*)k_mg_sssp<T>, dim3(grid), dim3(256), args, 0, cs);
+  }
+  cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&M->sssp_gexec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) return cuda_error(e, "multigraph shortest-path graph capture");
+  M->sssp_dist_bound = dist;
+  return GG_OK;
+}
+
+extern "C" {
+
+int gg_multigraph_sssp(gg_ctx* ctx, gg_multigraph* M, const int64_t* sources, void* dist,
+                       int dist_dtype, int64_t* rounds_out) {
+  if (!ctx || !M || !sources || !dist) return set_error(GG_ERR_ARGUMENT, "NULL argument");
+  const int want = M->dtype == GG_BOOL ? GG_INT32 : M->dtype;
+  if (dist_dtype != want)
+    return set_error(GG_ERR_TYPE, "dist element type must be Int32 for Bool graphs, else the graphs' type");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  if (M->nonneg < 0) {
+    GG_CUDA(cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned), ctx->stream));
+    k_mg_nonneg<<<mg_grid(ctx->num_sms, M->total_nnz), 256, 0, ctx->stream>>>(
+        M->nzval, M->dtype, M->total_nnz, ctx->d_flags);
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    M->nonneg = ctx->h_flags[0] ? 0 : 1;
+  }
+  if (!M->nonneg)
+    return set_error(GG_ERR_UNSUPPORTED, "multigraph shortest paths need non-negative weights");
+  std::vector<int64_t> gsrc(M->ngraphs);
+  for (int64_t g = 0; g < M->ngraphs; ++g) {
+    const int64_t n = M->h_row_off[g + 1] - M->h_row_off[g];
+    if (sources[g] < 1 || sources[g] > n)
+      return set_error(GG_ERR_BOUNDS, "source %lld of graph %lld out of 1:%lld", (long long)sources[g],
+                       (long long)g, (long long)n);
+    gsrc[g] = M->h_row_off[g] + sources[g] - 1;
+  }
+  const int64_t nw = M->total_n / 32 + 2;
+  if (!M->inq[0]) {
+    GG_CUDA(cudaMalloc((void**)&M->inq[0], nw * sizeof(unsigned)));
+    GG_CUDA(cudaMalloc((void**)&M->inq[1], nw * sizeof(unsigned)));
+  }
+  GG_CUDA(cudaMemcpyAsync(M->d_src, gsrc.data(), M->ngraphs * sizeof(int64_t),
+                          cudaMemcpyHostToDevice, ctx->stream));
+  if (!M->sssp_gexec || M->sssp_dist_bound != dist) {
+    if (M->sssp_gexec) {
+      cudaGraphExecDestroy(M->sssp_gexec);
+      M->sssp_gexec = nullptr;
+    }
+    switch (dist_dtype) {
+      case GG_INT32: GG_CHECK(mg_sssp_capture<int32_t>(ctx, M, static_cast<int32_t*>(dist))); break;
+      case GG_INT64: GG_CHECK(mg_sssp_capture<int64_t>(ctx, M, static_cast<int64_t*>(dist))); break;
+      case GG_FLOAT32: GG_CHECK(mg_sssp_capture<float>(ctx, M, static_cast<float*>(dist))); break;
+      default: GG_CHECK(mg_sssp_capture<double>(ctx, M, static_cast<double*>(dist))); break;
+    }
+  }
+  GG_CUDA(cudaGraphLaunch(M->sssp_gexec, ctx->stream));
+  unsigned hb[4] = {0, 0, 0, 0};
+  GG_CUDA(cudaMemcpyAsync(hb, M->bar, sizeof(hb), cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (hb[2] == 1) return set_error(GG_ERR_TIMEOUT, "multigraph shortest-path barrier wait ran out");
+  if (hb[2] == 2) return set_error(GG_ERR_NOT_CONVERGED, "multigraph shortest paths did not converge");
+  if (rounds_out) *rounds_out = hb[3];
   return GG_OK;
 }
 

@@ -317,9 +317,11 @@ static int launch_mm(gg_ctx* ctx, gg_mat* A, const SR& sr, int64_t k, const void
   const int64_t row_hi = lo > 0 ? hi : m;
   for (int64_t jlo = 0; jlo < k; jlo += jwin) {
     const int64_t jn = k - jlo < jwin ? k - jlo : jwin;
+    int tr = -1;
     if (A->format == GG_FMT_CSR) {
       const int64_t nrows = row_hi - row_lo;
       const int cpl = A->mm_cpl == 4 && jn >= 128 ? 4 : (A->mm_cpl >= 2 && jn >= 64 ? 2 : 1);
+      tr = trace_main_begin(ctx);
       if (cpl == 4)
         k_csr_spmm<SR, 4><<<grid_mm(ctx, P->nseg + nrows), 256, 0, ctx->stream>>>(
             sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials);
@@ -337,12 +339,16 @@ static int launch_mm(gg_ctx* ctx, gg_mat* A, const SR& sr, int64_t k, const void
         s_hi = ((hi + w - 1) / w) * w;
         if (s_hi > m) s_hi = m;
       }
+      tr = trace_main_begin(ctx);
       k_sell_spmm<SR><<<grid_mm(ctx, P->nseg + s_hi - s_lo), 256, 0, ctx->stream>>>(
           sr, A->slice_ptr, A->colval, A->sigma > 1 ? A->perm : nullptr, A->slice_size, s_lo, s_hi,
           jlo, jn, lo, hi, mask, tmask, P->segs, P->nseg, partials);
     }
+    trace_main_end(ctx, tr);
+    trace_count(ctx, 1);
     GG_CUDA(cudaGetLastError());
     if (P->nlong > 0) {
+      trace_count(ctx, 1);
       k_spmm_combine<SR><<<grid_mm(ctx, P->nlong), 256, 0, ctx->stream>>>(
           sr, P->rows, P->first, P->nlong, A->sigma > 1 ? A->perm : nullptr,
           A->format != GG_FMT_CSR, row_lo, row_hi, jlo, jn, mask, tmask, partials);

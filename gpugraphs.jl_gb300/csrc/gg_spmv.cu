@@ -511,6 +511,7 @@ int build_row_blocks(gg_ctx* ctx, gg_mat* A) {
   std::vector<int4> segs;
   std::vector<int32_t> first_seg, long_rows;
   blocks.reserve(m / 8 + 16);
+  const int64_t max_rows = A->block_rows > 0 ? A->block_rows : kBlockRows;
   int64_t r = 0;
   while (r < m) {
     int64_t len = rp[r + 1] - rp[r];
@@ -526,7 +527,7 @@ int build_row_blocks(gg_ctx* ctx, gg_mat* A) {
       continue;
     }
     int64_t first = r, cnt = 0;
-    while (r < m && r - first < kBlockRows) {
+    while (r < m && r - first < max_rows) {
       int64_t l = rp[r + 1] - rp[r];
       if (l > kShortRow || cnt + l > kBlockNnz) break;
       cnt += l;
@@ -605,9 +606,12 @@ int launch_rowblock_t(gg_ctx* ctx, gg_mat* A, const SR& sr, const RowFilter& flt
   int64_t grid = (items + kRBWarps - 1) / kRBWarps;
   const int64_t cap = (int64_t)ctx->num_sms * per_sm;  // one resident wave
   if (grid > cap) grid = cap;
+  const int tr = trace_main_begin(ctx);
   k_csr_rowblock<SR, kFiltered, kNeedsRow><<<(int)grid, kRBWarps * 32, 0, ctx->stream>>>(
       sr, A->rowptr, A->colval, rb->blocks, rb->nblocks, rb->segs, rb->nsegs, rb->long_first_seg,
       rb->long_rows, rb->long_count, static_cast<typename SR::T*>(rb->partials), flt);
+  trace_main_end(ctx, tr);
+  trace_count(ctx, 1);
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
@@ -656,8 +660,11 @@ static int spmv_generic(gg_ctx* ctx, gg_mat* A, int mul, int add, int accum, voi
   }
   const int G = group_width(A);
   if (add == GG_OP_ANY && mask != nullptr && lo == 0) {
+    const int tr = trace_main_begin(ctx);
     k_csr_first_hit<TC><<<grid_for(ctx, m * G, 256), 256, 0, ctx->stream>>>(
         sr, A->rowptr, A->colval, m, mask, tmask, G);
+    trace_main_end(ctx, tr);
+    trace_count(ctx, 1);
     GG_CUDA(cudaGetLastError());
     return GG_OK;
   }
@@ -753,15 +760,21 @@ static int launch_sell(gg_ctx* ctx, gg_mat* A, const SR& sr, const void* mask, i
   SellPlan* P = A->sellplan;
   const int64_t C = A->slice_size;
   typedef typename SR::T T;
-  if (P->nitems > 0)
+  if (P->nitems > 0) {
+    const int tr = trace_main_begin(ctx);
     k_sell<SR><<<grid_for(ctx, P->nitems * C, 256), 256, 0, ctx->stream>>>(
         sr, A->slice_ptr, colval_override ? colval_override : A->colval,
         A->sigma > 1 ? A->perm : nullptr, C, A->m, P->items,
         P->nitems, static_cast<T*>(P->partials), lo, hi, mask, tmask);
-  if (P->nmulti > 0)
+    trace_main_end(ctx, tr);
+    trace_count(ctx, 1);
+  }
+  if (P->nmulti > 0) {
     k_sell_combine<SR><<<grid_for(ctx, P->nmulti * C, 256), 256, 0, ctx->stream>>>(
         sr, A->sigma > 1 ? A->perm : nullptr, C, A->m, P->multi, P->nmulti,
         static_cast<const T*>(P->partials), lo, hi, mask, tmask);
+    trace_count(ctx, 1);
+  }
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
@@ -777,9 +790,11 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
     sr.nz = static_cast<const float*>(A->nzval);
     sr.x = static_cast<const float*>(x);
     sr.y = static_cast<float*>(y);
-    if (A->format == GG_FMT_CSR && A->m >= (1 << 16)) {
+    const bool use_copy = A->tuned_spmv == 2 || (A->tuned_spmv == 0 && A->m >= (1 << 16));
+    if (A->format == GG_FMT_CSR && use_copy) {
       // plus-times over a large CSR runs on a SELL-32 copy with rows sorted by length
-      // (built once): slices of equal-length rows give every thread the same work
+      // (built once; gg_tune may pick another C and sigma): slices of equal-length
+      // rows give every thread the same work
       if (!A->sell_copy) GG_CHECK(gg_sell_create(ctx, A, 32, A->m, &A->sell_copy));
       return spmv_dispatch(ctx, A->sell_copy, tc, mul, add, accum, y, ty, x, tx, mask, tmask, lo, hi);
     }
@@ -788,6 +803,7 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
     if (A->colperm->enabled) {
       k_gather_x<<<grid_for(ctx, A->n, 256), 256, 0, ctx->stream>>>(
           static_cast<const float*>(x), A->colperm->inv, A->n, A->colperm->xr);
+      trace_count(ctx, 1);
       sr.x = A->colperm->xr;
       colval = A->colperm->colval_r;
     }
@@ -805,9 +821,12 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
       int64_t grid = (items + kPipeWarps - 1) / kPipeWarps;
       const int64_t cap = (int64_t)ctx->num_sms * per_sm;  // one resident wave
       if (grid > cap) grid = cap;
+      const int tr = trace_main_begin(ctx);
       k_spmv_pipe<SRPlusTimesF32><<<(int)grid, kPipeWarps * 32, 0, ctx->stream>>>(
           sr, A->rowptr, colval, rb->blocks, rb->nblocks, rb->segs, rb->nsegs,
           rb->long_first_seg, rb->long_rows, rb->long_count, static_cast<float*>(rb->partials));
+      trace_main_end(ctx, tr);
+      trace_count(ctx, 1);
       GG_CUDA(cudaGetLastError());
       return GG_OK;
     }

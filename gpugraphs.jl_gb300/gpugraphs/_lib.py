@@ -26,6 +26,8 @@ SIGNATURES = {
     "gg_destroy": [P],
     "gg_set_stream": [P, P],
     "gg_stream_sync": [P],
+    "gg_trace_begin": [P],
+    "gg_trace_end": [P, PI64, PI64, ctypes.POINTER(ctypes.c_double)],
     "gg_csr_create": [P, I64, I64, I64, P, P, P, I, I, PP],
     "gg_sell_create": [P, P, I64, I64, PP],
     "gg_mat_destroy": [P],
@@ -49,6 +51,9 @@ SIGNATURES = {
     "gg_multigraph_info": [P, PI64, PI64, PI64, PI64],
     "gg_multigraph_spmv": [P, P, P, P],
     "gg_multigraph_bfs": [P, P, P, P, PI64],
+    "gg_multigraph_sssp": [P, P, P, P, I, PI64],
+    "gg_tune": [P, P, I64, P],
+    "gg_tune_apply": [P, P, P],
     "gg_bfs_levels_noalloc": [P, P, P, I, I64, I64, I64, P, P, PI64],
     "gg_gen_rmat_edges": [P, I, I64, D, D, D, U64, I, P, P, P],
     "gg_gen_er_edges": [P, I64, I64, U64, I, P, P, P],

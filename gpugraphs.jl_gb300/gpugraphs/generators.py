@@ -95,7 +95,7 @@ def erdos_renyi(n, avg_degree=16, seed=1, wkind=W_U01_F32, symmetric=False, devi
     """Erdos-Renyi graph with avg_degree * n uniform edges, duplicates merged (first
     kept): directed with self-loops kept, or (symmetric=True) undirected -- each edge
     mirrored, self-loops dropped, about 2 * avg_degree entries per row."""
-    s, d, w = er_edges(n, avg_degree * n, seed, wkind, device)
+    s, d, w = er_edges(n, int(round(avg_degree * n)), seed, wkind, device)
     return _csr(n, s, d, w, symmetric, symmetric)
 
 

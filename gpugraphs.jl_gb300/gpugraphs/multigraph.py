@@ -3,6 +3,7 @@
     mg = MultiGraph([A1, A2, ...])          # square CSR graphs of one element type
     y = mg.spmv(x)                          # y_g = A_g x_g for all graphs, one launch
     d = mg.bfs([s1, s2, ...])               # one BFS per graph, one persistent launch
+    D = mg.sssp([s1, s2, ...])              # one shortest-path search per graph
     parts = mg.split(d)                     # per-graph views of a concatenated vector
 """
 import ctypes
@@ -19,6 +20,7 @@ class MultiGraph:
         if not graphs:
             raise ArgumentError("need at least one graph")
         self.device = graphs[0].device
+        self.dtype_code = graphs[0].dtype_code
         L = core.lib()
         arr = (ctypes.c_void_p * len(graphs))(*[g.handle.value for g in graphs])
         h = ctypes.c_void_p()
@@ -55,6 +57,24 @@ class MultiGraph:
                                       src.ctypes.data_as(ctypes.c_void_p), core.ptr(dist),
                                       ctypes.byref(lv)), L)
         self.last_levels = lv.value
+        return dist
+
+    def sssp(self, sources, dist=None):
+        """Shortest-path distances of every graph from its source (1-based within the
+        graph), element type as shortest_path (Int32 for Bool graphs)."""
+        src = np.ascontiguousarray(np.asarray(sources, dtype=np.int64))
+        if len(src) != self.ngraphs:
+            raise ArgumentError("one source per graph")
+        code = core.INT32 if self.dtype_code == core.BOOL else self.dtype_code
+        if dist is None:
+            dist = torch.empty(self.total_n, dtype=core.CODE2TORCH[code], device=self.device)
+        L = core.lib()
+        r = ctypes.c_int64()
+        with torch.cuda.device(self.device):
+            check(L.gg_multigraph_sssp(core.ctx(self.device), self._h,
+                                       src.ctypes.data_as(ctypes.c_void_p), core.ptr(dist),
+                                       core.dtype_code(dist.dtype), ctypes.byref(r)), L)
+        self.last_rounds = r.value
         return dist
 
     def split(self, v):

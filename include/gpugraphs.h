@@ -116,6 +116,15 @@ int gg_set_stream(gg_ctx* ctx, void* stream);
 /* Replaces KernelAbstractions.synchronize(backend) (test/spmv.jl:25). */
 int gg_stream_sync(gg_ctx* ctx);
 
+/* Launch tracing (no reference counterpart).  Between gg_trace_begin and
+ * gg_trace_end, the kernel launches of gg_spmv / gg_spmm calls on this context are
+ * counted, and the main kernel of each call (the one that streams the matrix) is
+ * bracketed by CUDA events on the context's stream (first 4096 calls).  gg_trace_end
+ * synchronizes the stream and returns the launch count, the number of bracketed
+ * launches and their summed device time in ms.  Any out pointer may be NULL. */
+int gg_trace_begin(gg_ctx* ctx);
+int gg_trace_end(gg_ctx* ctx, int64_t* launches, int64_t* timed, double* timed_ms);
+
 /* ---- storage ------------------------------------------------------------------ */
 
 /*
@@ -319,11 +328,52 @@ int gg_multigraph_spmv(gg_ctx* ctx, const gg_multigraph* mg, const float* x, flo
 /* One BFS per graph (sources[g], 1-based within graph g, host array) in one
  * persistent cooperative launch captured in a CUDA graph (re-captured when dist
  * changes).  dist: concatenated Int32 device vector, levels as bfs_distances of
- * each graph with rows of A_T used as out-edges (exact for symmetric graphs),
- * typemax(Int32) when unreached.  Synchronous; GG_ERR_TIMEOUT if the grid barrier's
+ * each graph with rows of A_T used as out-edges (exact for symmetric graphs; a
+ * floating-point graph is searched over its Bool pattern, every stored entry an
+ * edge), typemax(Int32) when unreached.  Synchronous; GG_ERR_TIMEOUT if the grid barrier's
  * bounded wait ran out.  levels_out: levels run (deepest graph). */
 int gg_multigraph_bfs(gg_ctx* ctx, gg_multigraph* mg, const int64_t* sources, int32_t* dist,
                       int64_t* levels_out);
+/* One shortest-path search per graph (sources[g], 1-based within graph g, host
+ * array) in one persistent cooperative launch captured in a CUDA graph: frontier
+ * Bellman-Ford with atomic min, the fixpoint of shortest_path of each graph
+ * (src/algorithms/shortest_path.jl:12-83) with rows of A_T used as out-edges (exact
+ * for symmetric graphs).  dist: concatenated device vector of dist_dtype (Int32 for
+ * Bool graphs, else the graphs' type), typemax / +Inf when unreached.  Needs
+ * non-negative weights (GG_ERR_UNSUPPORTED otherwise).  Synchronous; GG_ERR_TIMEOUT
+ * if the grid barrier's bounded wait ran out.  rounds_out: rounds run. */
+int gg_multigraph_sssp(gg_ctx* ctx, gg_multigraph* mg, const int64_t* sources, void* dist,
+                       int dist_dtype, int64_t* rounds_out);
+
+/* ---- autotuning (no reference counterpart: the reference's layouts are fixed,
+ *      src/storage/SELL.jl:99-181) -------------------------------------------------- */
+
+typedef struct gg_tune_result {
+  int spmv_kernel;         /* 1 = CSR row blocks, 2 = a SELL-C-sigma layout */
+  int block_rows;          /* rows per row block (spmv_kernel 1) */
+  int64_t slice_size;      /* C (spmv_kernel 2) */
+  int64_t sigma;           /* sigma (spmv_kernel 2) */
+  double spmv_ms;          /* median time of the chosen SpMV configuration */
+  double spmv_default_ms;  /* median time of the built-in choice */
+  int mm_cols_per_lane;    /* SpMM column tile: 32 x this columns per warp pass */
+  double spmm_ms;          /* median time of the chosen SpMM tile (spmm_k > 0) */
+  int candidates;          /* configurations timed */
+} gg_tune_result;
+
+/*
+ * Times the Float32 plus-times SpMV of A over a grid of layouts (CSR row blocks of
+ * 32..256 rows; SELL-C-sigma copies, C in {8,16,32}, sigma in {1,64,1024,m}) and,
+ * when spmm_k > 0, the SpMM column tile (32, 64, 128 columns per warp pass) for a
+ * row-major n x spmm_k operand; keeps the fastest on the handle for later calls.
+ * Results of every configuration are identical for rows folded in storage order.
+ * GG_ERR_UNSUPPORTED unless A is Float32.  Synchronous.
+ */
+int gg_tune(gg_ctx* ctx, gg_mat* A, int64_t spmm_k, gg_tune_result* out);
+/* Applies a choice (e.g. one cached from an earlier gg_tune of the same matrix)
+ * without timing: spmv_kernel 1 with block_rows, 2 with slice_size and sigma (a SELL
+ * copy of a CSR handle is built), 0 leaves SpMV as is; mm_cols_per_lane 1, 2 or 4
+ * (0 leaves SpMM as is).  Synchronous. */
+int gg_tune_apply(gg_ctx* ctx, gg_mat* A, const gg_tune_result* choice);
 
 /* ---- seeded synthetic inputs (no reference counterpart: the reference's benchmark
  *      draws its inputs with Julia's sprand / Graphs.jl generators,

@@ -46,3 +46,30 @@ def test_multigraph_spmv_matches_per_graph():
         for g, xp, yp in zip(gs, mg.split(x), mg.split(y)):
             ref = g.to_scipy().astype(np.float64) @ xp.double().cpu().numpy()
             np.testing.assert_allclose(yp.cpu().numpy(), ref, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("wkind", [gen.W_INT_1_255, gen.W_F32_1_10, gen.W_PATTERN])
+def test_multigraph_sssp_matches_per_graph(wkind):
+    gs = _graphs(wkind)
+    if wkind == gen.W_INT_1_255:
+        gs = gs[:-1]  # the grid is a Bool pattern there
+    mg = MultiGraph(gs)
+    rng = np.random.default_rng(54)
+    for rep in range(2):
+        src = [int(rng.integers(1, g.n + 1)) for g in gs]
+        d = mg.sssp(src)
+        torch.cuda.synchronize()
+        for g, s, part in zip(gs, src, mg.split(d)):
+            assert torch.equal(part, G.shortest_path(g, s))
+
+
+def test_multigraph_bfs_float_graphs_use_the_pattern():
+    gs = _graphs(gen.W_U01_F32)[:-1]
+    mg = MultiGraph(gs)
+    src = [1 for _ in gs]
+    d = mg.bfs(src)
+    torch.cuda.synchronize()
+    for g, part in zip(gs, mg.split(d)):
+        P = G.SparseGPUMatrixCSR(g.m, g.n, g.rowptr, g.colval,
+                                 torch.ones(g.nnz(), dtype=torch.bool, device="cuda"))
+        assert torch.equal(part, G.bfs_distances(P, 1))
