@@ -246,7 +246,7 @@ def secondary_rmat22(device, A, x):
     return out
 
 
-def run_spmv_rmat22(args):
+def run_spmv_rmat(args, scale=22):
     import torch
     import torch.distributed as dist
     import gpugraphs as G
@@ -257,7 +257,7 @@ def run_spmv_rmat22(args):
     device = torch.device("cuda", local)
     if ws > 1:
         dist.init_process_group("nccl", device_id=device)
-    A = rmat(22, gen.W_U01_F32, device)
+    A = rmat(scale, gen.W_U01_F32, device)
     x = gen.uniform_vector(A.n, seed=2, device=device)
     n, nnz = A.n, A.nnz()
     y = torch.zeros(n, dtype=torch.float32, device=device)
@@ -308,7 +308,8 @@ def run_spmv_rmat22(args):
     kernel_ms = tr.kernel_ms / max(tr.timed, 1)
     peak, peak_kind = peak_hbm()
     achieved = B / (kernel_ms * 1e-3) / 1e9
-    traffic = traffic_from_profiles("spmv_csr_rmat22")
+    workload = "spmv_csr_rmat%d" % scale
+    traffic = traffic_from_profiles(workload)
 
     # e2e through the public API with host buffers
     xh = x.cpu().pin_memory()
@@ -327,15 +328,15 @@ def run_spmv_rmat22(args):
     e2e_val = ws * B / (float(e2e_t.item()) * 1e-3) / 1e9
 
     ok = spot_check(A, x, y)
-    secondary = {} if args.no_secondary else secondary_rmat22(device, A, x)
+    secondary = {} if (args.no_secondary or scale != 22) else secondary_rmat22(device, A, x)
     cpu = cpu_baseline_spmv(A, x) if (rank == 0 and not args.no_cpu) else None
     out = {
-        "metric": "SpMV GB/s (plus-times Float32, CSR, R-MAT scale 22)",
+        "metric": "SpMV GB/s (plus-times Float32, CSR, R-MAT scale %d)" % scale,
         "value": round(value, 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": round(per_step_ms, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded R-MAT generator on the device)",
-        "config": {"workload": "spmv_csr_rmat22", "n": n, "nnz": nnz, "format": "CSR",
+        "config": {"workload": workload, "n": n, "nnz": nnz, "format": "CSR",
                    "semiring": "(mul, add, second)",
                    "l2": "inputs larger than L2 (CSR %.2f GB)" % ((4 * (n + 1) + 8 * nnz) / 1e9),
                    "parallelism": "replicas" if ws > 1 else "single"},
@@ -393,7 +394,7 @@ def cpu_baseline_spmv(A, x, budget_s=8.0):
     t = statistics.median(times)
     return {"value": round(spmv_bytes(A.n, A.nnz()) / t / 1e9, 3), "unit": "GB/s",
             "cores": O.num_threads(), "kind": "port",
-            "sample": "%d full SpMVs over the same R-MAT s22 CSR (median)" % len(times)}
+            "sample": "%d full SpMVs over the same R-MAT CSR (median)" % len(times)}
 
 
 # ---------------------------------------------------------------------------------
@@ -657,16 +658,23 @@ def run_multigraph(args):
 
     ms_loop = time_steps(per_graph, max(3, args.steps // 4), warmup=1)
     src = [int(rng.integers(1, int(n) + 1)) for n in ns]
-    d = mg.bfs(src)
+    d = torch.empty(N, dtype=torch.int32, device=device)  # fixed buffer: the CUDA graph is reused
+    mg.bfs(src, d)
     torch.cuda.synchronize()
-    tb = time_host(lambda i: mg.bfs(src), max(3, args.steps // 4), warmup=1)
+    tb = time_host(lambda i: mg.bfs(src, d), max(3, args.steps // 4), warmup=1)
     t_bfs = statistics.median(tb)
     reached = int((d != I32MAX).sum().item())
     # traversed edges: entries of reached vertices, halved (symmetric graphs)
     mcc = 0
     for A, dv in zip(graphs, mg.split(d)):
         mcc += reached_edges(A, dv)
-    tl = time_host(lambda i: [G.bfs_distances(A, s) for A, s in zip(graphs, src)], 1, warmup=1)
+    # the one-call-per-graph path: bfs_distances needs the Bool pattern of each graph
+    pats = [G.SparseGPUMatrixCSR(A.m, A.n, A.rowptr, A.colval,
+                                 torch.ones(A.nnz(), dtype=torch.bool, device=device)) for A in graphs]
+    tl = time_host(lambda i: [G.bfs_distances(P, s) for P, s in zip(pats, src)], 1, warmup=1)
+    ok = all(torch.equal(dv, G.bfs_distances(P, s))
+             for P, s, dv in list(zip(pats, src, mg.split(d)))[:: max(1, ng // 20)])
+    del pats
     t_loop = statistics.median(tl)
     clocks = clk.stop()
     peak, peak_kind = peak_hbm()
@@ -685,7 +693,7 @@ def run_multigraph(args):
         "per_graph_launches": {"ms": round(ms_loop, 3), "speedup_of_one_launch": round(ms_loop / ms, 2)},
         "bfs": {"ms": round(t_bfs * 1e3, 3), "gteps": round(mcc / t_bfs / 1e9, 2), "levels": mg.last_levels,
                 "reached": reached, "per_graph_calls_ms": round(t_loop * 1e3, 1),
-                "speedup_of_one_launch": round(t_loop / t_bfs, 2)},
+                "speedup_of_one_launch": round(t_loop / t_bfs, 2), "equal_to_per_graph": ok},
         "e2e": None, "gpu_launches": args.steps, "clocks": clocks,
     }
     if rank == 0:
@@ -753,7 +761,9 @@ def main():
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "spmv_csr_rmat22":
-        run_spmv_rmat22(args)
+        run_spmv_rmat(args, 22)
+    elif args.workload == "spmv_csr_rmat24":
+        run_spmv_rmat(args, 24)
     elif args.workload in ("bfs_rmat24", "sssp_rmat24", "bfs_grid4096", "sssp_grid4096"):
         kind, graph = args.workload.split("_")
         if args.steps == 50:

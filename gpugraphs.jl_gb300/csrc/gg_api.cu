@@ -407,7 +407,7 @@ int gg_sell_create(gg_ctx* ctx, const gg_mat* csr, int64_t slice_size, int64_t s
     for (int64_t r = s * C; r < std::min<int64_t>((s + 1) * C, m); ++r)
       mx = std::max<int64_t>(mx, rp[perm[r]] - rp[perm[r] - 1]);
     acc += mx * C;
-    if (acc > (int64_t)INT32_MAX)
+    if (acc > (int64_t)INT32_MAX - 4096)  // kernels step Int32 positions past the end
       return set_error(GG_ERR_ARGUMENT, "SELL n_stored exceeds the Int32 index range (use a larger sigma)");
     sp[s + 1] = (int32_t)acc;
   }

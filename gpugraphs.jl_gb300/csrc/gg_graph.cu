@@ -33,6 +33,7 @@ struct PushCSR {       // out-edges (transpose of A_T), 0-based
   void* w = nullptr;          // weights in the distance type (SSSP only)
   int wtype = 0;
   int64_t nnz = 0;
+  int64_t max_deg = 0;  // largest out-degree: frontier hubs above kPushHub go to pieces
   bool built = false;
 };
 
@@ -297,6 +298,21 @@ int graph_view(gg_ctx* ctx, gg_mat* A, const int32_t** rp, const int32_t** cv, c
 }
 
 // which: 0 odd-valued edges, 1 all edges, 2 all edges with weights in the distance type
+__global__ void k_max_deg(int64_t n, const int32_t* __restrict__ rp, unsigned* out) {
+  unsigned mx = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned d = (unsigned)(rp[v + 1] - rp[v]);
+    mx = d > mx ? d : mx;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned t = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = t > mx ? t : mx;
+  }
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(out, mx);
+}
+
 static int ensure_push(gg_ctx* ctx, gg_mat* A, int which) {
   GG_CHECK(ensure_aux(ctx, A));
   GraphAux* g = A->aux;
@@ -353,9 +369,18 @@ static int ensure_push(gg_ctx* ctx, gg_mat* A, int which) {
                                                              odd_only, cnt, P.colval, (int32_t*)P.w);
     }
   }
-  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  cudaError_t e = cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned), ctx->stream);
+  if (e == cudaSuccess && n > 0) {
+    k_max_deg<<<gridsz(ctx, n), 256, 0, ctx->stream>>>(n, P.rowptr, ctx->d_flags);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                        ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   cudaFree(cnt);
   if (e != cudaSuccess) return cuda_error(e, "transpose");
+  P.max_deg = ctx->h_flags[0];
   GG_CUDA(cudaGetLastError());
   P.built = true;
   return GG_OK;
@@ -371,7 +396,15 @@ __device__ __forceinline__ bool bit_of(const unsigned* bm, int32_t v) {
 // counters: [0] next frontier size, [1] sum of out-degrees of the next frontier
 struct Counters {
   unsigned long long nf, mf, level, status;
+  unsigned long long nh;  // frontier hubs deferred to the piece kernel
+  unsigned long long pad[3];
 };
+
+// Frontier vertices with more than kPushHub out-edges are not walked by one warp:
+// the push kernels defer them to a hub queue, and the hub kernels split each one into
+// pieces of kPushPiece edges spread over all warps.
+static const int kPushHub = 2048;
+static const int kPushPiece = 1024;
 
 // warp-aggregated append of the lanes with `want` into q (full warp must call)
 __device__ __forceinline__ void warp_append(bool want, int32_t v, int32_t deg, int32_t* q,
@@ -402,12 +435,16 @@ __global__ void k_bfs_init(int32_t s, unsigned* visited, int32_t* dist, int32_t*
 __global__ void __launch_bounds__(256)
     k_bfs_push(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
                const int32_t* __restrict__ q, int64_t nf, int32_t level, unsigned* visited,
-               int32_t* dist, int32_t* qn, Counters* ctr) {
+               int32_t* dist, int32_t* qn, Counters* ctr, int32_t* hq) {
   const int lane = threadIdx.x & 31;
   for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nf;
        i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int32_t u = q[i];
     const int32_t k0 = prow[u], k1 = prow[u + 1];
+    if (hq && k1 - k0 > kPushHub) {  // left to k_bfs_push_hub
+      if (lane == 0) hq[atomicAdd(&ctr->nh, 1ull)] = u;
+      continue;
+    }
     for (int32_t base = k0; base < k1; base += 32) {
       const int32_t k = base + lane;
       bool claim = false;
@@ -423,6 +460,49 @@ __global__ void __launch_bounds__(256)
       }
       warp_append(claim, w, deg, qn, ctr);
     }
+  }
+}
+
+// pieces of the deferred frontier hubs: piece p of hub h has the global index
+// off_h + p (off_h = pieces of the hubs before it) and goes to warp (off_h + p) mod nw
+__device__ __forceinline__ int64_t first_piece(int64_t gw, int64_t nw, int64_t off) {
+  int64_t f = (gw - off) % nw;
+  return f < 0 ? f + nw : f;
+}
+
+__global__ void __launch_bounds__(256)
+    k_bfs_push_hub(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+                   const int32_t* __restrict__ hq, int32_t level, unsigned* visited,
+                   int32_t* dist, int32_t* qn, Counters* ctr, const Counters* hctr) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t nh = (int64_t)*((volatile const unsigned long long*)&hctr->nh);
+  int64_t off = 0;
+  for (int64_t h = 0; h < nh; ++h) {
+    const int32_t u = hq[h];
+    const int32_t k0 = prow[u], k1 = prow[u + 1];
+    const int64_t np = (k1 - k0 + kPushPiece - 1) / kPushPiece;
+    for (int64_t p = first_piece(gw, nw, off); p < np; p += nw) {
+      const int32_t kb = k0 + (int32_t)p * kPushPiece;
+      const int32_t ke = kb + kPushPiece < k1 ? kb + kPushPiece : k1;
+      for (int32_t base = kb; base < ke; base += 32) {
+        const int32_t k = base + lane;
+        bool claim = false;
+        int32_t w = 0, deg = 0;
+        if (k < ke) {
+          w = __ldg(pcol + k);
+          const unsigned bit = 1u << (w & 31);
+          if (!(__ldcg(visited + (w >> 5)) & bit)) claim = !(atomicOr(visited + (w >> 5), bit) & bit);
+          if (claim) {
+            dist[w] = level;
+            deg = prow[w + 1] - prow[w];
+          }
+        }
+        warp_append(claim, w, deg, qn, ctr);
+      }
+    }
+    off += np;
   }
 }
 
@@ -615,6 +695,7 @@ struct BfsScratch {
   unsigned* visited;
   unsigned* fb[2];
   int32_t* q[2];
+  int32_t* hq;  // deferred frontier hubs
   Counters* ctr;
 };
 
@@ -622,14 +703,15 @@ static int bfs_scratch(gg_ctx* ctx, int64_t n, BfsScratch* s) {
   const int64_t nw = (n + 31) / 32 + 1;
   const size_t bm = ((nw * sizeof(unsigned)) + 255) & ~(size_t)255;
   const size_t qb = (((n + 1) * sizeof(int32_t)) + 255) & ~(size_t)255;
-  GG_CHECK(ensure_scratch(ctx, 3 * bm + 2 * qb + 256));
+  GG_CHECK(ensure_scratch(ctx, 3 * bm + 3 * qb + 256));
   char* p = static_cast<char*>(ctx->scratch);
   s->visited = (unsigned*)p;
   s->fb[0] = (unsigned*)(p + bm);
   s->fb[1] = (unsigned*)(p + 2 * bm);
   s->q[0] = (int32_t*)(p + 3 * bm);
   s->q[1] = (int32_t*)(p + 3 * bm + qb);
-  s->ctr = (Counters*)(p + 3 * bm + 2 * qb);
+  s->hq = (int32_t*)(p + 3 * bm + 2 * qb);
+  s->ctr = (Counters*)(p + 3 * bm + 3 * qb);
   GG_CUDA(cudaMemsetAsync(p, 0, 3 * bm, ctx->stream));
   return GG_OK;
 }
@@ -697,8 +779,14 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
             (int32_t)level, sc.fb[cur ^ 1], sc.q[cur ^ 1], sc.ctr, P.rowptr);
       frontier_is_bitmap = true;
     } else {
+      const bool hubs = P.max_deg > kPushHub;
       k_bfs_push<<<gridsz(ctx, nf * 32), 256, 0, ctx->stream>>>(
-          P.rowptr, P.colval, sc.q[cur], nf, (int32_t)level, sc.visited, dist, sc.q[cur ^ 1], sc.ctr);
+          P.rowptr, P.colval, sc.q[cur], nf, (int32_t)level, sc.visited, dist, sc.q[cur ^ 1], sc.ctr,
+          hubs ? sc.hq : nullptr);
+      if (hubs)
+        k_bfs_push_hub<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(
+            P.rowptr, P.colval, sc.hq, (int32_t)level, sc.visited, dist, sc.q[cur ^ 1], sc.ctr,
+            sc.ctr);
       frontier_is_bitmap = false;
     }
     GG_CUDA(cudaGetLastError());
@@ -789,14 +877,18 @@ template <typename T>
 __global__ void __launch_bounds__(256)
     k_sssp_push(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
                 const T* __restrict__ pw, const int32_t* __restrict__ q, int64_t nf, T* dist,
-                unsigned* inq_cur, unsigned* inq_next, int32_t* qn, Counters* ctr) {
+                unsigned* inq_cur, unsigned* inq_next, int32_t* qn, Counters* ctr, int32_t* hq) {
   const int lane = threadIdx.x & 31;
   for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nf;
        i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int32_t u = q[i];
     if (lane == 0) atomicAnd(inq_cur + (u >> 5), ~(1u << (u & 31)));
-    const T du = ld_cg(dist + u);
     const int32_t k0 = prow[u], k1 = prow[u + 1];
+    if (hq && k1 - k0 > kPushHub) {  // left to k_sssp_push_hub
+      if (lane == 0) hq[atomicAdd(&ctr->nh, 1ull)] = u;
+      continue;
+    }
+    const T du = ld_cg(dist + u);
     for (int32_t base = k0; base < k1; base += 32) {
       const int32_t k = base + lane;
       bool add = false;
@@ -813,6 +905,48 @@ __global__ void __launch_bounds__(256)
         }
       }
       warp_append(add, w, 0, qn, ctr);
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_sssp_push_hub(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+                    const T* __restrict__ pw, const int32_t* __restrict__ hq, T* dist,
+                    unsigned* inq_next, int32_t* qn, Counters* ctr, const Counters* hctr) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t nh = (int64_t)*((volatile const unsigned long long*)&hctr->nh);
+  int64_t off = 0;
+  for (int64_t h = 0; h < nh; ++h) {
+    const int32_t u = hq[h];
+    const int32_t k0 = prow[u], k1 = prow[u + 1];
+    const int64_t np = (k1 - k0 + kPushPiece - 1) / kPushPiece;
+    const int64_t p0 = first_piece(gw, nw, off);
+    off += np;
+    if (p0 >= np) continue;
+    const T du = ld_cg(dist + u);
+    for (int64_t p = p0; p < np; p += nw) {
+      const int32_t kb = k0 + (int32_t)p * kPushPiece;
+      const int32_t ke = kb + kPushPiece < k1 ? kb + kPushPiece : k1;
+      for (int32_t base = kb; base < ke; base += 32) {
+        const int32_t k = base + lane;
+        bool add = false;
+        int32_t w = 0;
+        if (k < ke) {
+          w = __ldg(pcol + k);
+          const T cand = relax_add(__ldg(pw + k), du);
+          if (cand < ld_cg(dist + w)) {
+            const T old = atomic_min_t(dist + w, cand);
+            if (cand < old) {
+              const unsigned bit = 1u << (w & 31);
+              add = !(atomicOr(inq_next + (w >> 5), bit) & bit);
+            }
+          }
+        }
+        warp_append(add, w, 0, qn, ctr);
+      }
     }
   }
 }
@@ -1026,9 +1160,14 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
     }
     ++rounds;
     GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+    const bool hubs = P.max_deg > kPushHub;
     k_sssp_push<T><<<gridsz(ctx, nf * 32), 256, 0, ctx->stream>>>(
         P.rowptr, P.colval, static_cast<const T*>(P.w), sc.q[cur], nf, d, sc.fb[cur],
-        sc.fb[cur ^ 1], sc.q[cur ^ 1], sc.ctr);
+        sc.fb[cur ^ 1], sc.q[cur ^ 1], sc.ctr, hubs ? sc.hq : nullptr);
+    if (hubs)
+      k_sssp_push_hub<T><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(
+          P.rowptr, P.colval, static_cast<const T*>(P.w), sc.hq, d, sc.fb[cur ^ 1], sc.q[cur ^ 1],
+          sc.ctr, sc.ctr);
     GG_CUDA(cudaGetLastError());
     GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
     GG_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -1,0 +1,362 @@
+// gg_msearch.cuh -- device code shared by the batched searches (gg_batch.cu) and
+// the query server (gg_serve.cu): many BFS / shortest-path sources advanced together
+// over one graph.
+//  * BFS: the sources' frontier / visited sets are bits of W <= 8 words per vertex.
+//    A level (k_ms_level) ORs the frontier words of a vertex's in-neighbours (edges
+//    with odd / true values, the levels semiring of src/algorithms/bfs.jl:52-59) into
+//    its unvisited bits, for the sources in `act` only (those whose frontier is not
+//    empty); a vertex stops scanning once all of them reached it.  Vertices with more
+//    than kCoopDeg in-edges are scanned by the whole warp; hubs (more than kHubDegB)
+//    in pieces by separate warps (k_ms_hub), finished by k_ms_hub_final.  New levels
+//    are written through an output policy (a distance matrix, or per-query buffers).
+//  * Shortest paths: 32 source columns, lane = column, distances vertex-major so one
+//    in-neighbour costs one 128-byte read.  A round (k_ms_round) pulls from the
+//    in-neighbours whose distances changed in the previous round and lowers D in
+//    place; hubs are relaxed in pieces with atomic min (k_ms_round_hub).  The fixpoint
+//    is that of shortest_path's Jacobi rounds (src/algorithms/shortest_path.jl:61-80).
+#pragma once
+
+#include "gg_semiring.cuh"
+
+namespace gg {
+
+int graph_view(gg_ctx* ctx, gg_mat* A, const int32_t** rp, const int32_t** cv, const void** nz,
+               bool* all_odd, bool* nonneg);  // gg_graph.cu
+int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n);  // gg_batch.cu
+
+namespace {
+
+static const unsigned kFullB = 0xffffffffu;
+static const int kMaxW = 8;  // 256 sources per BFS group
+
+struct BatchGraph {  // CSR view of A_T used by the batched kernels
+  const int32_t* rowptr;
+  const int32_t* colval;
+  const void* nz;
+  int tv;
+  bool odd_only;
+};
+
+__device__ __forceinline__ bool b_odd(const void* nz, int tv, int64_t k) {
+  switch (tv) {
+    case GG_BOOL: return static_cast<const uint8_t*>(nz)[k] & 1;
+    case GG_INT32: return static_cast<const int32_t*>(nz)[k] & 1;
+    case GG_INT64: return static_cast<const int64_t*>(nz)[k] & 1;
+  }
+  return false;
+}
+
+static const int kCoopDeg = 32;  // in-degree above which the whole warp scans a vertex
+
+// output policies of the BFS kernels: source column q reached vertex v this level
+struct LevelOutMatrix {  // dist[q * ld + v] = level
+  int32_t* dist;
+  int64_t ld;
+  int32_t level;
+  __device__ __forceinline__ void put(int q, int64_t v) const { dist[(int64_t)q * ld + v] = level; }
+};
+struct LevelOutSlots {  // per-query buffers: out[q][v] = tick - start[q]
+  int32_t* const* outp;
+  const int32_t* start;
+  int32_t tick;
+  __device__ __forceinline__ void put(int q, int64_t v) const { outp[q][v] = tick - start[q]; }
+};
+
+// OR of the frontier words of in-edges [k0, k1) of one vertex, the whole warp
+// scanning 32 edges per step; stops once every bit of m is set.  Uniform result.
+template <int W>
+__device__ __forceinline__ void warp_scan_or(const BatchGraph& g, const unsigned* __restrict__ F,
+                                             int64_t k0, int64_t k1, const unsigned (&m)[W],
+                                             unsigned (&acc)[W], int lane) {
+#pragma unroll
+  for (int w = 0; w < W; ++w) acc[w] = 0;
+  for (int64_t kb = k0; kb < k1; kb += 32) {
+    const int64_t k = kb + lane;
+    unsigned f[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) f[w] = 0;
+    if (k < k1 && (!g.odd_only || b_odd(g.nz, g.tv, k))) {
+      const int64_t u = (int64_t)__ldg(g.colval + k) - 1;
+#pragma unroll
+      for (int w = 0; w < W; ++w) f[w] = __ldg(F + u * W + w);
+    }
+    bool full = true;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      acc[w] |= __reduce_or_sync(kFullB, f[w]);
+      full &= (acc[w] & m[w]) == m[w];
+    }
+    if (full) break;
+  }
+}
+
+// one bottom-up level for a group of sources (W words per vertex); act holds the
+// sources whose frontier is non-empty, act_next collects those of the next level
+template <int W, class Out>
+__global__ void __launch_bounds__(256)
+    k_ms_level(int64_t n, BatchGraph g, const unsigned* __restrict__ F, unsigned* Fn,
+               unsigned* V, const unsigned* __restrict__ act, unsigned* act_next, Out out,
+               unsigned long long* count) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned am[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) am[w] = act[w];
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int64_t v = base + threadIdx.x;
+    unsigned m[W], acc[W];
+    bool open = false, hub = false;
+    int64_t k0 = 0, k1 = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      m[w] = 0;
+      acc[w] = 0;
+    }
+    if (v < n) {
+      k0 = (int64_t)g.rowptr[v] - 1;
+      k1 = (int64_t)g.rowptr[v + 1] - 1;
+      hub = k1 - k0 > kHubDegB;
+      if (!hub) {
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          m[w] = ~V[v * W + w] & am[w];
+          open |= m[w] != 0;
+        }
+      }
+    }
+    const bool light = open && k1 - k0 <= kCoopDeg;
+    if (light) {
+      for (int64_t k = k0; k < k1; ++k) {
+        if (g.odd_only && !b_odd(g.nz, g.tv, k)) continue;
+        const int64_t u = (int64_t)__ldg(g.colval + k) - 1;
+        bool full = true;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          acc[w] |= __ldg(F + u * W + w);
+          full &= (acc[w] & m[w]) == m[w];
+        }
+        if (full) break;  // every open source reached this vertex
+      }
+    }
+    unsigned coop = __ballot_sync(kFullB, open && !light);
+    while (coop) {
+      const int h = __ffs(coop) - 1;
+      coop &= coop - 1;
+      unsigned hm[W], ha[W];
+#pragma unroll
+      for (int w = 0; w < W; ++w) hm[w] = __shfl_sync(kFullB, m[w], h);
+      warp_scan_or<W>(g, F, __shfl_sync(kFullB, k0, h), __shfl_sync(kFullB, k1, h), hm, ha, lane);
+      if (lane == h) {
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] = ha[w];
+      }
+    }
+    unsigned anynew = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      acc[w] &= m[w];
+      anynew |= acc[w];
+      if (v < n && !hub) {  // hubs are finished by k_ms_hub_final
+        if (acc[w]) V[v * W + w] |= acc[w];
+        Fn[v * W + w] = acc[w];
+      }
+    }
+    // level writes, one source column at a time (coalesced over the warp's vertices)
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const unsigned any_w = __reduce_or_sync(kFullB, acc[w]);
+      if (lane == 0 && any_w) atomicOr(act_next + w, any_w);
+      unsigned u = any_w;
+      while (u) {
+        const int b = __ffs(u) - 1;
+        u &= u - 1;
+        if ((acc[w] >> b) & 1u) out.put(w * 32 + b, v);
+      }
+    }
+    const unsigned bal = __ballot_sync(kFullB, anynew != 0);
+    if (lane == 0 && bal) atomicAdd(count, (unsigned long long)__popc(bal));
+  }
+}
+
+// hub pieces: one warp per piece ORs its in-neighbours' frontier words into the
+// hub's accumulator
+template <int W>
+__global__ void __launch_bounds__(256)
+    k_ms_hub(BatchGraph g, const int4* __restrict__ pieces, int64_t npiece,
+             const int32_t* __restrict__ hubs, const unsigned* __restrict__ F,
+             const unsigned* __restrict__ V, const unsigned* __restrict__ act, unsigned* hacc) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < npiece;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int4 p = pieces[i];
+    const int64_t v = hubs[p.x];
+    unsigned m[W], ha[W];
+    bool open = false;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      m[w] = ~V[v * W + w] & act[w];
+      open |= m[w] != 0;
+    }
+    if (!open) continue;
+    warp_scan_or<W>(g, F, p.y, p.z, m, ha, lane);
+    if (lane == 0) {
+#pragma unroll
+      for (int w = 0; w < W; ++w)
+        if (ha[w] & m[w]) atomicOr(hacc + (int64_t)p.x * kMaxW + w, ha[w] & m[w]);
+    }
+  }
+}
+
+// one thread per hub: new bits, visited, next frontier, levels
+template <int W, class Out>
+__global__ void k_ms_hub_final(const int32_t* __restrict__ hubs, int64_t nhub, unsigned* hacc,
+                               unsigned* Fn, unsigned* V, const unsigned* __restrict__ act,
+                               unsigned* act_next, Out out, unsigned long long* count) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nhub;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = hubs[i];
+    bool any = false;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const unsigned m = ~V[v * W + w] & act[w];
+      const unsigned a = hacc[i * kMaxW + w] & m;
+      hacc[i * kMaxW + w] = 0;
+      Fn[v * W + w] = a;
+      if (!a) continue;
+      any = true;
+      V[v * W + w] |= a;
+      atomicOr(act_next + w, a);
+      unsigned u = a;
+      while (u) {
+        const int b = __ffs(u) - 1;
+        u &= u - 1;
+        out.put(w * 32 + b, v);
+      }
+    }
+    if (any) atomicAdd(count, 1ull);
+  }
+}
+
+template <typename T> __device__ __forceinline__ T b_relax(T w, T d) {
+  return (w == Lim<T>::max() || d == Lim<T>::max()) ? Lim<T>::max() : w_add(w, d);
+}
+
+template <typename T>
+__device__ __forceinline__ T b_weight(const void* nz, int tv, int64_t k) {
+  switch (tv) {
+    case GG_BOOL: return static_cast<T>(static_cast<const uint8_t*>(nz)[k]);
+    case GG_INT32: return static_cast<T>(static_cast<const int32_t*>(nz)[k]);
+    case GG_INT64: return static_cast<T>(static_cast<const int64_t*>(nz)[k]);
+    case GG_FLOAT32: return static_cast<T>(static_cast<const float*>(nz)[k]);
+  }
+  return static_cast<T>(static_cast<const double*>(nz)[k]);
+}
+
+// pull over in-edges [k0, k1) of v from in-neighbours that changed last round:
+// per-lane (source column) minimum of D[u] + w
+template <typename T>
+__device__ __forceinline__ bool bs_pull(const BatchGraph& g, const T* D,
+                                        const uint8_t* __restrict__ chg, int64_t k0, int64_t k1,
+                                        int lane, T& best) {
+  bool any = false;
+  for (int64_t kb = k0; kb < k1; kb += 32) {
+    const int64_t kk = kb + lane;
+    int32_t u = -1;
+    if (kk < k1) {
+      const int32_t c = __ldg(g.colval + kk) - 1;
+      if (chg[c]) u = c;
+    }
+    unsigned act = __ballot_sync(kFullB, u >= 0);
+    while (act) {
+      const int src_lane = __ffs(act) - 1;
+      act &= act - 1;
+      const int32_t uu = __shfl_sync(kFullB, u, src_lane);
+      const T w = b_weight<T>(g.nz, g.tv, kb + src_lane);
+      const T cand = b_relax(w, D[(int64_t)uu * 32 + lane]);
+      if (cand < best) best = cand;
+      any = true;
+    }
+  }
+  return any;
+}
+
+// one round: warp per vertex v, lane = source column; pull from in-neighbours that
+// changed last round, lower D[v] in place, flag v when any column dropped (chg_next
+// is cleared before the round).  Hubs are left to k_ms_round_hub.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_ms_round(int64_t n, BatchGraph g, T* D, const uint8_t* __restrict__ chg,
+               uint8_t* chg_next, unsigned long long* count, unsigned* drop) {
+  const int lane = threadIdx.x & 31;
+  unsigned dropped_cols = 0;
+  for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n;
+       v += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t k0 = (int64_t)g.rowptr[v] - 1, k1 = (int64_t)g.rowptr[v + 1] - 1;
+    if (k1 - k0 > kHubDegB) continue;
+    T best = Lim<T>::max();
+    const bool any = bs_pull<T>(g, D, chg, k0, k1, lane, best);
+    bool dropped = false;
+    if (any) {
+      T* dv = D + v * 32 + lane;
+      if (best < *dv) {
+        *dv = best;
+        dropped = true;
+      }
+    }
+    const unsigned b = __ballot_sync(kFullB, dropped);
+    dropped_cols |= b;
+    if (lane == 0 && b) {
+      chg_next[v] = 1;
+      atomicAdd(count, 1ull);
+    }
+  }
+  if (drop && lane == 0 && dropped_cols) atomicOr(drop, dropped_cols);
+}
+
+template <typename T> __device__ __forceinline__ T b_atomic_min(T* p, T v);
+template <> __device__ __forceinline__ int32_t b_atomic_min<int32_t>(int32_t* p, int32_t v) {
+  return atomicMin(p, v);
+}
+template <> __device__ __forceinline__ int64_t b_atomic_min<int64_t>(int64_t* p, int64_t v) {
+  return (int64_t)atomicMin((long long*)p, (long long)v);
+}
+// distances are non-negative here (never -0.0: +0.0 + w), so floats order like
+// their bit patterns
+template <> __device__ __forceinline__ float b_atomic_min<float>(float* p, float v) {
+  return __int_as_float(atomicMin((int*)p, __float_as_int(v)));
+}
+template <> __device__ __forceinline__ double b_atomic_min<double>(double* p, double v) {
+  return __longlong_as_double(atomicMin((long long*)p, __double_as_longlong(v)));
+}
+
+// hub pieces: one warp per piece, atomic min into the hub's 32 columns
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_ms_round_hub(BatchGraph g, const int4* __restrict__ pieces, int64_t npiece,
+                   const int32_t* __restrict__ hubs, T* D, const uint8_t* __restrict__ chg,
+                   uint8_t* chg_next, unsigned long long* count, unsigned* drop) {
+  const int lane = threadIdx.x & 31;
+  unsigned dropped_cols = 0;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < npiece;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int4 p = pieces[i];
+    const int64_t v = hubs[p.x];
+    T best = Lim<T>::max();
+    const bool any = bs_pull<T>(g, D, chg, p.y, p.z, lane, best);
+    bool dropped = false;
+    if (any) {
+      T* dv = D + v * 32 + lane;
+      if (best < *dv) dropped = best < b_atomic_min<T>(dv, best);
+    }
+    const unsigned b = __ballot_sync(kFullB, dropped);
+    dropped_cols |= b;
+    if (lane == 0 && b) {
+      chg_next[v] = 1;
+      atomicAdd(count, 1ull);
+    }
+  }
+  if (drop && lane == 0 && dropped_cols) atomicOr(drop, dropped_cols);
+}
+
+}  // namespace
+}  // namespace gg

@@ -4,21 +4,25 @@
 // plus-times SpMV iterations (x <- A x, k times) from a dense start vector, each
 // against one of the server's resident graphs.  A scheduler thread keeps, per graph
 // and query kind, an executor with a fixed number of slots and advances all active
-// slots together, one step per tick:
+// slots of an executor together, one step per tick:
 //  * BFS: 256 slots, one bit each in the packed frontier / visited words; a tick is
-//    one bottom-up level for every active slot, each slot writing its own levels
-//    (tick - admission tick) into its output;
-//  * shortest paths: 32 slots, one distance column each (vertex-major, so one
-//    in-neighbour is one 128-byte read); a tick is one relaxation round from the
-//    vertices that changed in the previous round; a slot completes after a round
-//    in which none of its distances dropped;
+//    one bottom-up level for the slots whose frontier is not empty, each slot
+//    writing its own levels (tick - admission tick) into its output;
+//  * shortest paths: 32 slots, one distance column each (vertex-major); a tick is
+//    one relaxation round from the vertices that changed in the previous round; a
+//    slot completes after a round in which none of its distances dropped;
 //  * SpMV iterations: 32 slots, one column of a row-major n x 32 block; a tick is one
 //    SpMM of the block; a slot completes after its k steps.
-// Requests that arrive while others run are admitted into free slots at the next
-// tick (continuous batching).  Executors are created on first use and only when the
-// device has the memory they need plus the configured reserve (admission by free
-// HBM); requests wait in the queue otherwise.  Every slot's computation is
-// independent of the other slots, so a result does not depend on the mix it ran in.
+// (BFS and shortest-path kernels: gg_msearch.cuh, hub-aware.)  Every executor owns
+// a CUDA stream and a private context; the scheduler never waits for the GPU: it
+// polls each executor's tick event, retires finished slots, admits waiting requests
+// into free slots (continuous batching) and enqueues the next tick, so small graphs'
+// queries advance at their own pace beside long searches on large graphs.
+// Executors are created on first use and only when the device has the memory they
+// need plus the configured reserve (admission by free HBM); requests wait in the
+// queue otherwise.  Every slot's computation is independent of the other slots, so a
+// result does not depend on the mix it ran in.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -26,14 +30,10 @@
 #include <thread>
 #include <vector>
 
-#include "gg_semiring.cuh"
+#include "gg_msearch.cuh"
 
 namespace gg {
 
-int graph_view(gg_ctx* ctx, gg_mat* A, const int32_t** rp, const int32_t** cv, const void** nz,
-               bool* all_odd, bool* nonneg);
-
-static const unsigned kFullS = 0xffffffffu;
 static const int kBfsSlots = 256, kBfsW = 8, kColSlots = 32;
 
 static double now_s() {
@@ -52,29 +52,16 @@ struct Request {
 };
 
 struct SrvGraph {
-  const int32_t* rp;
-  const int32_t* cv;
-  const void* nz;
-  int tv;
-  bool odd_only;
+  BatchGraph g;
   bool nonneg;
   int64_t n;
 };
 
 // ---------------------------------------------------------------------------------
-// kernels
+// admission / output kernels
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ bool s_odd(const void* nz, int tv, int64_t k) {
-  switch (tv) {
-    case GG_BOOL: return static_cast<const uint8_t*>(nz)[k] & 1;
-    case GG_INT32: return static_cast<const int32_t*>(nz)[k] & 1;
-    case GG_INT64: return static_cast<const int64_t*>(nz)[k] & 1;
-  }
-  return false;
-}
-
-// admission of BFS slots (bits in amask): clear their visited / frontier bits,
-// fill their outputs with typemax, then seed their sources
+// BFS slots (bits in amask): clear their visited / frontier bits and fill their
+// outputs with typemax, then seed their sources
 __global__ void k_sb_admit_clear(int64_t n, unsigned* V, unsigned* F, const unsigned* amask,
                                  int32_t* const* outp, const int* slots, int nslots) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
@@ -99,92 +86,9 @@ __global__ void k_sb_admit_seed(unsigned* V, unsigned* F, int32_t* const* outp, 
   }
 }
 
-// one level for every active BFS slot; act receives the OR of the new bits
-__global__ void __launch_bounds__(256)
-    k_sb_level(int64_t n, SrvGraph g, const unsigned* __restrict__ F, unsigned* Fn, unsigned* V,
-               const unsigned* __restrict__ live, int32_t tick, const int32_t* __restrict__ start,
-               int32_t* const* __restrict__ outp, unsigned* act) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  unsigned lm[kBfsW], seen[kBfsW];
-#pragma unroll
-  for (int w = 0; w < kBfsW; ++w) {
-    lm[w] = live[w];
-    seen[w] = 0;
-  }
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
-    const int64_t v = base + threadIdx.x;
-    unsigned m[kBfsW], acc[kBfsW];
-    bool open = false;
-#pragma unroll
-    for (int w = 0; w < kBfsW; ++w) {
-      m[w] = 0;
-      acc[w] = 0;
-    }
-    if (v < n) {
-#pragma unroll
-      for (int w = 0; w < kBfsW; ++w) {
-        m[w] = ~V[v * kBfsW + w] & lm[w];
-        open |= m[w] != 0;
-      }
-    }
-    if (open) {
-      const int64_t k1 = (int64_t)g.rp[v + 1] - 1;
-      for (int64_t k = (int64_t)g.rp[v] - 1; k < k1; ++k) {
-        if (g.odd_only && !s_odd(g.nz, g.tv, k)) continue;
-        const int64_t u = (int64_t)__ldg(g.cv + k) - 1;
-        bool full = true;
-#pragma unroll
-        for (int w = 0; w < kBfsW; ++w) {
-          acc[w] |= __ldg(F + u * kBfsW + w);
-          full &= (acc[w] & m[w]) == m[w];
-        }
-        if (full) break;
-      }
-    }
-#pragma unroll
-    for (int w = 0; w < kBfsW; ++w) {
-      acc[w] &= m[w];
-      seen[w] |= acc[w];
-      if (v < n) {
-        if (acc[w]) V[v * kBfsW + w] |= acc[w];
-        Fn[v * kBfsW + w] = acc[w];
-      }
-    }
-#pragma unroll
-    for (int w = 0; w < kBfsW; ++w) {
-      unsigned u = __reduce_or_sync(kFullS, acc[w]);
-      while (u) {
-        const int b = __ffs(u) - 1;
-        u &= u - 1;
-        const int q = w * 32 + b;
-        if ((acc[w] >> b) & 1u) outp[q][v] = tick - start[q];
-      }
-    }
-  }
-#pragma unroll
-  for (int w = 0; w < kBfsW; ++w) {
-    const unsigned r = __reduce_or_sync(kFullS, seen[w]);
-    if ((threadIdx.x & 31) == 0 && r) atomicOr(act + w, r);
-  }
-}
-
-template <typename T> __device__ __forceinline__ T s_relax(T w, T d) {
-  return (w == Lim<T>::max() || d == Lim<T>::max()) ? Lim<T>::max() : w_add(w, d);
-}
-template <typename T> __device__ __forceinline__ T s_weight(const void* nz, int tv, int64_t k) {
-  switch (tv) {
-    case GG_BOOL: return static_cast<T>(static_cast<const uint8_t*>(nz)[k]);
-    case GG_INT32: return static_cast<T>(static_cast<const int32_t*>(nz)[k]);
-    case GG_INT64: return static_cast<T>(static_cast<const int64_t*>(nz)[k]);
-    case GG_FLOAT32: return static_cast<T>(static_cast<const float*>(nz)[k]);
-  }
-  return static_cast<T>(static_cast<const double*>(nz)[k]);
-}
-
-// admission of shortest-path columns: D[:, q] = typemax, D[s, q] = 0, s changed
+// shortest-path columns in qmask: D[:, q] = typemax
 template <typename T>
-__global__ void k_ss_admit(int64_t n, T* D, unsigned qmask, uint8_t* chg, const int* slots,
-                           const int64_t* srcs, int nslots) {
+__global__ void k_ss_admit(int64_t n, T* D, unsigned qmask) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x)
     for (int q = 0; q < kColSlots; ++q)
@@ -196,51 +100,6 @@ __global__ void k_ss_seed(T* D, uint8_t* chg, const int* slots, const int64_t* s
     D[srcs[i] * kColSlots + slots[i]] = T(0);
     chg[srcs[i]] = 1;
   }
-}
-
-// one round for every column (inactive columns are at their fixpoint and do not
-// move); drop receives the columns whose distances fell
-template <typename T>
-__global__ void __launch_bounds__(256)
-    k_ss_round(int64_t n, SrvGraph g, T* D, const uint8_t* __restrict__ chg, uint8_t* chg_next,
-               unsigned* drop) {
-  const int lane = threadIdx.x & 31;
-  unsigned dropped_cols = 0;
-  for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n;
-       v += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const int64_t k0 = (int64_t)g.rp[v] - 1, k1 = (int64_t)g.rp[v + 1] - 1;
-    T best = Lim<T>::max();
-    bool any = false;
-    for (int64_t kb = k0; kb < k1; kb += 32) {
-      const int64_t kk = kb + lane;
-      int32_t u = -1;
-      if (kk < k1) {
-        const int32_t c = __ldg(g.cv + kk) - 1;
-        if (chg[c]) u = c;
-      }
-      unsigned a = __ballot_sync(kFullS, u >= 0);
-      while (a) {
-        const int sl = __ffs(a) - 1;
-        a &= a - 1;
-        const int32_t uu = __shfl_sync(kFullS, u, sl);
-        const T cand = s_relax(s_weight<T>(g.nz, g.tv, kb + sl), D[(int64_t)uu * kColSlots + lane]);
-        if (cand < best) best = cand;
-        any = true;
-      }
-    }
-    bool dr = false;
-    if (any) {
-      T* dv = D + v * kColSlots + lane;
-      if (best < *dv) {
-        *dv = best;
-        dr = true;
-      }
-    }
-    const unsigned b = __ballot_sync(kFullS, dr);
-    if (lane == 0) chg_next[v] = b ? 1 : 0;
-    dropped_cols |= b;
-  }
-  if (lane == 0 && dropped_cols) atomicOr(drop, dropped_cols);
 }
 
 template <typename T>
@@ -279,25 +138,31 @@ struct Slot {
 struct Executor {
   int kind = 0;
   bool ready = false;
+  gg_ctx ectx;  // private stream and scratch
+  cudaEvent_t ev = nullptr, ev_out = nullptr;
+  bool inflight = false;
+  std::vector<Request> finishing;  // results being copied out (ev_out)
   std::vector<Slot> slots;
   std::vector<int> free_list;
   // BFS
-  unsigned *F = nullptr, *Fn = nullptr, *V = nullptr, *live = nullptr, *act = nullptr;
+  unsigned *F = nullptr, *Fn = nullptr, *V = nullptr, *act = nullptr, *hacc = nullptr;
   int32_t** outp = nullptr;
   int32_t* start = nullptr;
   int32_t tick = 0;
+  unsigned act_host[kBfsW] = {0};  // sources whose frontier is not empty
   // SSSP
   void* D = nullptr;
   uint8_t *c0 = nullptr, *c1 = nullptr;
-  unsigned* drop = nullptr;
   int dtype = 0;
   // SpMV iterations
   float *X = nullptr, *Y = nullptr;
-  // admission staging
+  // staging (pinned host / device)
   int* d_slots = nullptr;
   int64_t* d_srcs = nullptr;
   unsigned* d_amask = nullptr;
-  unsigned* h_result = nullptr;  // pinned: act / drop of the last tick
+  unsigned long long* d_cnt = nullptr;
+  unsigned* h_stage = nullptr;   // pinned: small uploads
+  unsigned* h_result = nullptr;  // pinned: new bits / dropped columns of the last tick
   size_t bytes = 0;
   int active() const {
     int a = 0;
@@ -310,7 +175,7 @@ struct Executor {
 
 struct gg_server {
   gg_ctx* ctx = nullptr;
-  gg_ctx own;  // private context state bound to the server stream
+  gg_ctx own;  // context used for graph analysis on the server's stream
   cudaStream_t stream = nullptr;
   int64_t reserve = 0;
   std::vector<gg_mat*> graphs;
@@ -348,9 +213,39 @@ static size_t exec_bytes(int kind, int64_t n, int dtype) {
   }
 }
 
+static void exec_free(Executor& E) {
+  if (E.ectx.stream) cudaStreamSynchronize(E.ectx.stream);
+  cudaFree(E.F);
+  cudaFree(E.Fn);
+  cudaFree(E.V);
+  cudaFree(E.act);
+  cudaFree(E.hacc);
+  cudaFree(E.outp);
+  cudaFree(E.start);
+  cudaFree(E.D);
+  cudaFree(E.c0);
+  cudaFree(E.c1);
+  cudaFree(E.X);
+  cudaFree(E.Y);
+  cudaFree(E.d_slots);
+  cudaFree(E.d_srcs);
+  cudaFree(E.d_amask);
+  cudaFree(E.d_cnt);
+  cudaFreeHost(E.h_stage);
+  cudaFreeHost(E.h_result);
+  cudaFree(E.ectx.scratch);
+  cudaFree(E.ectx.d_flags);
+  cudaFreeHost(E.ectx.h_flags);
+  if (E.ev) cudaEventDestroy(E.ev);
+  if (E.ev_out) cudaEventDestroy(E.ev_out);
+  if (E.ectx.stream) cudaStreamDestroy(E.ectx.stream);
+  E.ectx.scratch = nullptr;
+  E = Executor();
+}
+
 static int exec_create(gg_server* S, int gi, int kind, Executor& E) {
-  const SrvGraph& g = S->views[gi];
-  const int64_t n = g.n;
+  const SrvGraph& sg = S->views[gi];
+  const int64_t n = sg.n;
   const int dt = S->graphs[gi]->dtype == GG_BOOL ? GG_INT32 : S->graphs[gi]->dtype;
   const size_t need = exec_bytes(kind, n, dt);
   size_t fr = 0, tot = 0;
@@ -359,7 +254,23 @@ static int exec_create(gg_server* S, int gi, int kind, Executor& E) {
   E.kind = kind;
   E.dtype = dt;
   E.bytes = need;
-  cudaStream_t st = S->stream;
+  E.ectx.device = S->own.device;
+  E.ectx.num_sms = S->own.num_sms;
+  // short queries first: executors of smaller graphs get higher stream priorities,
+  // so their ticks are scheduled ahead of long searches on large graphs
+  int least = 0, greatest = 0;
+  GG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  int lg = 0;
+  while ((int64_t(1) << (lg + 1)) <= n) ++lg;
+  int prio = greatest + (lg > 16 ? (lg - 16) / 2 : 0);
+  if (kind == GG_QUERY_SSSP) prio += 1;
+  if (prio > least) prio = least;
+  GG_CUDA(cudaStreamCreateWithPriority(&E.ectx.stream, cudaStreamNonBlocking, prio));
+  GG_CUDA(cudaEventCreateWithFlags(&E.ev, cudaEventDisableTiming));
+  GG_CUDA(cudaEventCreateWithFlags(&E.ev_out, cudaEventDisableTiming));
+  GG_CUDA(cudaMalloc((void**)&E.ectx.d_flags, 64 * sizeof(unsigned)));
+  GG_CUDA(cudaMallocHost((void**)&E.ectx.h_flags, 64 * sizeof(unsigned)));
+  cudaStream_t st = E.ectx.stream;
   const int nslots = kind == GG_QUERY_BFS ? kBfsSlots : kColSlots;
   E.slots.assign(nslots, Slot());
   E.free_list.clear();
@@ -367,35 +278,39 @@ static int exec_create(gg_server* S, int gi, int kind, Executor& E) {
   GG_CUDA(cudaMalloc((void**)&E.d_slots, nslots * sizeof(int)));
   GG_CUDA(cudaMalloc((void**)&E.d_srcs, nslots * sizeof(int64_t)));
   GG_CUDA(cudaMalloc((void**)&E.d_amask, 64));
+  GG_CUDA(cudaMalloc((void**)&E.d_cnt, 64));
+  GG_CUDA(cudaMallocHost((void**)&E.h_stage, 4096));
   GG_CUDA(cudaMallocHost((void**)&E.h_result, 64));
+  if (kind != GG_QUERY_SPMV_ITER)
+    GG_CHECK(build_hub_plan(&S->own, S->graphs[gi], sg.g.rowptr, n));
   if (kind == GG_QUERY_BFS) {
     const size_t b = (size_t)n * kBfsW * 4;
+    const HubPlan* hp = S->graphs[gi]->hubplan;
     GG_CUDA(cudaMalloc((void**)&E.F, b));
     GG_CUDA(cudaMalloc((void**)&E.Fn, b));
     GG_CUDA(cudaMalloc((void**)&E.V, b));
-    GG_CUDA(cudaMalloc((void**)&E.live, 64));
-    GG_CUDA(cudaMalloc((void**)&E.act, 64));
+    GG_CUDA(cudaMalloc((void**)&E.act, 2 * kBfsW * sizeof(unsigned)));
+    GG_CUDA(cudaMalloc((void**)&E.hacc, (hp->nhub + 1) * kBfsW * sizeof(unsigned)));
     GG_CUDA(cudaMalloc((void**)&E.outp, kBfsSlots * sizeof(int32_t*)));
     GG_CUDA(cudaMalloc((void**)&E.start, kBfsSlots * sizeof(int32_t)));
     GG_CUDA(cudaMemsetAsync(E.F, 0, b, st));
     GG_CUDA(cudaMemsetAsync(E.Fn, 0, b, st));
     GG_CUDA(cudaMemsetAsync(E.V, 0, b, st));
+    GG_CUDA(cudaMemsetAsync(E.hacc, 0, (hp->nhub + 1) * kBfsW * sizeof(unsigned), st));
     GG_CUDA(cudaMemsetAsync(E.outp, 0, kBfsSlots * sizeof(int32_t*), st));
   } else if (kind == GG_QUERY_SSSP) {
     GG_CUDA(cudaMalloc(&E.D, (size_t)n * kColSlots * dtype_size(dt)));
     GG_CUDA(cudaMalloc((void**)&E.c0, (size_t)n + 64));
     GG_CUDA(cudaMalloc((void**)&E.c1, (size_t)n + 64));
-    GG_CUDA(cudaMalloc((void**)&E.drop, 64));
     GG_CUDA(cudaMemsetAsync(E.c0, 0, (size_t)n + 64, st));
     GG_CUDA(cudaMemsetAsync(E.c1, 0, (size_t)n + 64, st));
     // every column starts at the fixpoint of "no source": typemax everywhere
-    GG_CUDA(cudaMemsetAsync(E.D, 0, (size_t)n * kColSlots * dtype_size(dt), st));
     const unsigned all = 0xffffffffu;
     switch (dt) {
-      case GG_INT32: k_ss_admit<int32_t><<<grid_s(S, n), 256, 0, st>>>(n, (int32_t*)E.D, all, E.c0, nullptr, nullptr, 0); break;
-      case GG_INT64: k_ss_admit<int64_t><<<grid_s(S, n), 256, 0, st>>>(n, (int64_t*)E.D, all, E.c0, nullptr, nullptr, 0); break;
-      case GG_FLOAT32: k_ss_admit<float><<<grid_s(S, n), 256, 0, st>>>(n, (float*)E.D, all, E.c0, nullptr, nullptr, 0); break;
-      default: k_ss_admit<double><<<grid_s(S, n), 256, 0, st>>>(n, (double*)E.D, all, E.c0, nullptr, nullptr, 0); break;
+      case GG_INT32: k_ss_admit<int32_t><<<grid_s(S, n), 256, 0, st>>>(n, (int32_t*)E.D, all); break;
+      case GG_INT64: k_ss_admit<int64_t><<<grid_s(S, n), 256, 0, st>>>(n, (int64_t*)E.D, all); break;
+      case GG_FLOAT32: k_ss_admit<float><<<grid_s(S, n), 256, 0, st>>>(n, (float*)E.D, all); break;
+      default: k_ss_admit<double><<<grid_s(S, n), 256, 0, st>>>(n, (double*)E.D, all); break;
     }
   } else {
     GG_CUDA(cudaMalloc((void**)&E.X, (size_t)n * kColSlots * 4));
@@ -407,36 +322,20 @@ static int exec_create(gg_server* S, int gi, int kind, Executor& E) {
   return GG_OK;
 }
 
-static void exec_free(Executor& E) {
-  cudaFree(E.F);
-  cudaFree(E.Fn);
-  cudaFree(E.V);
-  cudaFree(E.live);
-  cudaFree(E.act);
-  cudaFree(E.outp);
-  cudaFree(E.start);
-  cudaFree(E.D);
-  cudaFree(E.c0);
-  cudaFree(E.c1);
-  cudaFree(E.drop);
-  cudaFree(E.X);
-  cudaFree(E.Y);
-  cudaFree(E.d_slots);
-  cudaFree(E.d_srcs);
-  cudaFree(E.d_amask);
-  cudaFreeHost(E.h_result);
-  E = Executor();
-}
-
 // admit waiting requests of (graph, kind) into free slots; returns how many
 static int exec_admit(gg_server* S, int gi, Executor& E, std::vector<Request>& waiting) {
   if (waiting.empty() || E.free_list.empty()) return 0;
   const int64_t n = S->views[gi].n;
-  cudaStream_t st = S->stream;
-  std::vector<int> qs;
-  std::vector<int64_t> srcs;
+  cudaStream_t st = E.ectx.stream;
+  // staging layout in pinned memory: slots [0,256) ints | sources [256,512) int64 |
+  // output pointers [512, 768) | start ticks [768, 1024) -- in 4-byte words
+  int* hs = reinterpret_cast<int*>(E.h_stage);
+  int64_t* hsrc = reinterpret_cast<int64_t*>(E.h_stage + 256);
+  int k = 0;
   unsigned amask[kBfsW] = {0};
   size_t taken = 0;
+  // lowest free slot first (descending list, taken from the back)
+  std::sort(E.free_list.begin(), E.free_list.end(), [](int x, int y) { return x > y; });
   while (taken < waiting.size() && !E.free_list.empty()) {
     const int q = E.free_list.back();
     E.free_list.pop_back();
@@ -445,99 +344,139 @@ static int exec_admit(gg_server* S, int gi, Executor& E, std::vector<Request>& w
     sl.req = waiting[taken++];
     sl.start = E.tick;
     sl.steps_left = sl.req.steps;
-    qs.push_back(q);
-    srcs.push_back(sl.req.source - 1);
+    hs[k] = q;
+    hsrc[k] = sl.req.source - 1;
     amask[q >> 5] |= 1u << (q & 31);
+    ++k;
   }
   waiting.erase(waiting.begin(), waiting.begin() + taken);
-  const int k = (int)qs.size();
-  cudaMemcpyAsync(E.d_slots, qs.data(), k * sizeof(int), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(E.d_srcs, srcs.data(), k * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+  GG_CUDA(cudaMemcpyAsync(E.d_slots, hs, k * sizeof(int), cudaMemcpyHostToDevice, st));
+  GG_CUDA(cudaMemcpyAsync(E.d_srcs, hsrc, k * sizeof(int64_t), cudaMemcpyHostToDevice, st));
   if (E.kind == GG_QUERY_BFS) {
     for (int i = 0; i < k; ++i) {
-      int32_t* p = static_cast<int32_t*>(E.slots[qs[i]].req.out);
-      cudaMemcpyAsync(E.outp + qs[i], &p, sizeof(p), cudaMemcpyHostToDevice, st);
+      const int q = hs[i];
+      int32_t* p = static_cast<int32_t*>(E.slots[q].req.out);
+      GG_CUDA(cudaMemcpyAsync(E.outp + q, &p, sizeof(p), cudaMemcpyHostToDevice, st));
       int32_t t0 = E.tick;
-      cudaMemcpyAsync(E.start + qs[i], &t0, sizeof(t0), cudaMemcpyHostToDevice, st);
+      GG_CUDA(cudaMemcpyAsync(E.start + q, &t0, sizeof(t0), cudaMemcpyHostToDevice, st));
     }
-    cudaMemcpyAsync(E.d_amask, amask, sizeof(amask), cudaMemcpyHostToDevice, st);
+    unsigned* ham = E.h_stage + 1000;
+    for (int w = 0; w < kBfsW; ++w) {
+      ham[w] = amask[w];
+      E.act_host[w] |= amask[w];
+    }
+    GG_CUDA(cudaMemcpyAsync(E.d_amask, ham, kBfsW * sizeof(unsigned), cudaMemcpyHostToDevice, st));
     k_sb_admit_clear<<<grid_s(S, n), 256, 0, st>>>(n, E.V, E.F, E.d_amask, E.outp, E.d_slots, k);
     k_sb_admit_seed<<<1, 256, 0, st>>>(E.V, E.F, E.outp, E.d_slots, E.d_srcs, k);
   } else if (E.kind == GG_QUERY_SSSP) {
-    unsigned qm = 0;
-    for (int q : qs) qm |= 1u << q;
+    const unsigned qm = amask[0];
     switch (E.dtype) {
       case GG_INT32:
-        k_ss_admit<int32_t><<<grid_s(S, n), 256, 0, st>>>(n, (int32_t*)E.D, qm, E.c0, nullptr, nullptr, 0);
+        k_ss_admit<int32_t><<<grid_s(S, n), 256, 0, st>>>(n, (int32_t*)E.D, qm);
         k_ss_seed<int32_t><<<1, 64, 0, st>>>((int32_t*)E.D, E.c0, E.d_slots, E.d_srcs, k);
         break;
       case GG_INT64:
-        k_ss_admit<int64_t><<<grid_s(S, n), 256, 0, st>>>(n, (int64_t*)E.D, qm, E.c0, nullptr, nullptr, 0);
+        k_ss_admit<int64_t><<<grid_s(S, n), 256, 0, st>>>(n, (int64_t*)E.D, qm);
         k_ss_seed<int64_t><<<1, 64, 0, st>>>((int64_t*)E.D, E.c0, E.d_slots, E.d_srcs, k);
         break;
       case GG_FLOAT32:
-        k_ss_admit<float><<<grid_s(S, n), 256, 0, st>>>(n, (float*)E.D, qm, E.c0, nullptr, nullptr, 0);
+        k_ss_admit<float><<<grid_s(S, n), 256, 0, st>>>(n, (float*)E.D, qm);
         k_ss_seed<float><<<1, 64, 0, st>>>((float*)E.D, E.c0, E.d_slots, E.d_srcs, k);
         break;
       default:
-        k_ss_admit<double><<<grid_s(S, n), 256, 0, st>>>(n, (double*)E.D, qm, E.c0, nullptr, nullptr, 0);
+        k_ss_admit<double><<<grid_s(S, n), 256, 0, st>>>(n, (double*)E.D, qm);
         k_ss_seed<double><<<1, 64, 0, st>>>((double*)E.D, E.c0, E.d_slots, E.d_srcs, k);
         break;
     }
   } else {
-    for (int q : qs) k_si_load<<<grid_s(S, n), 256, 0, st>>>(n, E.X, q, E.slots[q].req.x);
+    for (int i = 0; i < k; ++i)
+      k_si_load<<<grid_s(S, n), 256, 0, st>>>(n, E.X, hs[i], E.slots[hs[i]].req.x);
   }
+  GG_CUDA(cudaGetLastError());
   return k;
 }
 
-// one tick of an executor (enqueued only; results read after the sync)
+template <typename T>
+static void ss_round(gg_server* S, Executor& E, const SrvGraph& sg, const HubPlan* hp) {
+  cudaStream_t st = E.ectx.stream;
+  const int64_t n = sg.n;
+  T* D = static_cast<T*>(E.D);
+  k_ms_round<T><<<grid_s(S, n * 32), 256, 0, st>>>(n, sg.g, D, E.c0, E.c1, E.d_cnt, E.d_amask);
+  if (hp->npiece > 0)
+    k_ms_round_hub<T><<<grid_s(S, hp->npiece * 32), 256, 0, st>>>(sg.g, hp->pieces, hp->npiece,
+                                                                  hp->hubs, D, E.c0, E.c1, E.d_cnt,
+                                                                  E.d_amask);
+}
+
+// one tick of an executor, enqueued on its stream, followed by its event
 static int exec_tick(gg_server* S, int gi, Executor& E) {
-  const SrvGraph& g = S->views[gi];
-  const int64_t n = g.n;
-  cudaStream_t st = S->stream;
+  const SrvGraph& sg = S->views[gi];
+  const int64_t n = sg.n;
+  cudaStream_t st = E.ectx.stream;
+  const HubPlan* hp = S->graphs[gi]->hubplan;
   ++E.tick;
   if (E.kind == GG_QUERY_BFS) {
-    unsigned live[kBfsW] = {0};
-    for (int q = 0; q < kBfsSlots; ++q)
-      if (E.slots[q].busy) live[q >> 5] |= 1u << (q & 31);
-    cudaMemcpyAsync(E.live, live, sizeof(live), cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(E.act, 0, 64, st);
-    k_sb_level<<<grid_s(S, n), 256, 0, st>>>(n, g, E.F, E.Fn, E.V, E.live, E.tick, E.start, E.outp,
-                                            E.act);
+    unsigned* ha = E.h_stage + 1008;  // act of this tick, then zeros for act_next
+    for (int w = 0; w < kBfsW; ++w) {
+      ha[w] = E.act_host[w];
+      ha[kBfsW + w] = 0;
+    }
+    GG_CUDA(cudaMemcpyAsync(E.act, ha, 2 * kBfsW * sizeof(unsigned), cudaMemcpyHostToDevice, st));
+    GG_CUDA(cudaMemsetAsync(E.d_cnt, 0, 8, st));
+    const LevelOutSlots out{E.outp, E.start, E.tick};
+    k_ms_level<kBfsW, LevelOutSlots><<<grid_s(S, n), 256, 0, st>>>(
+        n, sg.g, E.F, E.Fn, E.V, E.act, E.act + kBfsW, out, E.d_cnt);
+    if (hp->nhub > 0) {
+      k_ms_hub<kBfsW><<<grid_s(S, hp->npiece * 32), 256, 0, st>>>(sg.g, hp->pieces, hp->npiece,
+                                                                  hp->hubs, E.F, E.V, E.act, E.hacc);
+      k_ms_hub_final<kBfsW, LevelOutSlots><<<grid_s(S, hp->nhub), 256, 0, st>>>(
+          hp->hubs, hp->nhub, E.hacc, E.Fn, E.V, E.act, E.act + kBfsW, out, E.d_cnt);
+    }
     std::swap(E.F, E.Fn);
-    cudaMemcpyAsync(E.h_result, E.act, kBfsW * 4, cudaMemcpyDeviceToHost, st);
+    GG_CUDA(cudaMemcpyAsync(E.h_result, E.act + kBfsW, kBfsW * 4, cudaMemcpyDeviceToHost, st));
   } else if (E.kind == GG_QUERY_SSSP) {
-    cudaMemsetAsync(E.drop, 0, 4, st);
-    const int gw = grid_s(S, n * 32);
+    GG_CUDA(cudaMemsetAsync(E.d_amask, 0, 4, st));  // dropped columns of this round
+    GG_CUDA(cudaMemsetAsync(E.c1, 0, (size_t)n, st));
     switch (E.dtype) {
-      case GG_INT32: k_ss_round<int32_t><<<gw, 256, 0, st>>>(n, g, (int32_t*)E.D, E.c0, E.c1, E.drop); break;
-      case GG_INT64: k_ss_round<int64_t><<<gw, 256, 0, st>>>(n, g, (int64_t*)E.D, E.c0, E.c1, E.drop); break;
-      case GG_FLOAT32: k_ss_round<float><<<gw, 256, 0, st>>>(n, g, (float*)E.D, E.c0, E.c1, E.drop); break;
-      default: k_ss_round<double><<<gw, 256, 0, st>>>(n, g, (double*)E.D, E.c0, E.c1, E.drop); break;
+      case GG_INT32: ss_round<int32_t>(S, E, sg, hp); break;
+      case GG_INT64: ss_round<int64_t>(S, E, sg, hp); break;
+      case GG_FLOAT32: ss_round<float>(S, E, sg, hp); break;
+      default: ss_round<double>(S, E, sg, hp); break;
     }
     std::swap(E.c0, E.c1);
-    cudaMemcpyAsync(E.h_result, E.drop, 4, cudaMemcpyDeviceToHost, st);
+    GG_CUDA(cudaMemcpyAsync(E.h_result, E.d_amask, 4, cudaMemcpyDeviceToHost, st));
   } else {
-    int tc = GG_FLOAT32;
-    GG_CHECK(spmm_dispatch(&S->own, S->graphs[gi], tc, GG_OP_MUL, GG_OP_ADD, GG_OP_SECOND, E.Y,
-                           GG_FLOAT32, kColSlots, E.X, GG_FLOAT32, kColSlots, kColSlots,
+    // only the columns up to the highest busy slot are multiplied (free slots are
+    // reused lowest first, so few queries cost few columns)
+    int kact = 0;
+    for (int q = 0; q < kColSlots; ++q)
+      if (E.slots[q].busy) kact = q + 1;
+    GG_CHECK(spmm_dispatch(&E.ectx, S->graphs[gi], GG_FLOAT32, GG_OP_MUL, GG_OP_ADD, GG_OP_SECOND,
+                           E.Y, GG_FLOAT32, kColSlots, E.X, GG_FLOAT32, kColSlots, kact,
                            GG_ROW_MAJOR, nullptr, 0, 0, 0));
     std::swap(E.X, E.Y);
   }
   GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaEventRecord(E.ev, st));
+  E.inflight = true;
   return GG_OK;
 }
 
-// after the tick's sync: retire the slots that finished
-static void exec_retire(gg_server* S, int gi, Executor& E, std::vector<Request>& finished) {
+// after the tick's event: retire the slots that finished.  BFS results are complete
+// already; the others get an output copy and finish when ev_out completes.
+static int exec_retire(gg_server* S, int gi, Executor& E, std::vector<Request>& finished) {
   const int64_t n = S->views[gi].n;
-  cudaStream_t st = S->stream;
+  cudaStream_t st = E.ectx.stream;
+  bool copies = false;
+  if (E.kind == GG_QUERY_BFS)
+    for (int w = 0; w < kBfsW; ++w) E.act_host[w] = E.h_result[w];
   for (int q = 0; q < (int)E.slots.size(); ++q) {
     Slot& sl = E.slots[q];
     if (!sl.busy) continue;
     bool done = false;
     if (E.kind == GG_QUERY_BFS) {
       done = !((E.h_result[q >> 5] >> (q & 31)) & 1u);  // no new vertex this level
+      if (done) finished.push_back(sl.req);
     } else if (E.kind == GG_QUERY_SSSP) {
       done = !((E.h_result[0] >> q) & 1u);  // no distance of this column dropped
       if (done) {
@@ -555,9 +494,15 @@ static void exec_retire(gg_server* S, int gi, Executor& E, std::vector<Request>&
     if (done) {
       sl.busy = false;
       E.free_list.push_back(q);
-      finished.push_back(sl.req);
+      if (E.kind != GG_QUERY_BFS) {
+        E.finishing.push_back(sl.req);
+        copies = true;
+      }
     }
   }
+  if (copies) GG_CUDA(cudaEventRecord(E.ev_out, st));
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
 }
 
 static void server_loop(gg_server* S) {
@@ -570,7 +515,7 @@ static void server_loop(gg_server* S) {
       std::unique_lock<std::mutex> lk(S->mu);
       bool busy = false;
       for (auto& per_g : S->exec)
-        for (auto& E : per_g) busy |= E.ready && E.active() > 0;
+        for (auto& E : per_g) busy |= E.ready && (E.active() > 0 || E.inflight || !E.finishing.empty());
       for (auto& per_g : waiting)
         for (auto& w : per_g) busy |= !w.empty();
       if (!busy && S->queue.empty() && !S->stop)
@@ -583,7 +528,8 @@ static void server_loop(gg_server* S) {
       }
     }
     int rc = GG_OK;
-    bool ticked = false;
+    bool progress = false;
+    std::vector<Request> finished;
     for (size_t gi = 0; gi < S->graphs.size() && rc == GG_OK; ++gi) {
       for (int kk = 0; kk < 3 && rc == GG_OK; ++kk) {
         Executor& E = S->exec[gi][kk];
@@ -598,41 +544,53 @@ static void server_loop(gg_server* S) {
           if (rc) break;
         }
         if (!E.ready) continue;
-        exec_admit(S, (int)gi, E, waiting[gi][kk]);
+        if (!E.finishing.empty()) {
+          const cudaError_t q = cudaEventQuery(E.ev_out);
+          if (q == cudaSuccess) {
+            finished.insert(finished.end(), E.finishing.begin(), E.finishing.end());
+            E.finishing.clear();
+            progress = true;
+          } else if (q != cudaErrorNotReady) {
+            rc = cuda_error(q, "server results");
+            break;
+          }
+        }
+        if (E.inflight) {
+          const cudaError_t q = cudaEventQuery(E.ev);
+          if (q == cudaErrorNotReady) continue;
+          if (q != cudaSuccess) {
+            rc = cuda_error(q, "server tick");
+            break;
+          }
+          E.inflight = false;
+          ++S->ticks;
+          progress = true;
+          rc = exec_retire(S, (int)gi, E, finished);
+          if (rc) break;
+        }
+        if (exec_admit(S, (int)gi, E, waiting[gi][kk]) > 0) progress = true;
         if (E.active() > 0) {
           rc = exec_tick(S, (int)gi, E);
-          ticked = true;
+          progress = true;
         }
       }
     }
-    if (rc == GG_OK && ticked) {
-      cudaError_t e = cudaStreamSynchronize(S->stream);
-      if (e != cudaSuccess) rc = cuda_error(e, "server tick");
-    }
-    std::vector<Request> finished;
-    if (rc == GG_OK && ticked) {
-      for (size_t gi = 0; gi < S->graphs.size(); ++gi)
-        for (int kk = 0; kk < 3; ++kk)
-          if (S->exec[gi][kk].ready) exec_retire(S, (int)gi, S->exec[gi][kk], finished);
-      if (!finished.empty()) {
-        cudaError_t e = cudaStreamSynchronize(S->stream);  // result copies
-        if (e != cudaSuccess) rc = cuda_error(e, "server results");
+    if (!finished.empty() || rc != GG_OK) {
+      const double t = now_s();
+      std::lock_guard<std::mutex> lk(S->mu);
+      for (auto& r : finished) {
+        S->done_ids.push_back(r.id);
+        S->done_lat.push_back(t - r.t_submit);
+        --S->inflight;
       }
-      ++S->ticks;
+      if (rc != GG_OK) {
+        S->error = rc;
+        S->error_msg = gg_last_error();
+        S->stop = true;
+        break;
+      }
     }
-    const double t = now_s();
-    std::lock_guard<std::mutex> lk(S->mu);
-    for (auto& r : finished) {
-      S->done_ids.push_back(r.id);
-      S->done_lat.push_back(t - r.t_submit);
-      --S->inflight;
-    }
-    if (rc != GG_OK) {
-      S->error = rc;
-      S->error_msg = gg_last_error();
-      S->stop = true;
-      break;
-    }
+    if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
 }
 
@@ -675,9 +633,9 @@ int gg_server_add_graph(gg_server* S, const gg_mat* A_T, int* graph_id) {
   gg_mat* A = const_cast<gg_mat*>(A_T);
   SrvGraph g;
   bool all_odd = false, nonneg = false;
-  GG_CHECK(graph_view(&S->own, A, &g.rp, &g.cv, &g.nz, &all_odd, &nonneg));
-  g.tv = A->dtype;
-  g.odd_only = !all_odd;
+  GG_CHECK(graph_view(&S->own, A, &g.g.rowptr, &g.g.colval, &g.g.nz, &all_odd, &nonneg));
+  g.g.tv = A->dtype;
+  g.g.odd_only = !all_odd;
   g.nonneg = nonneg;
   g.n = A->m;
   S->graphs.push_back(A);
@@ -694,7 +652,7 @@ int gg_server_submit(gg_server* S, int kind, int graph, int64_t source, const fl
   const SrvGraph& g = S->views[graph];
   if (kind == GG_QUERY_BFS || kind == GG_QUERY_SSSP) {
     if (source < 1 || source > g.n) return set_error(GG_ERR_BOUNDS, "source %lld out of 1:%lld", (long long)source, (long long)g.n);
-    if (kind == GG_QUERY_BFS && dtype_is_float(g.tv))
+    if (kind == GG_QUERY_BFS && dtype_is_float(g.g.tv))
       return set_error(GG_ERR_UNSUPPORTED, "GPUGraphs_band has no method for floating-point matrices");
     if (kind == GG_QUERY_SSSP && !g.nonneg)
       return set_error(GG_ERR_UNSUPPORTED, "served shortest paths need non-negative weights");

@@ -22,6 +22,8 @@
 //    walking with stride C (slice-column-major, so a warp reads C consecutive
 //    words), stopping at the first -1 padding column like sell_spmv_kernel!
 //    (SELL.jl:31-63); rows of multi-chunk slices are combined by k_sell_combine.
+//  * k_sell_hot: the same for plus-times Float32 over frequency-relabelled columns,
+//    with the 32768 most gathered x values in shared memory.
 #include <algorithm>
 #include <vector>
 
@@ -423,15 +425,19 @@ __global__ void k_sell(SR sr, const int32_t* __restrict__ slice_ptr,
   }
 }
 
+// one warp per (multi-chunk slice, row): lanes fold the chunk partials lane-strided,
+// then a shuffle tree.  A row of <= kSellChunk entries has one non-neutral partial,
+// so its value is unchanged (x + 0 == x; the partials are never -0.0).
 template <class SR>
 __global__ void k_sell_combine(SR sr, const int32_t* __restrict__ perm, int64_t C, int64_t m,
                                const int4* __restrict__ multi, int64_t nmulti,
                                const typename SR::T* __restrict__ partials, int64_t range_lo,
                                int64_t range_hi, const void* mask, int tmask) {
   typedef typename SR::T T;
+  const int lane = threadIdx.x & 31;
   const int64_t total = nmulti * C;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < total;
+       t += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t q = t / C, o = t - q * C;
     const int4 d = multi[q];  // slice, first partial, chunks
     const int64_t srow = (int64_t)d.x * C + o;
@@ -440,8 +446,88 @@ __global__ void k_sell_combine(SR sr, const int32_t* __restrict__ perm, int64_t 
     if (range_lo > 0 && (r1 < range_lo || r1 > range_hi)) continue;
     if (mask && raw_is_zero(load_raw(mask, tmask, r1 - 1), tmask)) continue;
     T acc = sr.neutral();
-    for (int32_t c = 0; c < d.z; ++c) acc = sr.addv(acc, partials[(int64_t)(d.y + c) * C + o]);
-    sr.write(r1 - 1, acc);
+    for (int32_t c = lane; c < d.z; c += 32) acc = sr.addv(acc, partials[(int64_t)(d.y + c) * C + o]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc = sr.addv(acc, shfl_xor_m<T>(kFull, acc, off, 32));
+    if (lane == 0) sr.write(r1 - 1, acc);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// SELL plus-times Float32 over relabelled columns with the hot part of x in shared
+// memory.  After relabelling by frequency, columns 1..hot are the most gathered
+// ones (about half of the entries of an R-MAT graph fall in the first 32768); each
+// CTA stages them once and serves those gathers from shared memory, so the L1 tag
+// stage -- one distinct line per cycle, the limit of scattered gathers -- sees only
+// the cold ones.  Same work items and fold order as k_sell.
+// ---------------------------------------------------------------------------------
+static const int kHotCols = 32768;
+static const int kHotThreads = 1024;
+
+__global__ void __launch_bounds__(kHotThreads, 1)
+    k_sell_hot(const float* __restrict__ nz, const float* __restrict__ xr, float* __restrict__ y,
+               const int32_t* __restrict__ slice_ptr, const int32_t* __restrict__ colval,
+               const int32_t* __restrict__ perm, int64_t C, int64_t m,
+               const int4* __restrict__ items, int64_t nitems, float* partials, int hot) {
+  extern __shared__ float sx[];
+  for (int i = threadIdx.x; i < hot; i += blockDim.x) sx[i] = __ldg(xr + i);
+  __syncthreads();
+  const int64_t total = nitems * C;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t it = t / C, o = t - it * C;
+    const int4 d = items[it];  // slice, first column, end column, partial index
+    const int64_t srow = (int64_t)d.x * C + o;
+    if (srow >= m) continue;
+    const int64_t r1 = perm ? (int64_t)perm[srow] : srow + 1;
+    // positions fit in Int32 (n_stored < 2^31 is checked when the SELL copy is built)
+    const int32_t Ci = (int32_t)C;
+    int32_t pos = slice_ptr[d.x] - 1 + (int32_t)o + d.y * Ci;  // entry (row o, column j)
+    // Padding columns (-1) contribute +0.0, which leaves the sum unchanged (the sum
+    // starts at +0.0 and is never -0.0), so the row is folded in storage order with
+    // no early exit; column / value loads of the next 8 entries are issued before the
+    // gathers of the current 8.
+    float acc = 0.0f;
+    int32_t c[8];
+    float a[8];
+    int32_t j = d.y;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool in = j + u < d.z;
+      c[u] = in ? ld_stream(colval + pos + u * Ci) : -1;
+      a[u] = in ? ld_stream(nz + pos + u * Ci) : 0.0f;
+    }
+    while (j < d.z) {
+      const int32_t jn = j + 8;
+      const int32_t pn = pos + 8 * Ci;
+      int32_t cn[8];
+      float an[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const bool in = jn + u < d.z;
+        cn[u] = in ? ld_stream(colval + pn + u * Ci) : -1;
+        an[u] = in ? ld_stream(nz + pn + u * Ci) : 0.0f;
+      }
+      float p[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int32_t col = c[u];
+        float xv = 0.0f;
+        if (col > 0) xv = col <= hot ? sx[col - 1] : __ldg(xr + (col - 1));
+        p[u] = __fmul_rn(a[u], xv);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) acc = __fadd_rn(acc, p[u]);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        c[u] = cn[u];
+        a[u] = an[u];
+      }
+      j = jn;
+      pos = pn;
+    }
+    if (d.w < 0) __stcs(y + (r1 - 1), acc);
+    else partials[(int64_t)d.w * C + o] = acc;
   }
 }
 
@@ -770,9 +856,40 @@ static int launch_sell(gg_ctx* ctx, gg_mat* A, const SR& sr, const void* mask, i
     trace_count(ctx, 1);
   }
   if (P->nmulti > 0) {
-    k_sell_combine<SR><<<grid_for(ctx, P->nmulti * C, 256), 256, 0, ctx->stream>>>(
+    k_sell_combine<SR><<<grid_for(ctx, P->nmulti * C * 32, 256), 256, 0, ctx->stream>>>(
         sr, A->sigma > 1 ? A->perm : nullptr, C, A->m, P->multi, P->nmulti,
         static_cast<const T*>(P->partials), lo, hi, mask, tmask);
+    trace_count(ctx, 1);
+  }
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// plus-times Float32 SELL over relabelled columns (k_sell_hot + chunk combination)
+static int launch_sell_hot(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32& sr,
+                           const int32_t* colval) {
+  GG_CHECK(build_sell_plan(ctx, A));
+  SellPlan* P = A->sellplan;
+  const int64_t C = A->slice_size;
+  const int hot = (int)std::min<int64_t>(A->n, kHotCols);
+  static bool attr_set[64] = {false};
+  if (ctx->device < 64 && !attr_set[ctx->device]) {
+    GG_CUDA(cudaFuncSetAttribute(k_sell_hot, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kHotCols * (int)sizeof(float)));
+    attr_set[ctx->device] = true;
+  }
+  if (P->nitems > 0) {
+    const int tr = trace_main_begin(ctx);
+    k_sell_hot<<<ctx->num_sms, kHotThreads, hot * sizeof(float), ctx->stream>>>(
+        sr.nz, sr.x, sr.y, A->slice_ptr, colval, A->sigma > 1 ? A->perm : nullptr, C, A->m,
+        P->items, P->nitems, static_cast<float*>(P->partials), hot);
+    trace_main_end(ctx, tr);
+    trace_count(ctx, 1);
+  }
+  if (P->nmulti > 0) {
+    k_sell_combine<SRPlusTimesF32><<<grid_for(ctx, P->nmulti * C * 32, 256), 256, 0, ctx->stream>>>(
+        sr, A->sigma > 1 ? A->perm : nullptr, C, A->m, P->multi, P->nmulti,
+        static_cast<const float*>(P->partials), 0, 0, nullptr, 0);
     trace_count(ctx, 1);
   }
   GG_CUDA(cudaGetLastError());
@@ -830,6 +947,7 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
       GG_CUDA(cudaGetLastError());
       return GG_OK;
     }
+    if (A->colperm->enabled) return launch_sell_hot(ctx, A, sr, colval);
     return launch_sell(ctx, A, sr, nullptr, 0, 0, 0, colval);
   }
   switch (tc) {
