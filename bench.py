@@ -343,7 +343,7 @@ def run_spmv_rmat(args, scale=22):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "peak_kind": peak_kind, "algorithmic_bytes": B,
-                     "kernel_ms": round(kernel_ms, 5), "kernel": "k_sell (SELL-32 sigma=n copy)"},
+                     "kernel_ms": round(kernel_ms, 5), "kernel": "k_sell_hot32 (SELL-32 copy sorted by row length, relabelled columns)"},
         "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * n},
         "gpu_launches": tr.launches,
@@ -458,7 +458,13 @@ def run_search(args, kind, graph):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu:
-        lv = G.bfs_distances(A, int(src[0])) if kind != "bfs" else d0
+        if kind != "bfs":  # level count of the same search on the Bool pattern
+            P = G.SparseGPUMatrixCSR(A.m, A.n, A.rowptr, A.colval,
+                                     torch.ones(A.nnz(), dtype=torch.bool, device=device))
+            lv = G.bfs_distances(P, int(src[0]))
+            del P
+        else:
+            lv = d0
         levels_full = int(lv[lv != I32MAX].max().item()) + 1
         out["cpu_baseline"] = cpu_baseline_search(A, kind, int(src[0]), mcc, levels_full)
     if rank == 0:

@@ -206,6 +206,7 @@ static void free_mat_storage(gg_mat* A) {
     cudaFree(A->sellplan->items);
     cudaFree(A->sellplan->multi);
     cudaFree(A->sellplan->partials);
+    cudaFree(A->sellplan->pitems);
     delete A->sellplan;
     A->sellplan = nullptr;
   }

@@ -334,7 +334,15 @@ struct SellPlan {
   int4* items = nullptr;
   int4* multi = nullptr;
   void* partials = nullptr;  // [npartials * C] accumulators (8 bytes each)
+  // work items of the SELL-32 warp kernel: a chunk of a slice wider than
+  // kNarrowCols as (first entry position, first stored row, columns, partial index
+  // or -1), or a group of up to 8 consecutive narrow slices holding at most
+  // kNarrowCols columns in total as (first entry position, first stored row,
+  // -(slices), widths packed 4 bits per slice)
+  int4* pitems = nullptr;
+  int64_t npitems = 0;
 };
+static const int kNarrowCols = 8;
 static const int kSellChunk = 128;
 
 // SpMM long-row segments.  Rows (CSR) or slices (SELL) longer than kSegMM entries
@@ -456,5 +464,6 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
                   const void* x, int tx, const void* mask, int tmask, int64_t lo, int64_t hi);
 int build_row_blocks(gg_ctx* ctx, gg_mat* A);
 int build_sell_plan(gg_ctx* ctx, gg_mat* A);
+int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n);  // gg_batch.cu
 int row_stats(gg_ctx* ctx, gg_mat* A);
 }  // namespace gg

@@ -46,6 +46,7 @@ struct GraphAux {
   bool all_odd = false;  // every stored value has bit 0 set (Bool true / odd integer)
   bool nonneg = false;   // every stored value is >= 0 and not NaN
   PushCSR push[3];       // 0: odd-valued edges, 1: all edges, 2: all edges + weights
+  int64_t max_in_deg = -1;  // largest row of the view (-1: not computed yet)
 };
 
 void free_graph_aux(gg_mat* A) {
@@ -673,6 +674,134 @@ __global__ void __launch_bounds__(1024)
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Persistent cooperative levels for graphs without hubs (grids, meshes: out-degree
+// <= kCoopMaxDeg) while the frontier is medium-sized: one launch runs level after
+// level over all SMs with a grid barrier in between, instead of one launch and one
+// host round trip per level.  The barrier's wait is bounded (about 7 s): when it runs
+// out, the kernel records an error, every block returns, and the call reports
+// GG_ERR_TIMEOUT.  Queue counters rotate over three words so that the counter being
+// zeroed is never the one being read or appended.
+// ---------------------------------------------------------------------------------
+static const int kCoopMaxDeg = 64;
+static const int kCoopLo = 1024;   // the single-CTA kernel takes smaller frontiers
+static const int kCoopThreads = 1024;
+
+struct CoopCtl {
+  unsigned long long cnt[3];
+  unsigned bar[4];  // arrivals, generation, error, unused
+  long long nf_out;
+  int level_out;    // last completed level / round (relative for SSSP)
+  int which_out;    // queue holding the remaining frontier: 0 = first, 1 = second
+};
+
+__device__ __forceinline__ bool coop_grid_sync(unsigned* bar, unsigned nblocks) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vgen = bar + 1;
+    volatile unsigned* verr = bar + 2;
+    const unsigned gen = *vgen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == nblocks - 1) {
+      bar[0] = 0;
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned long long polls = 0;
+      while (*vgen == gen && *verr == 0) {
+        if (++polls > (1ull << 26)) {
+          atomicExch(bar + 2, 1u);
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *((volatile unsigned*)(bar + 2)) == 0;
+}
+
+__global__ void k_coop_init(CoopCtl* cc, long long nf0) {
+  cc->cnt[0] = 0;
+  cc->cnt[1] = 0;
+  cc->cnt[2] = (unsigned long long)nf0;
+  cc->bar[0] = cc->bar[1] = cc->bar[2] = cc->bar[3] = 0;
+  cc->nf_out = 0;
+  cc->level_out = 0;
+  cc->which_out = 0;
+}
+
+// warp-aggregated append to a queue counted by *cnt (full warp must call)
+__device__ __forceinline__ void coop_append(bool want, int32_t v, int32_t* q,
+                                            unsigned long long* cnt) {
+  const int lane = threadIdx.x & 31;
+  const unsigned b = __ballot_sync(kFullG, want);
+  if (!b) return;
+  const int leader = __ffs(b) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(cnt, (unsigned long long)__popc(b));
+  base = __shfl_sync(kFullG, base, leader);
+  if (want) q[base + __popc(b & ((1u << lane) - 1u))] = v;
+}
+
+// BFS levels, thread per frontier vertex; exits when the frontier is empty, at most
+// lo, or above hi
+__global__ void __launch_bounds__(kCoopThreads, 1)
+    k_bfs_coop(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol, int32_t* qa,
+               int32_t* qb, unsigned* visited, int32_t* dist, CoopCtl* cc, int32_t level0,
+               long long lo, long long hi) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+  int32_t* cur = qa;
+  int32_t* nxt = qb;
+  for (int st = 0;; ++st) {
+    const int r = st % 3;
+    const long long nf = (long long)*((volatile unsigned long long*)&cc->cnt[(r + 2) % 3]);
+    if (nf == 0 || nf <= lo || nf > hi) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        cc->nf_out = nf;
+        cc->level_out = level0 + st;
+        cc->which_out = st & 1;
+      }
+      return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) cc->cnt[(r + 1) % 3] = 0;
+    const int32_t level = level0 + st + 1;
+    for (int64_t i0 = gt - lane; i0 < nf; i0 += nt) {  // warp-uniform trip count
+      const int64_t i = i0 + lane;
+      int32_t k0 = 0, k1 = 0;
+      if (i < nf) {
+        const int32_t u = cur[i];
+        k0 = __ldg(prow + u);
+        k1 = __ldg(prow + u + 1);
+      }
+      int32_t dmax = k1 - k0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const int32_t t = __shfl_xor_sync(kFullG, dmax, o);
+        dmax = t > dmax ? t : dmax;
+      }
+      for (int32_t j = 0; j < dmax; ++j) {
+        bool claim = false;
+        int32_t w = 0;
+        if (k0 + j < k1) {
+          w = __ldg(pcol + k0 + j);
+          const unsigned bit = 1u << (w & 31);
+          if (!(__ldcg(visited + (w >> 5)) & bit)) claim = !(atomicOr(visited + (w >> 5), bit) & bit);
+          if (claim) dist[w] = level;
+        }
+        coop_append(claim, w, nxt, &cc->cnt[r]);
+      }
+    }
+    if (!coop_grid_sync(cc->bar, gridDim.x)) return;
+    int32_t* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+}
+
 // sum of out-degrees of a frontier queue (direction heuristic after the small kernel)
 __global__ void k_queue_degree(const int32_t* __restrict__ prow, const int32_t* __restrict__ q,
                                int64_t nf, Counters* ctr) {
@@ -697,13 +826,14 @@ struct BfsScratch {
   int32_t* q[2];
   int32_t* hq;  // deferred frontier hubs
   Counters* ctr;
+  CoopCtl* cc;
 };
 
 static int bfs_scratch(gg_ctx* ctx, int64_t n, BfsScratch* s) {
   const int64_t nw = (n + 31) / 32 + 1;
   const size_t bm = ((nw * sizeof(unsigned)) + 255) & ~(size_t)255;
   const size_t qb = (((n + 1) * sizeof(int32_t)) + 255) & ~(size_t)255;
-  GG_CHECK(ensure_scratch(ctx, 3 * bm + 3 * qb + 256));
+  GG_CHECK(ensure_scratch(ctx, 3 * bm + 3 * qb + 512));
   char* p = static_cast<char*>(ctx->scratch);
   s->visited = (unsigned*)p;
   s->fb[0] = (unsigned*)(p + bm);
@@ -712,7 +842,18 @@ static int bfs_scratch(gg_ctx* ctx, int64_t n, BfsScratch* s) {
   s->q[1] = (int32_t*)(p + 3 * bm + qb);
   s->hq = (int32_t*)(p + 3 * bm + 2 * qb);
   s->ctr = (Counters*)(p + 3 * bm + 3 * qb);
+  s->cc = (CoopCtl*)(p + 3 * bm + 3 * qb + 256);
   GG_CUDA(cudaMemsetAsync(p, 0, 3 * bm, ctx->stream));
+  return GG_OK;
+}
+
+// cooperative launch of a persistent level kernel, then its control block read back
+static int coop_launch(gg_ctx* ctx, const void* fn, void** args, CoopCtl* cc, CoopCtl* h) {
+  GG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(ctx->num_sms), dim3(kCoopThreads), args, 0,
+                                      ctx->stream));
+  GG_CUDA(cudaMemcpyAsync(h, cc, sizeof(CoopCtl), cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (h->bar[2]) return set_error(GG_ERR_TIMEOUT, "grid barrier wait ran out");
   return GG_OK;
 }
 
@@ -736,10 +877,36 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
   int cur = 0;
   bool frontier_is_bitmap = false, pull = false;
   const int64_t total_edges = P.nnz;
+  // hub-free graphs (grids, meshes) run medium frontiers in the persistent kernel
+  const bool coop_ok = P.max_deg <= kCoopMaxDeg && n >= (1 << 16);
+  const int32_t small_cap = coop_ok ? kCoopLo : kSmallCap;
+  const long long coop_hi = n / 24 > kCoopLo ? n / 24 : kCoopLo;
+  CoopCtl* hc = reinterpret_cast<CoopCtl*>(ctx->h_flags);
   while (nf > 0) {
-    if (!pull && nf <= kSmallCap) {
+    if (coop_ok && !pull && nf > small_cap && nf <= coop_hi) {
+      k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf);
+      int32_t* qa = sc.q[cur];
+      int32_t* qb = sc.q[cur ^ 1];
+      int32_t lv0 = (int32_t)level;
+      long long lo = kCoopLo / 2, hi = coop_hi;
+      void* args[] = {&P.rowptr, &P.colval, &qa, &qb, &sc.visited, &dist, &sc.cc, &lv0, &lo, &hi};
+      GG_CHECK(coop_launch(ctx, (const void*)k_bfs_coop, args, sc.cc, hc));
+      nf = hc->nf_out;
+      level = hc->level_out;
+      if (hc->which_out) cur ^= 1;
+      if (nf > 0) {
+        GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+        k_queue_degree<<<gridsz(ctx, nf), 256, 0, ctx->stream>>>(P.rowptr, sc.q[cur], nf, sc.ctr);
+        GG_CUDA(cudaMemcpyAsync(ctx->h_flags, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        GG_CUDA(cudaStreamSynchronize(ctx->stream));
+        mf = (int64_t)reinterpret_cast<Counters*>(ctx->h_flags)->mf;
+      }
+      continue;
+    }
+    if (!pull && nf <= small_cap) {
       k_bfs_small<<<1, kSmallThreads, kSmallSmem, ctx->stream>>>(
-          P.rowptr, P.colval, sc.q[cur], (int32_t)nf, (int32_t)level, kSmallCap, sc.visited, dist,
+          P.rowptr, P.colval, sc.q[cur], (int32_t)nf, (int32_t)level, small_cap, sc.visited, dist,
           sc.ctr);
       GG_CUDA(cudaGetLastError());
       GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
@@ -904,7 +1071,7 @@ __global__ void __launch_bounds__(256)
           }
         }
       }
-      warp_append(add, w, 0, qn, ctr);
+      warp_append(add, w, add ? prow[w + 1] - prow[w] : 0, qn, ctr);
     }
   }
 }
@@ -945,7 +1112,7 @@ __global__ void __launch_bounds__(256)
             }
           }
         }
-        warp_append(add, w, 0, qn, ctr);
+        warp_append(add, w, add ? prow[w + 1] - prow[w] : 0, qn, ctr);
       }
     }
   }
@@ -1118,6 +1285,190 @@ __global__ void k_changed_copy(int64_t n, const T* next, T* dist, unsigned* flag
   if (ch) atomicOr(flag, 1u);
 }
 
+// Bellman-Ford rounds (push, atomic min, membership bitmaps), thread per frontier vertex
+template <typename T>
+__global__ void __launch_bounds__(kCoopThreads, 1)
+    k_sssp_coop(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+                const T* __restrict__ pw, int32_t* qa, int32_t* qb, T* dist, unsigned* inq_a,
+                unsigned* inq_b, CoopCtl* cc, long long lo, long long hi, long long max_rounds) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+  int32_t* cur = qa;
+  int32_t* nxt = qb;
+  unsigned* icur = inq_a;
+  unsigned* inxt = inq_b;
+  for (int st = 0;; ++st) {
+    const int r = st % 3;
+    const long long nf = (long long)*((volatile unsigned long long*)&cc->cnt[(r + 2) % 3]);
+    if (nf == 0 || nf <= lo || nf > hi || st >= max_rounds) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        cc->nf_out = nf;
+        cc->level_out = st;
+        cc->which_out = st & 1;
+      }
+      return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) cc->cnt[(r + 1) % 3] = 0;
+    for (int64_t i0 = gt - lane; i0 < nf; i0 += nt) {
+      const int64_t i = i0 + lane;
+      int32_t k0 = 0, k1 = 0;
+      T du = T(0);
+      if (i < nf) {
+        const int32_t u = cur[i];
+        atomicAnd(icur + (u >> 5), ~(1u << (u & 31)));
+        k0 = __ldg(prow + u);
+        k1 = __ldg(prow + u + 1);
+        du = ld_cg(dist + u);
+      }
+      int32_t dmax = k1 - k0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const int32_t t = __shfl_xor_sync(kFullG, dmax, o);
+        dmax = t > dmax ? t : dmax;
+      }
+      for (int32_t j = 0; j < dmax; ++j) {
+        bool add = false;
+        int32_t w = 0;
+        if (k0 + j < k1) {
+          w = __ldg(pcol + k0 + j);
+          const T cand = relax_add(__ldg(pw + k0 + j), du);
+          if (cand < ld_cg(dist + w)) {
+            const T old = atomic_min_t(dist + w, cand);
+            if (cand < old) {
+              const unsigned bit = 1u << (w & 31);
+              add = !(atomicOr(inxt + (w >> 5), bit) & bit);
+            }
+          }
+        }
+        coop_append(add, w, nxt, &cc->cnt[r]);
+      }
+    }
+    if (!coop_grid_sync(cc->bar, gridDim.x)) return;
+    int32_t* t = cur;
+    cur = nxt;
+    nxt = t;
+    unsigned* tb = icur;
+    icur = inxt;
+    inxt = tb;
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// pull rounds for large frontiers: every vertex takes the minimum over its in-edges
+// from vertices that changed in the previous round (membership bitmap chg), in place.
+// Only v's own lane writes dist[v], so no atomics; the new membership bitmap is
+// written word by word from a ballot.  Rows with more than kHubDegB in-edges are
+// skipped and relaxed in pieces with atomic min by k_sssp_pull_hub.
+// ---------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T view_weight(const void* nz, int tv, int64_t k) {
+  switch (tv) {
+    case GG_BOOL: return static_cast<T>(static_cast<const uint8_t*>(nz)[k]);
+    case GG_INT32: return static_cast<T>(static_cast<const int32_t*>(nz)[k]);
+    case GG_INT64: return static_cast<T>(static_cast<const int64_t*>(nz)[k]);
+    case GG_FLOAT32: return static_cast<T>(static_cast<const float*>(nz)[k]);
+  }
+  return static_cast<T>(static_cast<const double*>(nz)[k]);
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_min_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const T t = __shfl_xor_sync(kFullG, v, o);
+    v = t < v ? t : v;
+  }
+  return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_sssp_pull(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cv,
+                const void* nz, int tv, const unsigned* __restrict__ chg, T* dist,
+                unsigned* chg_next, int32_t* qn, Counters* ctr, const int32_t* __restrict__ prow) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int64_t v = base + threadIdx.x;
+    int64_t k0 = 0, k1 = 0;
+    if (v < n) {
+      k0 = (int64_t)rp[v] - 1;
+      k1 = (int64_t)rp[v + 1] - 1;
+    }
+    const bool hub = k1 - k0 > kHubDegB;  // relaxed by k_sssp_pull_hub
+    T best = Lim<T>::max();
+    if (v < n && !hub && k1 - k0 <= 32) {
+      for (int64_t k = k0; k < k1; ++k) {
+        const int32_t u = __ldg(cv + k) - 1;
+        if (bit_of(chg, u)) {
+          const T c = relax_add(view_weight<T>(nz, tv, k), ld_cg(dist + u));
+          best = c < best ? c : best;
+        }
+      }
+    }
+    // vertices with 33..kPushHub in-edges: the whole warp scans each
+    unsigned coop = __ballot_sync(kFullG, v < n && !hub && k1 - k0 > 32);
+    while (coop) {
+      const int h = __ffs(coop) - 1;
+      coop &= coop - 1;
+      const int64_t h0 = __shfl_sync(kFullG, k0, h), h1 = __shfl_sync(kFullG, k1, h);
+      T b = Lim<T>::max();
+      for (int64_t k = h0 + lane; k < h1; k += 32) {
+        const int32_t u = __ldg(cv + k) - 1;
+        if (bit_of(chg, u)) {
+          const T c = relax_add(view_weight<T>(nz, tv, k), ld_cg(dist + u));
+          b = c < b ? c : b;
+        }
+      }
+      b = warp_min_t(b);
+      if (lane == h) best = b;
+    }
+    bool changed = false;
+    if (v < n && !hub && best < dist[v]) {
+      dist[v] = best;
+      changed = true;
+    }
+    const unsigned word = __ballot_sync(kFullG, changed);
+    if (lane == 0 && base + threadIdx.x - lane < n) chg_next[v >> 5] = word;
+    warp_append(changed, (int32_t)v, changed ? prow[v + 1] - prow[v] : 0, qn, ctr);
+  }
+}
+
+// hub rows of the pull round: one warp per piece of the matrix's hub plan (rows of
+// more than kHubDegB entries cut into kHubPieceB), atomic min into the hub
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_sssp_pull_hub(const int32_t* __restrict__ cv, const void* nz, int tv,
+                    const unsigned* __restrict__ chg, T* dist, unsigned* chg_next, int32_t* qn,
+                    Counters* ctr, const int32_t* __restrict__ prow,
+                    const int4* __restrict__ pieces, int64_t npiece,
+                    const int32_t* __restrict__ hubs) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < npiece;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int4 pc = pieces[i];  // hub index, first entry, end entry (0-based)
+    const int32_t v = hubs[pc.x];
+    T b = Lim<T>::max();
+    for (int64_t k = pc.y + lane; k < pc.z; k += 32) {
+      const int32_t u = __ldg(cv + k) - 1;
+      if (bit_of(chg, u)) {
+        const T c = relax_add(view_weight<T>(nz, tv, k), ld_cg(dist + u));
+        b = c < b ? c : b;
+      }
+    }
+    b = warp_min_t(b);
+    if (lane == 0 && b < ld_cg(dist + v) && b < atomic_min_t(dist + v, b)) {
+      const unsigned bit = 1u << (v & 31);
+      if (!(atomicOr(chg_next + (v >> 5), bit) & bit)) {
+        const unsigned long long pos = atomicAdd(&ctr->nf, 1ull);
+        atomicAdd(&ctr->mf, (unsigned long long)(prow[v + 1] - prow[v]));
+        qn[pos] = v;
+      }
+    }
+  }
+}
+
 template <typename T>
 static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
   GG_CHECK(ensure_push(ctx, A, 2));
@@ -1134,15 +1485,56 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
   GG_CUDA(cudaGetLastError());
   GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
-  int64_t nf = (int64_t)h->nf, rounds = 0;
+  int64_t nf = (int64_t)h->nf, rounds = 0, mf = 0;
   int cur = 0;
   const int64_t max_rounds = n + 1;  // Bellman-Ford bound for non-negative weights
+  if (g->max_in_deg < 0) {
+    GG_CUDA(cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned), ctx->stream));
+    k_max_deg<<<gridsz(ctx, n), 256, 0, ctx->stream>>>(n, g->vrowptr, ctx->d_flags);
+    GG_CUDA(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    g->max_in_deg = ctx->h_flags[0];
+  }
+  // rows with more than kHubDegB in-edges: relaxed in pieces during pull rounds
+  const HubPlan* hp = nullptr;
+  if (g->max_in_deg > kHubDegB) {
+    GG_CHECK(build_hub_plan(ctx, A, g->vrowptr, n));
+    hp = A->hubplan;
+  }
+  const bool coop_ok = P.max_deg <= kCoopMaxDeg && n >= (1 << 16);
+  const int32_t small_cap = coop_ok ? kCoopLo : kSmallCap;
+  const long long coop_hi = n / 8 > kCoopLo ? n / 8 : kCoopLo;
   while (nf > 0) {
     if (rounds > max_rounds) return set_error(GG_ERR_NOT_CONVERGED, "shortest_path did not converge");
-    if (nf <= kSmallCap) {
+    if (coop_ok && nf > small_cap && nf <= coop_hi && mf * 8 <= P.nnz) {
+      k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf);
+      int32_t* qa = sc.q[cur];
+      int32_t* qb = sc.q[cur ^ 1];
+      unsigned* ia = sc.fb[cur];
+      unsigned* ib = sc.fb[cur ^ 1];
+      const T* pw = static_cast<const T*>(P.w);
+      long long lo = kCoopLo / 2, hi = coop_hi, mr = max_rounds - rounds + 1;
+      void* args[] = {&P.rowptr, &P.colval, &pw, &qa, &qb, &d, &ia, &ib, &sc.cc, &lo, &hi, &mr};
+      CoopCtl* hc = reinterpret_cast<CoopCtl*>(ctx->h_flags);
+      GG_CHECK(coop_launch(ctx, (const void*)k_sssp_coop<T>, args, sc.cc, hc));
+      nf = hc->nf_out;
+      rounds += hc->level_out;
+      if (hc->which_out) cur ^= 1;
+      mf = 0;
+      if (nf > 0) {
+        GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+        k_queue_degree<<<gridsz(ctx, nf), 256, 0, ctx->stream>>>(P.rowptr, sc.q[cur], nf, sc.ctr);
+        GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+        GG_CUDA(cudaStreamSynchronize(ctx->stream));
+        mf = (int64_t)h->mf;
+      }
+      continue;
+    }
+    if (nf <= small_cap) {
       GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
       k_sssp_small<T><<<1, kSmallThreads, kSmallSmem, ctx->stream>>>(
-          P.rowptr, P.colval, static_cast<const T*>(P.w), sc.q[cur], (int32_t)nf, kSmallCap, d,
+          P.rowptr, P.colval, static_cast<const T*>(P.w), sc.q[cur], (int32_t)nf, small_cap, d,
           sc.fb[cur], sc.fb[cur ^ 1], sc.ctr, max_rounds - rounds);
       GG_CUDA(cudaGetLastError());
       GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1156,10 +1548,37 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
         GG_CUDA(cudaMemcpyAsync(sc.q[cur], sc.q[cur ^ 1], nf * sizeof(int32_t),
                                 cudaMemcpyDeviceToDevice, ctx->stream));
       }
+      mf = 0;
+      if (nf > 0) {  // out-edges of the remaining frontier, for the direction choice
+        GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+        k_queue_degree<<<gridsz(ctx, nf), 256, 0, ctx->stream>>>(P.rowptr, sc.q[cur], nf, sc.ctr);
+        GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+        GG_CUDA(cudaStreamSynchronize(ctx->stream));
+        mf = (int64_t)h->mf;
+      }
       continue;
     }
     ++rounds;
     GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+    if (mf * 4 > P.nnz) {
+      // large frontier: pull round (no atomics on the common path)
+      k_sssp_pull<T><<<gridsz(ctx, n), 256, 0, ctx->stream>>>(
+          n, g->vrowptr, g->vcolval, g->vnz, A->dtype, sc.fb[cur], d, sc.fb[cur ^ 1], sc.q[cur ^ 1],
+          sc.ctr, P.rowptr);
+      if (hp && hp->npiece > 0)
+        k_sssp_pull_hub<T><<<gridsz(ctx, hp->npiece * 32), 256, 0, ctx->stream>>>(
+            g->vcolval, g->vnz, A->dtype, sc.fb[cur], d, sc.fb[cur ^ 1], sc.q[cur ^ 1], sc.ctr,
+            P.rowptr, hp->pieces, hp->npiece, hp->hubs);
+      // the consumed membership bitmap becomes the next round's target: clear it
+      GG_CUDA(cudaMemsetAsync(sc.fb[cur], 0, ((n + 31) / 32) * sizeof(unsigned), ctx->stream));
+      GG_CUDA(cudaGetLastError());
+      GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+      GG_CUDA(cudaStreamSynchronize(ctx->stream));
+      nf = (int64_t)h->nf;
+      mf = (int64_t)h->mf;
+      cur ^= 1;
+      continue;
+    }
     const bool hubs = P.max_deg > kPushHub;
     k_sssp_push<T><<<gridsz(ctx, nf * 32), 256, 0, ctx->stream>>>(
         P.rowptr, P.colval, static_cast<const T*>(P.w), sc.q[cur], nf, d, sc.fb[cur],
@@ -1172,6 +1591,7 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
     GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
     GG_CUDA(cudaStreamSynchronize(ctx->stream));
     nf = (int64_t)h->nf;
+    mf = (int64_t)h->mf;
     cur ^= 1;
   }
   if (rounds_out) *rounds_out += rounds;

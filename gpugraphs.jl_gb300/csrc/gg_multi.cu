@@ -33,7 +33,7 @@ struct gg_multigraph {
   int dtype = GG_FLOAT32;
   int64_t* row_off = nullptr;  // [G+1] global vertex offsets (0-based)
   int64_t* rp64 = nullptr;     // [total_n+1] global 0-based entry offsets of each row
-  int32_t* colval = nullptr;   // [total_nnz] per-graph 1-based columns
+  int32_t* colval = nullptr;   // [total_nnz] global 0-based column (vertex) ids
   void* nzval = nullptr;       // [total_nnz]
   std::vector<int64_t> h_row_off;
   bool all_odd = true;
@@ -66,20 +66,18 @@ __device__ __forceinline__ int graph_of(const int64_t* __restrict__ off, int64_t
   return (int)lo;
 }
 
-// 8 lanes per row over all graphs' rows
+// 8 lanes per row over all graphs' rows (global column ids: no per-row graph lookup)
 __global__ void __launch_bounds__(256)
-    k_mg_spmv(int64_t total_n, const int64_t* __restrict__ row_off, int64_t G,
-              const int64_t* __restrict__ rp, const int32_t* __restrict__ colval,
+    k_mg_spmv(int64_t total_n, const int64_t* __restrict__ rp, const int32_t* __restrict__ colval,
               const float* __restrict__ nz, const float* __restrict__ x, float* __restrict__ y) {
   const int sub = threadIdx.x & 7;
   const unsigned gm = 0xffu << ((threadIdx.x & 31) & ~7);
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3; r < total_n;
        r += ((int64_t)gridDim.x * blockDim.x) >> 3) {
-    const int g = graph_of(row_off, G, r);
-    const float* xg = x + row_off[g] - 1;  // columns are 1-based within the graph
     float acc = 0.0f;
-    for (int64_t k = rp[r] + sub; k < rp[r + 1]; k += 8)
-      acc = __fadd_rn(acc, __fmul_rn(ld_stream(nz + k), __ldg(xg + ld_stream(colval + k))));
+    const int64_t k1 = rp[r + 1];
+    for (int64_t k = rp[r] + sub; k < k1; k += 8)
+      acc = __fadd_rn(acc, __fmul_rn(ld_stream(nz + k), __ldg(x + ld_stream(colval + k))));
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(gm, acc, o, 8));
     if (sub == 0) y[r] = acc;
@@ -162,15 +160,13 @@ __global__ void __launch_bounds__(256)
     if (blockIdx.x == 0 && threadIdx.x == 0) ctr[(r + 1) % 3] = 0;
     for (int64_t i = gw; i < nf; i += nw) {
       const int64_t v = cur[i];
-      const int g = graph_of(row_off, G, v);
-      const int64_t base = row_off[g] - 1;  // global id of column 1 of graph g
       const int64_t k0 = rp[v], k1 = rp[v + 1];
       for (int64_t kb = k0; kb < k1; kb += 32) {
         const int64_t k = kb + lane;
         bool claim = false;
         int64_t w = 0;
         if (k < k1 && (!odd_only || mg_odd(nz, tv, k))) {
-          w = base + __ldg(colval + k);
+          w = __ldg(colval + k);
           const unsigned bit = 1u << (w & 31);
           if (!(__ldcg(visited + (w >> 5)) & bit))
             claim = !(atomicOr(visited + (w >> 5), bit) & bit);
@@ -273,15 +269,13 @@ __global__ void __launch_bounds__(256)
       const int64_t u = cur[i];
       if (lane == 0) atomicAnd(icur + (u >> 5), ~(1u << (u & 31)));
       const T du = __ldcg(dist + u);
-      const int g = graph_of(row_off, G, u);
-      const int64_t base = row_off[g] - 1;
       const int64_t k0 = rp[u], k1 = rp[u + 1];
       for (int64_t kb = k0; kb < k1; kb += 32) {
         const int64_t k = kb + lane;
         bool add = false;
         int64_t v = 0;
         if (k < k1) {
-          v = base + __ldg(colval + k);
+          v = __ldg(colval + k);
           const T w = mg_weight<T>(nz, tv, k);
           const T cand = (w == Lim<T>::max() || du == Lim<T>::max()) ? Lim<T>::max() : w_add(w, du);
           if (cand < __ldcg(dist + v)) {
@@ -331,6 +325,13 @@ __global__ void k_mg_fill(int32_t* d, int64_t n, int32_t v) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     d[i] = v;
+}
+
+// global 0-based column ids: colval_g (1-based within graph g) + row_off[g] - 1
+__global__ void k_mg_cols(int64_t nnz, const int32_t* __restrict__ cv, int32_t base, int32_t* out) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
+       k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = cv[k] - 1 + base;
 }
 
 // global entry offsets of each row: rp64[row_off[g] + v] = nnz_off[g] + rowptr_g[v] - 1
@@ -389,9 +390,11 @@ int gg_multigraph_create(gg_ctx* ctx, const gg_mat* const* graphs, int64_t ngrap
     k_mg_rp<<<mg_grid(ctx->num_sms, A->m + 1), 256, 0, ctx->stream>>>(A->m, A->rowptr, off[g], noff[g],
                                                                        M->rp64);
     e = cudaGetLastError();
-    if (e == cudaSuccess && A->nnz > 0)
-      e = cudaMemcpyAsync(M->colval + noff[g], A->colval, A->nnz * sizeof(int32_t),
-                          cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e == cudaSuccess && A->nnz > 0) {
+      k_mg_cols<<<mg_grid(ctx->num_sms, A->nnz), 256, 0, ctx->stream>>>(A->nnz, A->colval,
+                                                                        (int32_t)off[g], M->colval + noff[g]);
+      e = cudaGetLastError();
+    }
     if (e == cudaSuccess && A->nnz > 0)
       e = cudaMemcpyAsync(static_cast<char*>(M->nzval) + noff[g] * esz, A->nzval, A->nnz * esz,
                           cudaMemcpyDeviceToDevice, ctx->stream);
@@ -454,8 +457,7 @@ int gg_multigraph_spmv(gg_ctx* ctx, const gg_multigraph* M, const float* x, floa
   if (M->dtype != GG_FLOAT32) return set_error(GG_ERR_TYPE, "multigraph SpMV needs Float32 values");
   GG_CUDA(cudaSetDevice(ctx->device));
   k_mg_spmv<<<mg_grid(ctx->num_sms, M->total_n * 8), 256, 0, ctx->stream>>>(
-      M->total_n, M->row_off, M->ngraphs, M->rp64, M->colval, static_cast<const float*>(M->nzval),
-      x, y);
+      M->total_n, M->rp64, M->colval, static_cast<const float*>(M->nzval), x, y);
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }

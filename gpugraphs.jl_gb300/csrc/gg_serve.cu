@@ -192,8 +192,20 @@ struct gg_server {
   int error = GG_OK;
   std::string error_msg;
   std::thread worker;
+  // solo workers: a request that finds its executor idle runs alone through the
+  // single-query engine on a worker's own context and stream
+  struct SoloJob {
+    gg::Request req;
+  };
+  std::vector<std::thread> solo_threads;
+  std::vector<gg_ctx*> solo_ctx;
+  std::deque<SoloJob> solo_q;
+  std::condition_variable solo_cv;
+  int solo_idle = 0;
+  std::vector<std::vector<char>> solo_active;  // [graph][kind], scheduler-owned
+  std::vector<std::pair<int, int>> solo_finished;  // (graph, kind) released by workers
   // statistics
-  int64_t ticks = 0, admission_waits = 0;
+  int64_t ticks = 0, admission_waits = 0, solo_runs = 0;
 };
 
 namespace gg {
@@ -505,6 +517,71 @@ static int exec_retire(gg_server* S, int gi, Executor& E, std::vector<Request>& 
   return GG_OK;
 }
 
+static const int kSoloWorkers = 4;
+
+// one request through the single-query engines (the plain per-query path); SpMV
+// iterations use the one-column SpMM so that they fold exactly like an executor slot
+static int solo_run(gg_server* S, gg_ctx* c, const Request& r) {
+  gg_mat* A = S->graphs[r.graph];
+  const int64_t n = A->m;
+  if (r.kind == GG_QUERY_BFS)
+    return gg_bfs_levels(c, A, r.source, static_cast<int32_t*>(r.out), n, nullptr);
+  if (r.kind == GG_QUERY_SSSP) {
+    const int dt = A->dtype == GG_BOOL ? GG_INT32 : A->dtype;
+    const int64_t src = r.source;
+    return gg_sssp(c, A, &src, 1, r.out, nullptr, dt, n, nullptr);
+  }
+  float* tmp = nullptr;
+  GG_CUDA(cudaMallocAsync((void**)&tmp, (size_t)n * sizeof(float), c->stream));
+  float* out = static_cast<float*>(r.out);
+  const float* src = r.x;
+  float* dst = (r.steps % 2 == 1) ? out : tmp;  // the last step lands in out
+  int rc = GG_OK;
+  for (int st = 0; st < r.steps && rc == GG_OK; ++st) {
+    rc = spmm_dispatch(c, A, GG_FLOAT32, GG_OP_MUL, GG_OP_ADD, GG_OP_SECOND, dst, GG_FLOAT32, 1,
+                       src, GG_FLOAT32, 1, 1, GG_ROW_MAJOR, nullptr, 0, 0, 0);
+    src = dst;
+    dst = (dst == out) ? tmp : out;
+  }
+  cudaFreeAsync(tmp, c->stream);
+  if (rc == GG_OK) GG_CUDA(cudaStreamSynchronize(c->stream));
+  return rc;
+}
+
+static void solo_loop(gg_server* S, int w) {
+  gg_ctx* c = S->solo_ctx[w];
+  cudaSetDevice(c->device);
+  for (;;) {
+    gg_server::SoloJob job;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->solo_cv.wait(lk, [&] { return S->stop || !S->solo_q.empty(); });
+      if (S->stop) return;
+      job = S->solo_q.front();
+      S->solo_q.pop_front();
+    }
+    const int rc = solo_run(S, c, job.req);
+    const double t = now_s();
+    std::string msg = rc ? gg_last_error() : "";
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->solo_finished.emplace_back(job.req.graph, job.req.kind - 1);
+      ++S->solo_idle;
+      if (rc != GG_OK) {
+        S->error = rc;
+        S->error_msg = msg;
+        S->stop = true;
+      } else {
+        S->done_ids.push_back(job.req.id);
+        S->done_lat.push_back(t - job.req.t_submit);
+        --S->inflight;
+        ++S->solo_runs;
+      }
+    }
+    S->cv.notify_one();
+  }
+}
+
 static void server_loop(gg_server* S) {
   cudaSetDevice(S->own.device);
   // waiting requests per (graph, kind)
@@ -526,6 +603,24 @@ static void server_loop(gg_server* S) {
         S->queue.pop_front();
         waiting[r.graph][r.kind - 1].push_back(r);
       }
+      for (auto& f : S->solo_finished) S->solo_active[f.first][f.second] = 0;
+      S->solo_finished.clear();
+      // a lone request whose executor is idle runs on a solo worker (no batching
+      // needed: the single-query engine is the fastest path for one query)
+      for (size_t gi = 0; gi < S->graphs.size() && S->solo_idle > 0; ++gi)
+        for (int kk = 0; kk < 3 && S->solo_idle > 0; ++kk) {
+          Executor& E = S->exec[gi][kk];
+          const bool idle = !E.ready || (E.active() == 0 && !E.inflight && E.finishing.empty());
+          if (waiting[gi][kk].size() == 1 && idle && !S->solo_active[gi][kk]) {
+            gg_server::SoloJob job;
+            job.req = waiting[gi][kk].front();
+            waiting[gi][kk].clear();
+            S->solo_active[gi][kk] = 1;
+            --S->solo_idle;
+            S->solo_q.push_back(job);
+            S->solo_cv.notify_one();
+          }
+        }
     }
     int rc = GG_OK;
     bool progress = false;
@@ -622,6 +717,20 @@ int gg_server_create(gg_ctx* ctx, int64_t reserve_bytes, gg_server** out) {
     delete S;
     return cuda_error(e, "gg_server_create");
   }
+  for (int w = 0; w < kSoloWorkers; ++w) {
+    gg_ctx* c = nullptr;
+    int rc = gg_init(ctx->device, &c);
+    cudaStream_t st = nullptr;
+    if (rc == GG_OK && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+      rc = set_error(GG_ERR_CUDA, "solo worker stream");
+    if (rc == GG_OK) rc = gg_set_stream(c, st);
+    if (rc != GG_OK) {
+      if (c) gg_destroy(c);
+      if (st) cudaStreamDestroy(st);
+      break;  // fewer solo workers; batching alone still serves every request
+    }
+    S->solo_ctx.push_back(c);
+  }
   *out = S;
   return GG_OK;
 }
@@ -638,6 +747,30 @@ int gg_server_add_graph(gg_server* S, const gg_mat* A_T, int* graph_id) {
   g.g.odd_only = !all_odd;
   g.nonneg = nonneg;
   g.n = A->m;
+  // Build every per-matrix analysis the executors and the solo engines use now, so
+  // that later concurrent calls on this matrix only read it.
+  {
+    const int64_t n = A->m;
+    void* tmp = nullptr;
+    GG_CUDA(cudaMalloc(&tmp, (size_t)(n > 0 ? n : 1) * 16));
+    int rc = build_hub_plan(&S->own, A, g.g.rowptr, n);
+    if (rc == GG_OK && !dtype_is_float(A->dtype) && n > 0)
+      rc = gg_bfs_levels(&S->own, A, 1, static_cast<int32_t*>(tmp), n, nullptr);
+    if (rc == GG_OK && nonneg && n > 0) {
+      const int64_t one = 1;
+      rc = gg_sssp(&S->own, A, &one, 1, tmp, nullptr, A->dtype == GG_BOOL ? GG_INT32 : A->dtype, n,
+                   nullptr);
+    }
+    if (rc == GG_OK && A->dtype == GG_FLOAT32 && n > 0) {
+      float* xb = static_cast<float*>(tmp);
+      cudaMemsetAsync(xb, 0, (size_t)n * 4, S->stream);
+      rc = spmm_dispatch(&S->own, A, GG_FLOAT32, GG_OP_MUL, GG_OP_ADD, GG_OP_SECOND, xb + n,
+                         GG_FLOAT32, 1, xb, GG_FLOAT32, 1, 1, GG_ROW_MAJOR, nullptr, 0, 0, 0);
+    }
+    cudaStreamSynchronize(S->stream);
+    cudaFree(tmp);
+    if (rc != GG_OK) return rc;
+  }
   S->graphs.push_back(A);
   S->views.push_back(g);
   S->exec.emplace_back(3);
@@ -679,7 +812,12 @@ int gg_server_submit(gg_server* S, int kind, int graph, int64_t source, const fl
     S->queue.push_back(r);
     ++S->inflight;
     if (request_id) *request_id = r.id;
-    if (!S->worker.joinable()) S->worker = std::thread(server_loop, S);
+    if (!S->worker.joinable()) {
+      S->solo_active.assign(S->graphs.size(), std::vector<char>(3, 0));
+      for (int w = 0; w < (int)S->solo_ctx.size(); ++w) S->solo_threads.emplace_back(solo_loop, S, w);
+      S->solo_idle = (int)S->solo_ctx.size();
+      S->worker = std::thread(server_loop, S);
+    }
   }
   S->cv.notify_one();
   return GG_OK;
@@ -723,7 +861,15 @@ int gg_server_destroy(gg_server* S) {
     S->stop = true;
   }
   S->cv.notify_one();
+  S->solo_cv.notify_all();
   if (S->worker.joinable()) S->worker.join();
+  for (auto& t : S->solo_threads)
+    if (t.joinable()) t.join();
+  for (gg_ctx* c : S->solo_ctx) {
+    cudaStream_t st = c->stream;
+    gg_destroy(c);
+    if (st) cudaStreamDestroy(st);
+  }
   cudaSetDevice(S->own.device);
   cudaStreamSynchronize(S->stream);
   for (auto& per_g : S->exec)

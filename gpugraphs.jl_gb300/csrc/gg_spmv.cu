@@ -538,12 +538,33 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
   GG_CUDA(cudaMemcpyAsync(sp.data(), A->slice_ptr, (ns + 1) * sizeof(int32_t),
                           cudaMemcpyDeviceToHost, ctx->stream));
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
-  std::vector<int4> items, multi;
+  std::vector<int4> items, multi, pitems;
   int32_t np = 0;
+  // narrow-slice groups of the warp kernel (C == 32 only)
+  int64_t g_first = -1, g_cols = 0, g_count = 0;
+  uint32_t g_widths = 0;
+  auto flush_group = [&]() {
+    if (g_count > 0)
+      pitems.push_back(make_int4(sp[g_first] - 1, (int)(g_first * C), -(int)g_count, (int)g_widths));
+    g_first = -1;
+    g_cols = 0;
+    g_count = 0;
+    g_widths = 0;
+  };
   for (int64_t s = 0; s < ns; ++s) {
     const int64_t L = C > 0 ? ((int64_t)sp[s + 1] - sp[s]) / C : 0;
+    if (C == 32 && L <= kNarrowCols) {
+      if (g_count == 8 || g_cols + L > kNarrowCols) flush_group();
+      if (g_count == 0) g_first = s;
+      g_widths |= (uint32_t)L << (4 * g_count);
+      g_cols += L;
+      ++g_count;
+    } else {
+      flush_group();
+    }
     if (L <= kSellChunk) {
       items.push_back(make_int4((int)s, 0, (int)L, -1));
+      if (!(C == 32 && L <= kNarrowCols)) pitems.push_back(make_int4(sp[s] - 1, (int)(s * C), (int)L, -1));
       continue;
     }
     const int32_t nch = (int32_t)((L + kSellChunk - 1) / kSellChunk);
@@ -552,15 +573,22 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
       const int64_t jb = (int64_t)c * kSellChunk;
       const int64_t je = jb + kSellChunk < L ? jb + kSellChunk : L;
       items.push_back(make_int4((int)s, (int)jb, (int)je, np + c));
+      pitems.push_back(make_int4((int)(sp[s] - 1 + jb * C), (int)(s * C), (int)(je - jb), np + c));
     }
     np += nch;
   }
+  flush_group();
   SellPlan* P = new SellPlan();
+  P->npitems = (int64_t)pitems.size();
   P->nitems = (int64_t)items.size();
   P->nmulti = (int64_t)multi.size();
   cudaError_t e = cudaMalloc((void**)&P->items, (items.size() + 1) * sizeof(int4));
   if (e == cudaSuccess) e = cudaMalloc((void**)&P->multi, (multi.size() + 1) * sizeof(int4));
   if (e == cudaSuccess) e = cudaMalloc(&P->partials, ((int64_t)np * C + 1) * 8);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&P->pitems, (pitems.size() + 1) * sizeof(int4));
+  if (e == cudaSuccess && !pitems.empty())
+    e = cudaMemcpyAsync(P->pitems, pitems.data(), pitems.size() * sizeof(int4),
+                        cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess && !items.empty())
     e = cudaMemcpyAsync(P->items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice,
                         ctx->stream);
@@ -572,6 +600,7 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
     cudaFree(P->items);
     cudaFree(P->multi);
     cudaFree(P->partials);
+    cudaFree(P->pitems);
     delete P;
     return cuda_error(e, "SELL analysis");
   }
@@ -865,6 +894,111 @@ static int launch_sell(gg_ctx* ctx, gg_mat* A, const SR& sr, const void* mask, i
   return GG_OK;
 }
 
+// SELL-32 variant: one warp per work item (lane = row of the slice), with the item's
+// first position, first stored row, width and partial slot precomputed, and the next
+// item's descriptor loaded while the current one runs -- rows of one or two entries
+// (most rows of a power-law graph) no longer pay a chain of dependent descriptor
+// loads before their first column load.
+__global__ void __launch_bounds__(kHotThreads, 1)
+    k_sell_hot32(const float* __restrict__ nz, const float* __restrict__ xr, float* __restrict__ y,
+                 const int32_t* __restrict__ colval, const int32_t* __restrict__ perm, int64_t m,
+                 const int4* __restrict__ pitems, int64_t nitems, float* partials, int hot) {
+  extern __shared__ float sx[];
+  for (int i = threadIdx.x; i < hot; i += blockDim.x) sx[i] = __ldg(xr + i);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int4 dn = gw < nitems ? __ldg(pitems + gw) : make_int4(0, 0, 0, -1);
+  for (int64_t it = gw; it < nitems; it += nw) {
+    const int4 d = dn;  // first position, first stored row, columns, partial
+    if (it + nw < nitems) dn = __ldg(pitems + it + nw);
+    if (d.z < 0) {
+      // group of -d.z narrow slices (widths in 4-bit fields of d.w), <= 8 columns in
+      // all: load every entry at once, then fold slice by slice in column order
+      const int ns = -d.z;
+      const uint32_t widths = (uint32_t)d.w;
+      int total = 0;
+      for (int t = 0; t < ns; ++t) total += (widths >> (4 * t)) & 15u;
+      int32_t c[kNarrowCols];
+      float a[kNarrowCols];
+#pragma unroll
+      for (int u = 0; u < kNarrowCols; ++u) {
+        const bool in = u < total;
+        c[u] = in ? ld_stream(colval + d.x + u * 32 + lane) : -1;
+        a[u] = in ? ld_stream(nz + d.x + u * 32 + lane) : 0.0f;
+      }
+      float p[kNarrowCols];
+#pragma unroll
+      for (int u = 0; u < kNarrowCols; ++u) {
+        const int32_t col = c[u];
+        float xv = 0.0f;
+        if (col > 0) xv = col <= hot ? sx[col - 1] : __ldg(xr + (col - 1));
+        p[u] = __fmul_rn(a[u], xv);
+      }
+      int u0 = 0;
+      for (int t = 0; t < ns; ++t) {
+        const int w = (int)((widths >> (4 * t)) & 15u);
+        float acc = 0.0f;
+#pragma unroll
+        for (int u = 0; u < kNarrowCols; ++u)
+          if (u >= u0 && u < u0 + w) acc = __fadd_rn(acc, p[u]);
+        u0 += w;
+        const int64_t srow = (int64_t)d.y + t * 32 + lane;
+        if (srow < m) {
+          const int32_t r1 = perm ? __ldg(perm + srow) : (int32_t)(srow + 1);
+          __stcs(y + (r1 - 1), acc);
+        }
+      }
+      continue;
+    }
+    const int64_t srow = (int64_t)d.y + lane;
+    const bool live = srow < m;
+    const int32_t r1 = (live && perm) ? __ldg(perm + srow) : (int32_t)(srow + 1);
+    int32_t pos = d.x + lane;
+    // padding columns (-1) add +0.0: storage-order fold without an early exit
+    float acc = 0.0f;
+    int32_t c[8];
+    float a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool in = live && u < d.z;
+      c[u] = in ? ld_stream(colval + pos + u * 32) : -1;
+      a[u] = in ? ld_stream(nz + pos + u * 32) : 0.0f;
+    }
+    for (int32_t j = 0; j < d.z; j += 8) {
+      const int32_t pn = pos + 8 * 32;
+      int32_t cn[8];
+      float an[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const bool in = live && j + 8 + u < d.z;
+        cn[u] = in ? ld_stream(colval + pn + u * 32) : -1;
+        an[u] = in ? ld_stream(nz + pn + u * 32) : 0.0f;
+      }
+      float p[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int32_t col = c[u];
+        float xv = 0.0f;
+        if (col > 0) xv = col <= hot ? sx[col - 1] : __ldg(xr + (col - 1));
+        p[u] = __fmul_rn(a[u], xv);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) acc = __fadd_rn(acc, p[u]);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        c[u] = cn[u];
+        a[u] = an[u];
+      }
+      pos = pn;
+    }
+    if (!live) continue;
+    if (d.w < 0) __stcs(y + (r1 - 1), acc);
+    else partials[(int64_t)d.w * 32 + lane] = acc;
+  }
+}
+
 // plus-times Float32 SELL over relabelled columns (k_sell_hot + chunk combination)
 static int launch_sell_hot(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32& sr,
                            const int32_t* colval) {
@@ -876,13 +1010,20 @@ static int launch_sell_hot(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32& sr,
   if (ctx->device < 64 && !attr_set[ctx->device]) {
     GG_CUDA(cudaFuncSetAttribute(k_sell_hot, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  kHotCols * (int)sizeof(float)));
+    GG_CUDA(cudaFuncSetAttribute(k_sell_hot32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kHotCols * (int)sizeof(float)));
     attr_set[ctx->device] = true;
   }
   if (P->nitems > 0) {
     const int tr = trace_main_begin(ctx);
-    k_sell_hot<<<ctx->num_sms, kHotThreads, hot * sizeof(float), ctx->stream>>>(
-        sr.nz, sr.x, sr.y, A->slice_ptr, colval, A->sigma > 1 ? A->perm : nullptr, C, A->m,
-        P->items, P->nitems, static_cast<float*>(P->partials), hot);
+    if (C == 32)
+      k_sell_hot32<<<ctx->num_sms, kHotThreads, hot * sizeof(float), ctx->stream>>>(
+          sr.nz, sr.x, sr.y, colval, A->sigma > 1 ? A->perm : nullptr, A->m, P->pitems, P->npitems,
+          static_cast<float*>(P->partials), hot);
+    else
+      k_sell_hot<<<ctx->num_sms, kHotThreads, hot * sizeof(float), ctx->stream>>>(
+          sr.nz, sr.x, sr.y, A->slice_ptr, colval, A->sigma > 1 ? A->perm : nullptr, C, A->m,
+          P->items, P->nitems, static_cast<float*>(P->partials), hot);
     trace_main_end(ctx, tr);
     trace_count(ctx, 1);
   }

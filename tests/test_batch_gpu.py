@@ -129,3 +129,24 @@ def test_sssp_batch_hubs(dtype):
     ref, _ = O.sssp(n, rp, cv, nz, src)
     got = host(G.shortest_path(B, src))
     assert (got == ref).all()
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.float32])
+def test_single_source_hub_pieces(dtype):
+    """Single-source BFS and shortest paths where frontier vertices have thousands of
+    out-edges (push pieces) and in-edges (pull pieces), on a directed graph and on its
+    symmetrised version."""
+    n = 12000
+    rp, cv, nz = hub_graph(n, 43, dtype)
+    A = sp.csr_matrix((nz, cv - 1, rp - 1), shape=(n, n))
+    for M in (A, (A + A.T).tocsr()):
+        M.sort_indices()
+        rp2, cv2, nz2 = csr_from_scipy(M)
+        B = G.SparseGPUMatrixCSR(n, n, rp2, cv2, nz2)
+        for s in (1, 2, 3, 77, 5000):
+            ref, _ = O.sssp(n, rp2, cv2, nz2, np.array([s], np.int64))
+            got = host(G.shortest_path(B, s))
+            assert (got == ref[:, 0] if ref.ndim == 2 else got == ref).all(), s
+            if dtype == np.int32:
+                lv, _ = O.bfs_levels(n, rp2, cv2, nz2, s)
+                assert (host(G.bfs_distances(B, s)) == lv).all(), s
