@@ -259,6 +259,10 @@ def run_spmv_rmat(args, scale=22):
         dist.init_process_group("nccl", device_id=device)
     A = rmat(scale, gen.W_U01_F32, device)
     x = gen.uniform_vector(A.n, seed=2, device=device)
+    if args.sell_variant:
+        from gpugraphs import tuning
+        G.gpu_spmv_(torch.zeros(A.n, device=device), A, x)  # builds the SELL-32 copy
+        tuning.apply(A, {"sell_variant": args.sell_variant})
     n, nnz = A.n, A.nnz()
     y = torch.zeros(n, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
@@ -343,7 +347,10 @@ def run_spmv_rmat(args, scale=22):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "peak_kind": peak_kind, "algorithmic_bytes": B,
-                     "kernel_ms": round(kernel_ms, 5), "kernel": "k_sell_hot32 (SELL-32 copy sorted by row length, relabelled columns)"},
+                     "kernel_ms": round(kernel_ms, 5),
+                     "kernel": {"registers": "k_sell_hot32", "bulk_copy": "k_sell_tma32"}[
+                         args.sell_variant or "registers"]
+                     + " (SELL-32 copy sorted by row length, relabelled columns)"},
         "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * n},
         "gpu_launches": tr.launches,
@@ -763,6 +770,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-secondary", action="store_true", help="headline SpMV only")
     ap.add_argument("--graphs", type=int, default=1000, help="graph count of --workload multigraph")
+    ap.add_argument("--sell-variant", default=None, choices=["registers", "bulk_copy"],
+                    help="SpMV workloads: kernel variant over the SELL-32 copy (default: built-in)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

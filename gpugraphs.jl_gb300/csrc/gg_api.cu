@@ -242,8 +242,11 @@ int gg_init(int device, gg_ctx** out) {
   cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_flags, 64 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_flags, 64 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(unsigned));
   if (e != cudaSuccess) {
     cudaFree(c->d_flags);
+    cudaFree(c->d_err);
     delete c;
     return cuda_error(e, "gg_init");
   }
@@ -258,6 +261,7 @@ int gg_destroy(gg_ctx* ctx) {
   cudaFree(ctx->scratch);
   cudaFree(ctx->d_flags);
   cudaFreeHost(ctx->h_flags);
+  cudaFree(ctx->d_err);
   if (ctx->trace_ev) {
     for (int i = 0; i < 2 * kTraceMax; ++i) cudaEventDestroy(ctx->trace_ev[i]);
     delete[] ctx->trace_ev;
@@ -313,6 +317,14 @@ int gg_set_stream(gg_ctx* ctx, void* stream) {
 int gg_stream_sync(gg_ctx* ctx) {
   if (!ctx) return set_error(GG_ERR_ARGUMENT, "ctx is NULL");
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (ctx->d_err) {  // a bounded device-side wait ran out since the last check
+    unsigned e = 0;
+    GG_CUDA(cudaMemcpy(&e, ctx->d_err, sizeof(e), cudaMemcpyDeviceToHost));
+    if (e) {
+      GG_CUDA(cudaMemset(ctx->d_err, 0, sizeof(unsigned)));
+      return set_error(GG_ERR_TIMEOUT, "a device-side wait ran out (results of the calls since the last sync are invalid)");
+    }
+  }
   return GG_OK;
 }
 

@@ -152,11 +152,12 @@ __global__ void k_bs_init(T* D, int64_t n, const int64_t* src, int64_t S, uint8_
 }
 
 template <typename T>
-__global__ void k_bs_seed(T* D, const int64_t* src, int64_t S, uint8_t* changed) {
+__global__ void k_bs_seed(T* D, const int64_t* src, int64_t S, uint8_t* changed, int32_t* cq) {
   for (int64_t q = threadIdx.x; q < S; q += blockDim.x) {
     const int64_t s = src[q] - 1;
     D[s * 32 + q] = T(0);
     changed[s] = 1;
+    cq[q] = (int32_t)s;  // the first round's changed vertices
   }
 }
 
@@ -170,39 +171,80 @@ __global__ void k_bs_out(const T* D, int64_t n, int64_t S, T* dist, int64_t ld) 
   }
 }
 
+// Work buffers of one batched shortest-path call.  ctr: [0] vertices changed this
+// round, [1] / [2] lengths of the changed queues cq[0] / cq[1], [3] marked vertices.
 template <typename T>
-static int bs_group(gg_ctx* ctx, int64_t n, const BatchGraph& g, const HubPlan* hp,
-                    const int64_t* dsrc, int64_t S,
-                    T* dist, int64_t ld, T* D, uint8_t* c0, uint8_t* c1, unsigned long long* cnt,
-                    int64_t* rounds) {
+struct BsWork {
+  T* D;
+  uint8_t* c[2];
+  int32_t* cq[2];
+  int32_t* vlist;
+  unsigned* mark;
+  unsigned long long* ctr;
+};
+
+// Rounds run over every vertex while many vertices change, and over the marked
+// out-neighbours of the changed ones (k_ms_mark) once few do: a round's work then
+// follows the frontier instead of the whole graph.  Both kinds compute the same
+// in-place relaxation, so the fixpoint is unchanged.
+template <typename T>
+static int bs_group(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, const HubPlan* hp,
+                    const int32_t* prow, const int32_t* pcol, const int64_t* dsrc, int64_t S,
+                    T* dist, int64_t ld, BsWork<T>& w, int64_t* rounds) {
   int64_t gb = (n * 32 + 255) / 256;
   if (gb > (int64_t)ctx->num_sms * 8) gb = (int64_t)ctx->num_sms * 8;
   int64_t pb = (hp->npiece * 32 + 255) / 256;
   if (pb > (int64_t)ctx->num_sms * 8) pb = (int64_t)ctx->num_sms * 8;
-  k_bs_init<T><<<(int)gb, 256, 0, ctx->stream>>>(D, n, dsrc, S, c0);
-  k_bs_seed<T><<<1, 64, 0, ctx->stream>>>(D, dsrc, S, c0);
+  if (pb < 1) pb = 1;
+  const int64_t gcap = (int64_t)ctx->num_sms * 8;
+  k_bs_init<T><<<(int)gb, 256, 0, ctx->stream>>>(w.D, n, dsrc, S, w.c[0]);
+  k_bs_seed<T><<<1, 64, 0, ctx->stream>>>(w.D, dsrc, S, w.c[0], w.cq[0]);
   GG_CUDA(cudaGetLastError());
+  unsigned long long hs[4] = {0, (unsigned long long)S, 0, 0};
+  GG_CUDA(cudaMemcpyAsync(w.ctr, hs, sizeof(hs), cudaMemcpyHostToDevice, ctx->stream));
   unsigned long long* h = reinterpret_cast<unsigned long long*>(ctx->h_flags);
+  const int64_t avg_deg = n > 0 ? (nnz + n - 1) / n : 1;
+  int64_t nchanged = S;
+  int cur = 0;
   for (int64_t r = 0;; ++r) {
     if (r > n + 1) return set_error(GG_ERR_NOT_CONVERGED, "batched shortest paths did not converge");
-    GG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), ctx->stream));
-    GG_CUDA(cudaMemsetAsync(c1, 0, (size_t)n, ctx->stream));
-    k_ms_round<T><<<(int)gb, 256, 0, ctx->stream>>>(n, g, D, c0, c1, cnt, nullptr);
+    unsigned long long* ncq_cur = w.ctr + 1 + cur;
+    unsigned long long* ncq_nxt = w.ctr + 1 + (cur ^ 1);
+    GG_CUDA(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long), ctx->stream));
+    GG_CUDA(cudaMemsetAsync(ncq_nxt, 0, sizeof(unsigned long long), ctx->stream));
+    GG_CUDA(cudaMemsetAsync(w.c[cur ^ 1], 0, (size_t)n, ctx->stream));
+    const bool restricted = nchanged * avg_deg * 4 < nnz;
+    if (restricted) {
+      GG_CUDA(cudaMemsetAsync(w.mark, 0, ((n + 31) / 32) * sizeof(unsigned), ctx->stream));
+      GG_CUDA(cudaMemsetAsync(w.ctr + 3, 0, sizeof(unsigned long long), ctx->stream));
+      int64_t mb = (nchanged * 32 + 255) / 256;
+      if (mb > gcap) mb = gcap;
+      k_ms_mark<<<(int)(mb < 1 ? 1 : mb), 256, 0, ctx->stream>>>(prow, pcol, w.cq[cur], ncq_cur,
+                                                                 w.mark, w.vlist, w.ctr + 3);
+      k_ms_round<T><<<(int)gcap, 256, 0, ctx->stream>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr,
+                                                        nullptr, w.vlist, w.ctr + 3,
+                                                        w.cq[cur ^ 1], ncq_nxt);
+    } else {
+      k_ms_round<T><<<(int)gb, 256, 0, ctx->stream>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr,
+                                                      nullptr, nullptr, nullptr, w.cq[cur ^ 1],
+                                                      ncq_nxt);
+    }
     GG_CUDA(cudaGetLastError());
     if (hp->npiece > 0) {
-      k_ms_round_hub<T><<<(int)pb, 256, 0, ctx->stream>>>(g, hp->pieces, hp->npiece, hp->hubs, D,
-                                                          c0, c1, cnt, nullptr);
+      k_ms_round_hub<T><<<(int)pb, 256, 0, ctx->stream>>>(
+          g, hp->pieces, hp->npiece, hp->hubs, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr,
+          restricted ? w.mark : nullptr, w.cq[cur ^ 1], ncq_nxt);
       GG_CUDA(cudaGetLastError());
     }
-    GG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    GG_CUDA(cudaMemcpyAsync(h, w.ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            ctx->stream));
     GG_CUDA(cudaStreamSynchronize(ctx->stream));
     if (rounds) *rounds += 1;
     if (h[0] == 0) break;
-    uint8_t* t = c0;
-    c0 = c1;
-    c1 = t;
+    nchanged = (int64_t)h[1 + (cur ^ 1)];
+    cur ^= 1;
   }
-  k_bs_out<T><<<(int)gb, 256, 0, ctx->stream>>>(D, n, S, dist, ld);
+  k_bs_out<T><<<(int)gb, 256, 0, ctx->stream>>>(w.D, n, S, dist, ld);
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
@@ -212,24 +254,40 @@ static int sssp_batch_t(gg_ctx* ctx, gg_mat* A, const BatchGraph& g, const int64
                         int64_t S, T* dist, int64_t ld, int64_t* rounds) {
   const int64_t n = A->m;
   GG_CHECK(build_hub_plan(ctx, A, g.rowptr, n));
-  T* D = nullptr;
+  const int32_t* prow = nullptr;
+  const int32_t* pcol = nullptr;
+  GG_CHECK(push_view(ctx, A, &prow, &pcol));
+  const HubPlan* hp = A->hubplan;
+  // a hub may enter a changed queue once per piece
+  const int64_t qcap = n + hp->npiece + 64;
+  BsWork<T> w;
   uint8_t* c = nullptr;
   int64_t* dsrc = nullptr;
-  unsigned long long* cnt = nullptr;
-  GG_CUDA(cudaMallocAsync((void**)&D, (size_t)n * 32 * sizeof(T), ctx->stream));
+  GG_CUDA(cudaMallocAsync((void**)&w.D, (size_t)n * 32 * sizeof(T), ctx->stream));
   GG_CUDA(cudaMallocAsync((void**)&c, (size_t)2 * n + 64, ctx->stream));
+  GG_CUDA(cudaMallocAsync((void**)&w.cq[0], (size_t)qcap * sizeof(int32_t), ctx->stream));
+  GG_CUDA(cudaMallocAsync((void**)&w.cq[1], (size_t)qcap * sizeof(int32_t), ctx->stream));
+  GG_CUDA(cudaMallocAsync((void**)&w.vlist, (size_t)(n + 64) * sizeof(int32_t), ctx->stream));
+  GG_CUDA(cudaMallocAsync((void**)&w.mark, (size_t)((n + 31) / 32 + 2) * sizeof(unsigned), ctx->stream));
+  GG_CUDA(cudaMallocAsync((void**)&w.ctr, 64, ctx->stream));
   GG_CUDA(cudaMallocAsync((void**)&dsrc, (size_t)S * sizeof(int64_t) + 8, ctx->stream));
-  GG_CUDA(cudaMallocAsync((void**)&cnt, 64, ctx->stream));
   GG_CUDA(cudaMemcpyAsync(dsrc, sources, S * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+  w.c[0] = c;
+  w.c[1] = c + n;
+  const int64_t nnz = (int64_t)A->nnz;
   int rc = GG_OK;
   for (int64_t q0 = 0; q0 < S && rc == GG_OK; q0 += 32) {
     const int64_t Sg = S - q0 < 32 ? S - q0 : 32;
-    rc = bs_group<T>(ctx, n, g, A->hubplan, dsrc + q0, Sg, dist + q0 * ld, ld, D, c, c + n, cnt, rounds);
+    rc = bs_group<T>(ctx, n, nnz, g, hp, prow, pcol, dsrc + q0, Sg, dist + q0 * ld, ld, w, rounds);
   }
-  cudaFreeAsync(D, ctx->stream);
+  cudaFreeAsync(w.D, ctx->stream);
   cudaFreeAsync(c, ctx->stream);
+  cudaFreeAsync(w.cq[0], ctx->stream);
+  cudaFreeAsync(w.cq[1], ctx->stream);
+  cudaFreeAsync(w.vlist, ctx->stream);
+  cudaFreeAsync(w.mark, ctx->stream);
+  cudaFreeAsync(w.ctr, ctx->stream);
   cudaFreeAsync(dsrc, ctx->stream);
-  cudaFreeAsync(cnt, ctx->stream);
   return rc;
 }
 

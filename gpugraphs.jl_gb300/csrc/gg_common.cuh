@@ -399,6 +399,7 @@ struct gg_ctx {
   size_t scratch_bytes = 0;
   unsigned int* d_flags = nullptr;  // small device word array for status flags
   unsigned int* h_flags = nullptr;  // pinned mirror
+  unsigned int* d_err = nullptr;    // set by kernels whose bounded waits ran out
   // launch tracing (gg_trace_begin / gg_trace_end): kernel launches of the SpMV /
   // SpMM paths are counted and their main kernel bracketed by events from a pool
   bool trace_on = false;
@@ -453,6 +454,9 @@ struct gg_mat {
   int tuned_spmv = 0;
   int block_rows = 0;
   int mm_cpl = 0;
+  // SELL-32 plus-times kernel: 0 = register loads (k_sell_hot32), 1 = matrix stream
+  // staged by bulk copies (k_sell_tma32)
+  int sell_variant = 0;
 };
 
 namespace gg {
@@ -465,5 +469,7 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
 int build_row_blocks(gg_ctx* ctx, gg_mat* A);
 int build_sell_plan(gg_ctx* ctx, gg_mat* A);
 int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n);  // gg_batch.cu
+int launch_sell_tma(gg_ctx* ctx, gg_mat* A, const float* nzv, const float* xr, float* y,
+                    const int32_t* colval);  // gg_spmv_tma.cu
 int row_stats(gg_ctx* ctx, gg_mat* A);
 }  // namespace gg

@@ -286,6 +286,16 @@ static int ensure_aux(gg_ctx* ctx, gg_mat* A) {
 }
 
 // CSR view of A_T (1-based) and its value flags, for the batched kernels
+static int ensure_push(gg_ctx* ctx, gg_mat* A, int which);
+
+// out-edges of every vertex (transpose of A_T, 0-based, all stored entries)
+int push_view(gg_ctx* ctx, gg_mat* A, const int32_t** prow, const int32_t** pcol) {
+  GG_CHECK(ensure_push(ctx, A, 1));
+  *prow = A->aux->push[1].rowptr;
+  *pcol = A->aux->push[1].colval;
+  return GG_OK;
+}
+
 int graph_view(gg_ctx* ctx, gg_mat* A, const int32_t** rp, const int32_t** cv, const void** nz,
                bool* all_odd, bool* nonneg) {
   GG_CHECK(ensure_aux(ctx, A));

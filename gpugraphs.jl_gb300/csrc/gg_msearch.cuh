@@ -23,6 +23,7 @@ namespace gg {
 int graph_view(gg_ctx* ctx, gg_mat* A, const int32_t** rp, const int32_t** cv, const void** nz,
                bool* all_odd, bool* nonneg);  // gg_graph.cu
 int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n);  // gg_batch.cu
+int push_view(gg_ctx* ctx, gg_mat* A, const int32_t** prow, const int32_t** pcol);  // gg_graph.cu
 
 namespace {
 
@@ -280,17 +281,31 @@ __device__ __forceinline__ bool bs_pull(const BatchGraph& g, const T* D,
   return any;
 }
 
-// one round: warp per vertex v, lane = source column; pull from in-neighbours that
-// changed last round, lower D[v] in place, flag v when any column dropped (chg_next
-// is cleared before the round).  Hubs are left to k_ms_round_hub.
+// Changed-vertex bookkeeping of a round: chg_next[v] = 1 and, when cq is given, v is
+// appended to the changed queue cq (count *ncq) that drives the next round's marking.
+__device__ __forceinline__ void ms_changed(int64_t v, uint8_t* chg_next, unsigned long long* count,
+                                           int32_t* cq, unsigned long long* ncq) {
+  chg_next[v] = 1;
+  atomicAdd(count, 1ull);
+  if (cq) cq[atomicAdd(ncq, 1ull)] = (int32_t)v;
+}
+
+// one round: warp per vertex v (every vertex, or the marked ones in vlist[0, *nlist)),
+// lane = source column; pull from in-neighbours that changed last round, lower D[v]
+// in place, flag v when any column dropped (chg_next is cleared before the round).
+// Hubs are left to k_ms_round_hub.
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_ms_round(int64_t n, BatchGraph g, T* D, const uint8_t* __restrict__ chg,
-               uint8_t* chg_next, unsigned long long* count, unsigned* drop) {
+               uint8_t* chg_next, unsigned long long* count, unsigned* drop,
+               const int32_t* __restrict__ vlist, const unsigned long long* nlist, int32_t* cq,
+               unsigned long long* ncq) {
   const int lane = threadIdx.x & 31;
   unsigned dropped_cols = 0;
-  for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n;
-       v += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+  const int64_t total = vlist ? (int64_t)*((volatile const unsigned long long*)nlist) : n;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < total;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t v = vlist ? (int64_t)vlist[i] : i;
     const int64_t k0 = (int64_t)g.rowptr[v] - 1, k1 = (int64_t)g.rowptr[v + 1] - 1;
     if (k1 - k0 > kHubDegB) continue;
     T best = Lim<T>::max();
@@ -305,12 +320,43 @@ __global__ void __launch_bounds__(256)
     }
     const unsigned b = __ballot_sync(kFullB, dropped);
     dropped_cols |= b;
-    if (lane == 0 && b) {
-      chg_next[v] = 1;
-      atomicAdd(count, 1ull);
-    }
+    if (lane == 0 && b) ms_changed(v, chg_next, count, cq, ncq);
   }
   if (drop && lane == 0 && dropped_cols) atomicOr(drop, dropped_cols);
+}
+
+// marking for a frontier-restricted round: the out-neighbours of the changed vertices
+// cq[0, *ncq) are the only vertices whose distances can drop; each is marked once in
+// the bitmap and listed in vlist
+__global__ void __launch_bounds__(256)
+    k_ms_mark(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+              const int32_t* __restrict__ cq, const unsigned long long* ncq, unsigned* mark,
+              int32_t* vlist, unsigned long long* nlist) {
+  const int lane = threadIdx.x & 31;
+  const int64_t total = (int64_t)*((volatile const unsigned long long*)ncq);
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < total;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int32_t u = cq[i];
+    const int32_t k0 = prow[u], k1 = prow[u + 1];
+    for (int32_t kb = k0; kb < k1; kb += 32) {
+      const int32_t k = kb + lane;
+      bool add = false;
+      int32_t w = 0;
+      if (k < k1) {
+        w = __ldg(pcol + k);
+        const unsigned bit = 1u << (w & 31);
+        if (!(__ldcg(mark + (w >> 5)) & bit)) add = !(atomicOr(mark + (w >> 5), bit) & bit);
+      }
+      const unsigned b = __ballot_sync(kFullB, add);
+      if (b) {
+        const int leader = __ffs(b) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(nlist, (unsigned long long)__popc(b));
+        base = __shfl_sync(kFullB, base, leader);
+        if (add) vlist[base + __popc(b & ((1u << lane) - 1u))] = w;
+      }
+    }
+  }
 }
 
 template <typename T> __device__ __forceinline__ T b_atomic_min(T* p, T v);
@@ -330,17 +376,20 @@ template <> __device__ __forceinline__ double b_atomic_min<double>(double* p, do
 }
 
 // hub pieces: one warp per piece, atomic min into the hub's 32 columns
+// (with mark given, only hubs marked for this round are relaxed)
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_ms_round_hub(BatchGraph g, const int4* __restrict__ pieces, int64_t npiece,
                    const int32_t* __restrict__ hubs, T* D, const uint8_t* __restrict__ chg,
-                   uint8_t* chg_next, unsigned long long* count, unsigned* drop) {
+                   uint8_t* chg_next, unsigned long long* count, unsigned* drop,
+                   const unsigned* __restrict__ mark, int32_t* cq, unsigned long long* ncq) {
   const int lane = threadIdx.x & 31;
   unsigned dropped_cols = 0;
   for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < npiece;
        i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int4 p = pieces[i];
     const int64_t v = hubs[p.x];
+    if (mark && !((__ldcg(mark + (v >> 5)) >> (v & 31)) & 1u)) continue;
     T best = Lim<T>::max();
     const bool any = bs_pull<T>(g, D, chg, p.y, p.z, lane, best);
     bool dropped = false;
@@ -350,10 +399,7 @@ __global__ void __launch_bounds__(256)
     }
     const unsigned b = __ballot_sync(kFullB, dropped);
     dropped_cols |= b;
-    if (lane == 0 && b) {
-      chg_next[v] = 1;
-      atomicAdd(count, 1ull);
-    }
+    if (lane == 0 && b) ms_changed(v, chg_next, count, cq, ncq);
   }
   if (drop && lane == 0 && dropped_cols) atomicOr(drop, dropped_cols);
 }

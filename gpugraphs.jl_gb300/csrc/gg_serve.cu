@@ -23,6 +23,7 @@
 // queue otherwise.  Every slot's computation is independent of the other slots, so a
 // result does not depend on the mix it ran in.
 #include <algorithm>
+#include <cstring>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -95,10 +96,12 @@ __global__ void k_ss_admit(int64_t n, T* D, unsigned qmask) {
       if ((qmask >> q) & 1u) D[v * kColSlots + q] = Lim<T>::max();
 }
 template <typename T>
-__global__ void k_ss_seed(T* D, uint8_t* chg, const int* slots, const int64_t* srcs, int nslots) {
+__global__ void k_ss_seed(T* D, uint8_t* chg, const int* slots, const int64_t* srcs, int nslots,
+                          int32_t* cq, unsigned long long* ncq) {
   for (int i = threadIdx.x; i < nslots; i += blockDim.x) {
     D[srcs[i] * kColSlots + slots[i]] = T(0);
     chg[srcs[i]] = 1;
+    cq[atomicAdd(ncq, 1ull)] = (int32_t)srcs[i];  // changed for the next round's marking
   }
 }
 
@@ -107,6 +110,12 @@ __global__ void k_ss_out(const T* D, int64_t n, int q, T* out) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x)
     out[v] = D[v * kColSlots + q];
+}
+
+__global__ void k_fill_levels(int32_t* d, int64_t n) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x)
+    d[v] = INT32_MAX;
 }
 
 // SpMV-iteration columns
@@ -153,6 +162,14 @@ struct Executor {
   // SSSP
   void* D = nullptr;
   uint8_t *c0 = nullptr, *c1 = nullptr;
+  // frontier-restricted rounds: changed queues, marked vertices (gg_msearch.cuh)
+  int32_t* cq[2] = {nullptr, nullptr};
+  int32_t* vlist = nullptr;
+  unsigned* mark = nullptr;
+  int cq_cur = 0;
+  int64_t nchanged = 0;
+  const int32_t* prow = nullptr;
+  const int32_t* pcol = nullptr;
   int dtype = 0;
   // SpMV iterations
   float *X = nullptr, *Y = nullptr;
@@ -237,6 +254,10 @@ static void exec_free(Executor& E) {
   cudaFree(E.D);
   cudaFree(E.c0);
   cudaFree(E.c1);
+  cudaFree(E.cq[0]);
+  cudaFree(E.cq[1]);
+  cudaFree(E.vlist);
+  cudaFree(E.mark);
   cudaFree(E.X);
   cudaFree(E.Y);
   cudaFree(E.d_slots);
@@ -316,6 +337,14 @@ static int exec_create(gg_server* S, int gi, int kind, Executor& E) {
     GG_CUDA(cudaMalloc((void**)&E.c1, (size_t)n + 64));
     GG_CUDA(cudaMemsetAsync(E.c0, 0, (size_t)n + 64, st));
     GG_CUDA(cudaMemsetAsync(E.c1, 0, (size_t)n + 64, st));
+    const HubPlan* hp = S->graphs[gi]->hubplan;
+    const int64_t qcap = n + hp->npiece + kColSlots + 64;  // a hub may be queued once per piece
+    GG_CUDA(cudaMalloc((void**)&E.cq[0], qcap * sizeof(int32_t)));
+    GG_CUDA(cudaMalloc((void**)&E.cq[1], qcap * sizeof(int32_t)));
+    GG_CUDA(cudaMalloc((void**)&E.vlist, (n + 64) * sizeof(int32_t)));
+    GG_CUDA(cudaMalloc((void**)&E.mark, ((n + 31) / 32 + 2) * sizeof(unsigned)));
+    GG_CUDA(cudaMemsetAsync(E.d_cnt, 0, 64, st));  // [0] count, [1]/[2] queue lengths, [3] marked
+    GG_CHECK(push_view(&S->own, S->graphs[gi], &E.prow, &E.pcol));
     // every column starts at the fixpoint of "no source": typemax everywhere
     const unsigned all = 0xffffffffu;
     switch (dt) {
@@ -382,22 +411,27 @@ static int exec_admit(gg_server* S, int gi, Executor& E, std::vector<Request>& w
     k_sb_admit_seed<<<1, 256, 0, st>>>(E.V, E.F, E.outp, E.d_slots, E.d_srcs, k);
   } else if (E.kind == GG_QUERY_SSSP) {
     const unsigned qm = amask[0];
+    E.nchanged += k;
     switch (E.dtype) {
       case GG_INT32:
         k_ss_admit<int32_t><<<grid_s(S, n), 256, 0, st>>>(n, (int32_t*)E.D, qm);
-        k_ss_seed<int32_t><<<1, 64, 0, st>>>((int32_t*)E.D, E.c0, E.d_slots, E.d_srcs, k);
+        k_ss_seed<int32_t><<<1, 64, 0, st>>>((int32_t*)E.D, E.c0, E.d_slots, E.d_srcs, k, E.cq[E.cq_cur],
+                                       E.d_cnt + 1 + E.cq_cur);
         break;
       case GG_INT64:
         k_ss_admit<int64_t><<<grid_s(S, n), 256, 0, st>>>(n, (int64_t*)E.D, qm);
-        k_ss_seed<int64_t><<<1, 64, 0, st>>>((int64_t*)E.D, E.c0, E.d_slots, E.d_srcs, k);
+        k_ss_seed<int64_t><<<1, 64, 0, st>>>((int64_t*)E.D, E.c0, E.d_slots, E.d_srcs, k, E.cq[E.cq_cur],
+                                       E.d_cnt + 1 + E.cq_cur);
         break;
       case GG_FLOAT32:
         k_ss_admit<float><<<grid_s(S, n), 256, 0, st>>>(n, (float*)E.D, qm);
-        k_ss_seed<float><<<1, 64, 0, st>>>((float*)E.D, E.c0, E.d_slots, E.d_srcs, k);
+        k_ss_seed<float><<<1, 64, 0, st>>>((float*)E.D, E.c0, E.d_slots, E.d_srcs, k, E.cq[E.cq_cur],
+                                       E.d_cnt + 1 + E.cq_cur);
         break;
       default:
         k_ss_admit<double><<<grid_s(S, n), 256, 0, st>>>(n, (double*)E.D, qm);
-        k_ss_seed<double><<<1, 64, 0, st>>>((double*)E.D, E.c0, E.d_slots, E.d_srcs, k);
+        k_ss_seed<double><<<1, 64, 0, st>>>((double*)E.D, E.c0, E.d_slots, E.d_srcs, k, E.cq[E.cq_cur],
+                                       E.d_cnt + 1 + E.cq_cur);
         break;
     }
   } else {
@@ -409,15 +443,33 @@ static int exec_admit(gg_server* S, int gi, Executor& E, std::vector<Request>& w
 }
 
 template <typename T>
-static void ss_round(gg_server* S, Executor& E, const SrvGraph& sg, const HubPlan* hp) {
+static void ss_round(gg_server* S, Executor& E, const SrvGraph& sg, const HubPlan* hp,
+                     int64_t nnz) {
   cudaStream_t st = E.ectx.stream;
   const int64_t n = sg.n;
   T* D = static_cast<T*>(E.D);
-  k_ms_round<T><<<grid_s(S, n * 32), 256, 0, st>>>(n, sg.g, D, E.c0, E.c1, E.d_cnt, E.d_amask);
+  const int cur = E.cq_cur;
+  unsigned long long* ncq_cur = E.d_cnt + 1 + cur;
+  unsigned long long* ncq_nxt = E.d_cnt + 1 + (cur ^ 1);
+  cudaMemsetAsync(ncq_nxt, 0, sizeof(unsigned long long), st);
+  const int64_t avg_deg = n > 0 ? (nnz + n - 1) / n : 1;
+  // few changed vertices: visit only their out-neighbours (same fixpoint)
+  const bool restricted = E.nchanged * avg_deg * 4 < nnz;
+  if (restricted) {
+    cudaMemsetAsync(E.mark, 0, ((n + 31) / 32) * sizeof(unsigned), st);
+    cudaMemsetAsync(E.d_cnt + 3, 0, sizeof(unsigned long long), st);
+    k_ms_mark<<<grid_s(S, E.nchanged * 32), 256, 0, st>>>(E.prow, E.pcol, E.cq[cur], ncq_cur, E.mark,
+                                                          E.vlist, E.d_cnt + 3);
+    k_ms_round<T><<<grid_s(S, n * 32), 256, 0, st>>>(n, sg.g, D, E.c0, E.c1, E.d_cnt, E.d_amask,
+                                                      E.vlist, E.d_cnt + 3, E.cq[cur ^ 1], ncq_nxt);
+  } else {
+    k_ms_round<T><<<grid_s(S, n * 32), 256, 0, st>>>(n, sg.g, D, E.c0, E.c1, E.d_cnt, E.d_amask,
+                                                      nullptr, nullptr, E.cq[cur ^ 1], ncq_nxt);
+  }
   if (hp->npiece > 0)
-    k_ms_round_hub<T><<<grid_s(S, hp->npiece * 32), 256, 0, st>>>(sg.g, hp->pieces, hp->npiece,
-                                                                  hp->hubs, D, E.c0, E.c1, E.d_cnt,
-                                                                  E.d_amask);
+    k_ms_round_hub<T><<<grid_s(S, hp->npiece * 32), 256, 0, st>>>(
+        sg.g, hp->pieces, hp->npiece, hp->hubs, D, E.c0, E.c1, E.d_cnt, E.d_amask,
+        restricted ? E.mark : nullptr, E.cq[cur ^ 1], ncq_nxt);
 }
 
 // one tick of an executor, enqueued on its stream, followed by its event
@@ -449,14 +501,18 @@ static int exec_tick(gg_server* S, int gi, Executor& E) {
   } else if (E.kind == GG_QUERY_SSSP) {
     GG_CUDA(cudaMemsetAsync(E.d_amask, 0, 4, st));  // dropped columns of this round
     GG_CUDA(cudaMemsetAsync(E.c1, 0, (size_t)n, st));
+    const int64_t nnz = S->graphs[gi]->nnz;
     switch (E.dtype) {
-      case GG_INT32: ss_round<int32_t>(S, E, sg, hp); break;
-      case GG_INT64: ss_round<int64_t>(S, E, sg, hp); break;
-      case GG_FLOAT32: ss_round<float>(S, E, sg, hp); break;
-      default: ss_round<double>(S, E, sg, hp); break;
+      case GG_INT32: ss_round<int32_t>(S, E, sg, hp, nnz); break;
+      case GG_INT64: ss_round<int64_t>(S, E, sg, hp, nnz); break;
+      case GG_FLOAT32: ss_round<float>(S, E, sg, hp, nnz); break;
+      default: ss_round<double>(S, E, sg, hp, nnz); break;
     }
     std::swap(E.c0, E.c1);
     GG_CUDA(cudaMemcpyAsync(E.h_result, E.d_amask, 4, cudaMemcpyDeviceToHost, st));
+    // length of the changed queue of this round (h_result[2..3]) for the next decision
+    GG_CUDA(cudaMemcpyAsync(E.h_result + 2, E.d_cnt + 1 + (E.cq_cur ^ 1), 8, cudaMemcpyDeviceToHost, st));
+    E.cq_cur ^= 1;
   } else {
     // only the columns up to the highest busy slot are multiplied (free slots are
     // reused lowest first, so few queries cost few columns)
@@ -482,6 +538,11 @@ static int exec_retire(gg_server* S, int gi, Executor& E, std::vector<Request>& 
   bool copies = false;
   if (E.kind == GG_QUERY_BFS)
     for (int w = 0; w < kBfsW; ++w) E.act_host[w] = E.h_result[w];
+  if (E.kind == GG_QUERY_SSSP) {
+    unsigned long long nq = 0;
+    memcpy(&nq, E.h_result + 2, sizeof(nq));
+    E.nchanged = (int64_t)nq;
+  }
   for (int q = 0; q < (int)E.slots.size(); ++q) {
     Slot& sl = E.slots[q];
     if (!sl.busy) continue;
@@ -524,8 +585,13 @@ static const int kSoloWorkers = 4;
 static int solo_run(gg_server* S, gg_ctx* c, const Request& r) {
   gg_mat* A = S->graphs[r.graph];
   const int64_t n = A->m;
-  if (r.kind == GG_QUERY_BFS)
-    return gg_bfs_levels(c, A, r.source, static_cast<int32_t*>(r.out), n, nullptr);
+  if (r.kind == GG_QUERY_BFS) {
+    // bfs_distances: typemax(Int32) for every vertex the search does not reach
+    int32_t* out = static_cast<int32_t*>(r.out);
+    k_fill_levels<<<grid_s(S, n), 256, 0, c->stream>>>(out, n);
+    GG_CUDA(cudaGetLastError());
+    return gg_bfs_levels(c, A, r.source, out, n, nullptr);
+  }
   if (r.kind == GG_QUERY_SSSP) {
     const int dt = A->dtype == GG_BOOL ? GG_INT32 : A->dtype;
     const int64_t src = r.source;
@@ -606,12 +672,25 @@ static void server_loop(gg_server* S) {
       for (auto& f : S->solo_finished) S->solo_active[f.first][f.second] = 0;
       S->solo_finished.clear();
       // a lone request whose executor is idle runs on a solo worker (no batching
-      // needed: the single-query engine is the fastest path for one query)
+      // needed: the single-query engine is the fastest path for one query), when free
+      // HBM covers its working set plus the reserve (admission by free memory)
+      size_t fr = 0, tot = 0;
+      bool mem_known = false;
       for (size_t gi = 0; gi < S->graphs.size() && S->solo_idle > 0; ++gi)
         for (int kk = 0; kk < 3 && S->solo_idle > 0; ++kk) {
           Executor& E = S->exec[gi][kk];
           const bool idle = !E.ready || (E.active() == 0 && !E.inflight && E.finishing.empty());
           if (waiting[gi][kk].size() == 1 && idle && !S->solo_active[gi][kk]) {
+            if (!mem_known) {
+              if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) fr = 0;
+              mem_known = true;
+            }
+            const size_t need = (size_t)S->views[gi].n * 24 + ((size_t)1 << 20);
+            if (fr < need + (size_t)S->reserve) {
+              ++S->admission_waits;
+              continue;  // stays queued; the executor path checks memory the same way
+            }
+            fr -= need;
             gg_server::SoloJob job;
             job.req = waiting[gi][kk].front();
             waiting[gi][kk].clear();
@@ -754,6 +833,11 @@ int gg_server_add_graph(gg_server* S, const gg_mat* A_T, int* graph_id) {
     void* tmp = nullptr;
     GG_CUDA(cudaMalloc(&tmp, (size_t)(n > 0 ? n : 1) * 16));
     int rc = build_hub_plan(&S->own, A, g.g.rowptr, n);
+    if (rc == GG_OK && nonneg) {
+      const int32_t* pr = nullptr;
+      const int32_t* pc = nullptr;
+      rc = push_view(&S->own, A, &pr, &pc);
+    }
     if (rc == GG_OK && !dtype_is_float(A->dtype) && n > 0)
       rc = gg_bfs_levels(&S->own, A, 1, static_cast<int32_t*>(tmp), n, nullptr);
     if (rc == GG_OK && nonneg && n > 0) {

@@ -1014,7 +1014,9 @@ static int launch_sell_hot(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32& sr,
                                  kHotCols * (int)sizeof(float)));
     attr_set[ctx->device] = true;
   }
-  if (P->nitems > 0) {
+  if (P->nitems > 0 && C == 32 && A->sell_variant == 1) {
+    GG_CHECK(launch_sell_tma(ctx, A, sr.nz, sr.x, sr.y, colval));  // brackets its own kernel
+  } else if (P->nitems > 0) {
     const int tr = trace_main_begin(ctx);
     if (C == 32)
       k_sell_hot32<<<ctx->num_sms, kHotThreads, hot * sizeof(float), ctx->stream>>>(

@@ -114,7 +114,7 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
     rc = time_median(ctx, &out->spmv_default_ms, run_spmv, &args);
   }
   double best = out->spmv_default_ms;
-  int best_kind = 0, best_rows = 0;
+  int best_kind = 0, best_rows = 0, best_variant = 0;
   int64_t best_C = 0, best_sigma = 0;
   gg_mat* best_copy = A->sell_copy;  // the built-in choice's copy (if it made one)
   A->sell_copy = nullptr;
@@ -152,20 +152,30 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
         if (gg_sell_create(ctx, A, C, sg, &S) != GG_OK) continue;  // e.g. out of memory
         A->sell_copy = S;
         A->tuned_spmv = 2;
-        double ms = 0;
-        rc = time_median(ctx, &ms, run_spmv, &args);
+        bool keep = false;
+        for (int variant = (C == 32 ? 1 : 0); variant >= 0 && rc == GG_OK; --variant) {
+          S->sell_variant = variant;
+          double ms = 0;
+          rc = time_median(ctx, &ms, run_spmv, &args);
+          if (rc != GG_OK) break;
+          ++cand;
+          if (ms < best) {
+            best = ms;
+            best_kind = 2;
+            best_C = C;
+            best_sigma = sg;
+            best_variant = variant;
+            keep = true;
+          }
+        }
         A->sell_copy = nullptr;
         if (rc != GG_OK) {
           gg_mat_destroy(S);
           break;
         }
-        ++cand;
-        if (ms < best) {
-          best = ms;
-          best_kind = 2;
-          best_C = C;
-          best_sigma = sg;
+        if (keep) {
           if (best_copy) gg_mat_destroy(best_copy);
+          S->sell_variant = best_variant;
           best_copy = S;
         } else {
           gg_mat_destroy(S);
@@ -188,6 +198,7 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
     if (L) {
       out->slice_size = L->slice_size;
       out->sigma = L->sigma;
+      out->sell_variant = L->sell_variant;
     } else {
       out->block_rows = kBlockRows;
     }
@@ -205,6 +216,7 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
     out->spmv_kernel = 2;
     out->slice_size = best_C;
     out->sigma = best_sigma;
+    out->sell_variant = best_variant;
   }
   out->spmv_ms = best;
   out->candidates += cand;
@@ -291,5 +303,9 @@ extern "C" int gg_tune_apply(gg_ctx* ctx, gg_mat* A, const gg_tune_result* choic
     return set_error(GG_ERR_ARGUMENT, "spmv_kernel must be 0, 1 or 2");
   }
   if (cpl) A->mm_cpl = cpl;
+  if (choice->sell_variant == 0 || choice->sell_variant == 1) {
+    A->sell_variant = choice->sell_variant;
+    if (A->sell_copy) A->sell_copy->sell_variant = choice->sell_variant;
+  }
   return GG_OK;
 }

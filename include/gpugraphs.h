@@ -358,6 +358,9 @@ typedef struct gg_tune_result {
   int mm_cols_per_lane;    /* SpMM column tile: 32 x this columns per warp pass */
   double spmm_ms;          /* median time of the chosen SpMM tile (spmm_k > 0) */
   int candidates;          /* configurations timed */
+  int sell_variant;        /* SELL-32 plus-times kernel: 0 = register loads, 1 = matrix stream
+                              staged in shared memory by bulk copies (-1 in gg_tune_apply:
+                              leave as is) */
 } gg_tune_result;
 
 /*

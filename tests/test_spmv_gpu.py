@@ -470,7 +470,8 @@ def test_spmv_generic_semirings_on_rmat():
 def test_spmv_plus_times_large_csr_sorted_sell_path():
     """CSR of >= 65536 rows: plus-times runs on the internal SELL-32 copy with rows
     sorted by length, relabelled columns and the hot part of x in shared memory
-    (narrow slices grouped per warp, wide ones in chunks).  Rows of <= 128 entries are
+    (narrow slices grouped per warp, wide ones in chunks; matrix stream staged by bulk
+    copies or loaded into registers).  Rows of <= 128 entries are
     folded in storage order -> bit-exact against the oracle; all rows within rtol 1e-5
     of FP64; repeated calls give identical results."""
     from gpugraphs import generators as gen
@@ -483,7 +484,10 @@ def test_spmv_plus_times_large_csr_sorted_sell_path():
     ref = A.to_scipy().astype(np.float64) @ x.astype(np.float64)
     deg = np.diff(rowptr)
     first = None
-    for rep in range(2):
+    from gpugraphs import tuning
+    # register loads and bulk-copy staging: the same bits
+    for rep, variant in enumerate(["registers", "registers", "bulk_copy", "bulk_copy"]):
+        tuning.apply(A, {"sell_variant": variant})
         y = torch.full((n,), -1.0, dtype=torch.float32, device="cuda")
         G.gpu_spmv_(y, A, dev(x))
         yh = host(y)
