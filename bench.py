@@ -259,10 +259,13 @@ def run_spmv_rmat(args, scale=22):
         dist.init_process_group("nccl", device_id=device)
     A = rmat(scale, gen.W_U01_F32, device)
     x = gen.uniform_vector(A.n, seed=2, device=device)
-    if args.sell_variant:
+    if args.sell_variant or args.hot_cols:
         from gpugraphs import tuning
         G.gpu_spmv_(torch.zeros(A.n, device=device), A, x)  # builds the SELL-32 copy
-        tuning.apply(A, {"sell_variant": args.sell_variant})
+        choice = {"sell_variant": args.sell_variant or "registers"}
+        if args.hot_cols:
+            choice["hot_cols"] = args.hot_cols
+        tuning.apply(A, choice)
     n, nnz = A.n, A.nnz()
     y = torch.zeros(n, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
@@ -772,6 +775,8 @@ def main():
     ap.add_argument("--graphs", type=int, default=1000, help="graph count of --workload multigraph")
     ap.add_argument("--sell-variant", default=None, choices=["registers", "bulk_copy"],
                     help="SpMV workloads: kernel variant over the SELL-32 copy (default: built-in)")
+    ap.add_argument("--hot-cols", type=int, default=0,
+                    help="SpMV workloads: x values staged in shared memory (default: built-in)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

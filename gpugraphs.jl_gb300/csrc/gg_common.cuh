@@ -457,6 +457,7 @@ struct gg_mat {
   // SELL-32 plus-times kernel: 0 = register loads (k_sell_hot32), 1 = matrix stream
   // staged by bulk copies (k_sell_tma32)
   int sell_variant = 0;
+  int hot_cols = 0;  // x values staged in shared memory by the register kernels (0: 32768)
 };
 
 namespace gg {

@@ -97,7 +97,8 @@ template <class SR, int CPL>
 __global__ void __launch_bounds__(256)
     k_csr_spmm(SR sr, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colval,
                int64_t row_lo, int64_t nrows, int64_t jlo, int64_t jn, const void* mask, int tmask,
-               const int4* __restrict__ segs, int64_t nseg, typename SR::T* partials) {
+               const int4* __restrict__ segs, int64_t nseg, typename SR::T* partials,
+               int32_t skip_le) {
   typedef typename SR::T T;
   const int lane = threadIdx.x & 31;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(256)
       r = row_lo + (t - nseg);
       k0 = __ldg(rowptr + r) - 1;
       k1 = __ldg(rowptr + r + 1) - 1;
-      if (k1 - k0 > kSegMM) continue;
+      if (k1 - k0 > kSegMM || k1 - k0 <= skip_le) continue;
     }
     if (mask && raw_is_zero(load_raw(mask, tmask, r), tmask)) continue;
     for (int64_t jb = 0; jb < jn; jb += 32 * CPL) {
@@ -221,6 +222,83 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Rows of at most kShortMM entries, plus-times Float32, row-major B and C with
+// 16-byte aligned rows: four rows per warp, 8 lanes per row, each lane owning 4
+// consecutive columns (one float4 of B per entry), so a warp keeps four rows' gathers
+// in flight instead of one.  Each column is still folded in storage order.
+static const int kShortMM = 32;
+
+__global__ void __launch_bounds__(256)
+    k_spmm_short_f32x4(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colval,
+                       const float* __restrict__ nz, const float* __restrict__ B, int64_t ldb,
+                       float* __restrict__ C, int64_t ldc, int64_t row_lo, int64_t nrows,
+                       int64_t jlo, int64_t jn) {
+  const int lane = threadIdx.x & 31;
+  const int grp = lane >> 3, sub = lane & 7;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = gw * 4; base < nrows; base += nw * 4) {
+    const int64_t t = base + grp;
+    if (t >= nrows) continue;
+    const int64_t r = row_lo + t;
+    const int32_t k0 = __ldg(rowptr + r) - 1, k1 = __ldg(rowptr + r + 1) - 1;
+    if (k1 - k0 > kShortMM) continue;
+    for (int64_t jb = 0; jb < jn; jb += 32) {
+      const int64_t j = jlo + jb + 4 * sub;
+      if (jb + 4 * sub >= jn) continue;
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      int32_t k = k0;
+      for (; k + 2 <= k1; k += 2) {
+        const int32_t c0 = __ldg(colval + k) - 1, c1 = __ldg(colval + k + 1) - 1;
+        const float a0 = __ldg(nz + k), a1 = __ldg(nz + k + 1);
+        const float4 b0 = __ldg(reinterpret_cast<const float4*>(B + (int64_t)c0 * ldb + j));
+        const float4 b1 = __ldg(reinterpret_cast<const float4*>(B + (int64_t)c1 * ldb + j));
+        acc.x = __fadd_rn(acc.x, __fmul_rn(a0, b0.x));
+        acc.y = __fadd_rn(acc.y, __fmul_rn(a0, b0.y));
+        acc.z = __fadd_rn(acc.z, __fmul_rn(a0, b0.z));
+        acc.w = __fadd_rn(acc.w, __fmul_rn(a0, b0.w));
+        acc.x = __fadd_rn(acc.x, __fmul_rn(a1, b1.x));
+        acc.y = __fadd_rn(acc.y, __fmul_rn(a1, b1.y));
+        acc.z = __fadd_rn(acc.z, __fmul_rn(a1, b1.z));
+        acc.w = __fadd_rn(acc.w, __fmul_rn(a1, b1.w));
+      }
+      if (k < k1) {
+        const int32_t c0 = __ldg(colval + k) - 1;
+        const float a0 = __ldg(nz + k);
+        const float4 b0 = __ldg(reinterpret_cast<const float4*>(B + (int64_t)c0 * ldb + j));
+        acc.x = __fadd_rn(acc.x, __fmul_rn(a0, b0.x));
+        acc.y = __fadd_rn(acc.y, __fmul_rn(a0, b0.y));
+        acc.z = __fadd_rn(acc.z, __fmul_rn(a0, b0.z));
+        acc.w = __fadd_rn(acc.w, __fmul_rn(a0, b0.w));
+      }
+      *reinterpret_cast<float4*>(C + r * ldc + j) = acc;
+    }
+  }
+}
+
+static int grid_mm(gg_ctx* ctx, int64_t warps);
+
+// which semirings / operands take the short-row kernel
+template <class SR>
+struct ShortRowsMM {
+  static bool ok(const SR&, int64_t, int64_t, const void*) { return false; }
+  static void launch(gg_ctx*, const SR&, const int32_t*, const int32_t*, int64_t, int64_t, int64_t,
+                     int64_t) {}
+};
+template <>
+struct ShortRowsMM<SRPlusTimesF32MM> {
+  static bool ok(const SRPlusTimesF32MM& sr, int64_t jlo, int64_t jn, const void* mask) {
+    const bool aligned = ((uintptr_t)sr.x % 16 == 0) && ((uintptr_t)sr.y % 16 == 0) &&
+                         sr.ldb % 4 == 0 && sr.ldc % 4 == 0;
+    return !mask && aligned && jlo % 4 == 0 && jn % 4 == 0;
+  }
+  static void launch(gg_ctx* ctx, const SRPlusTimesF32MM& sr, const int32_t* rowptr,
+                     const int32_t* colval, int64_t row_lo, int64_t nrows, int64_t jlo, int64_t jn) {
+    k_spmm_short_f32x4<<<grid_mm(ctx, (nrows + 3) / 4), 256, 0, ctx->stream>>>(
+        rowptr, colval, sr.nz, sr.x, sr.ldb, sr.y, sr.ldc, row_lo, nrows, jlo, jn);
+  }
+};
+
 static int grid_mm(gg_ctx* ctx, int64_t warps) {
   int64_t g = (warps * 32 + 255) / 256;
   int64_t cap = (int64_t)ctx->num_sms * 8;
@@ -321,16 +399,27 @@ static int launch_mm(gg_ctx* ctx, gg_mat* A, const SR& sr, int64_t k, const void
     if (A->format == GG_FMT_CSR) {
       const int64_t nrows = row_hi - row_lo;
       const int cpl = A->mm_cpl == 4 && jn >= 128 ? 4 : (A->mm_cpl >= 2 && jn >= 64 ? 2 : 1);
+      // plus-times Float32 on 16-byte aligned row-major operands: rows of <= 32 entries
+      // go to the four-rows-per-warp float4 kernel
+      int32_t skip = 0;
+      if (ShortRowsMM<SR>::ok(sr, jlo, jn, mask)) {
+        skip = kShortMM;
+        ShortRowsMM<SR>::launch(ctx, sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn);
+        trace_count(ctx, 1);
+      }
       tr = trace_main_begin(ctx);
       if (cpl == 4)
         k_csr_spmm<SR, 4><<<grid_mm(ctx, P->nseg + nrows), 256, 0, ctx->stream>>>(
-            sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials);
+            sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials,
+            skip);
       else if (cpl == 2)
         k_csr_spmm<SR, 2><<<grid_mm(ctx, P->nseg + nrows), 256, 0, ctx->stream>>>(
-            sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials);
+            sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials,
+            skip);
       else
         k_csr_spmm<SR, 1><<<grid_mm(ctx, P->nseg + nrows), 256, 0, ctx->stream>>>(
-            sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials);
+            sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials,
+            skip);
     } else {
       int64_t s_lo = 0, s_hi = m;
       if (lo > 0) {

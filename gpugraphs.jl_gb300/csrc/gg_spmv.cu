@@ -461,7 +461,8 @@ __global__ void k_sell_combine(SR sr, const int32_t* __restrict__ perm, int64_t 
 // stage -- one distinct line per cycle, the limit of scattered gathers -- sees only
 // the cold ones.  Same work items and fold order as k_sell.
 // ---------------------------------------------------------------------------------
-static const int kHotCols = 32768;
+static const int kHotCols = 32768;     // default hot x values in shared memory
+static const int kHotColsMax = 53248;  // 208 KB: the most a 1024-thread CTA may stage
 static const int kHotThreads = 1024;
 
 __global__ void __launch_bounds__(kHotThreads, 1)
@@ -1005,13 +1006,15 @@ static int launch_sell_hot(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32& sr,
   GG_CHECK(build_sell_plan(ctx, A));
   SellPlan* P = A->sellplan;
   const int64_t C = A->slice_size;
-  const int hot = (int)std::min<int64_t>(A->n, kHotCols);
+  const int hot_cap = A->hot_cols > 0 ? (A->hot_cols < kHotColsMax ? A->hot_cols : kHotColsMax)
+                                      : kHotCols;
+  const int hot = (int)std::min<int64_t>(A->n, hot_cap);
   static bool attr_set[64] = {false};
   if (ctx->device < 64 && !attr_set[ctx->device]) {
     GG_CUDA(cudaFuncSetAttribute(k_sell_hot, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 kHotCols * (int)sizeof(float)));
+                                 kHotColsMax * (int)sizeof(float)));
     GG_CUDA(cudaFuncSetAttribute(k_sell_hot32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 kHotCols * (int)sizeof(float)));
+                                 kHotColsMax * (int)sizeof(float)));
     attr_set[ctx->device] = true;
   }
   if (P->nitems > 0 && C == 32 && A->sell_variant == 1) {
@@ -1055,7 +1058,11 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
       // plus-times over a large CSR runs on a SELL-32 copy with rows sorted by length
       // (built once; gg_tune may pick another C and sigma): slices of equal-length
       // rows give every thread the same work
-      if (!A->sell_copy) GG_CHECK(gg_sell_create(ctx, A, 32, A->m, &A->sell_copy));
+      if (!A->sell_copy) {
+        GG_CHECK(gg_sell_create(ctx, A, 32, A->m, &A->sell_copy));
+        A->sell_copy->sell_variant = A->sell_variant;  // choices applied before the copy
+        A->sell_copy->hot_cols = A->hot_cols;
+      }
       return spmv_dispatch(ctx, A->sell_copy, tc, mul, add, accum, y, ty, x, tx, mask, tmask, lo, hi);
     }
     GG_CHECK(build_colperm(ctx, A));

@@ -114,7 +114,7 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
     rc = time_median(ctx, &out->spmv_default_ms, run_spmv, &args);
   }
   double best = out->spmv_default_ms;
-  int best_kind = 0, best_rows = 0, best_variant = 0;
+  int best_kind = 0, best_rows = 0, best_variant = 0, best_hot = 32768;
   int64_t best_C = 0, best_sigma = 0;
   gg_mat* best_copy = A->sell_copy;  // the built-in choice's copy (if it made one)
   A->sell_copy = nullptr;
@@ -153,8 +153,14 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
         A->sell_copy = S;
         A->tuned_spmv = 2;
         bool keep = false;
-        for (int variant = (C == 32 ? 1 : 0); variant >= 0 && rc == GG_OK; --variant) {
+        // kernels over the copy: register loads with 32768 or 16384 hot x values in
+        // shared memory, or the bulk-copy staged kernel (SELL-32 only)
+        const int nvar = C == 32 ? 3 : 2;
+        for (int vi = 0; vi < nvar && rc == GG_OK; ++vi) {
+          const int variant = vi == 2 ? 1 : 0;
+          const int hc = vi == 1 ? 16384 : 32768;
           S->sell_variant = variant;
+          S->hot_cols = hc;
           double ms = 0;
           rc = time_median(ctx, &ms, run_spmv, &args);
           if (rc != GG_OK) break;
@@ -165,6 +171,7 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
             best_C = C;
             best_sigma = sg;
             best_variant = variant;
+            best_hot = hc;
             keep = true;
           }
         }
@@ -176,6 +183,7 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
         if (keep) {
           if (best_copy) gg_mat_destroy(best_copy);
           S->sell_variant = best_variant;
+          S->hot_cols = best_hot;
           best_copy = S;
         } else {
           gg_mat_destroy(S);
@@ -199,6 +207,7 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
       out->slice_size = L->slice_size;
       out->sigma = L->sigma;
       out->sell_variant = L->sell_variant;
+      out->hot_cols = L->hot_cols > 0 ? L->hot_cols : 32768;
     } else {
       out->block_rows = kBlockRows;
     }
@@ -217,6 +226,7 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
     out->slice_size = best_C;
     out->sigma = best_sigma;
     out->sell_variant = best_variant;
+    out->hot_cols = best_hot;
   }
   out->spmv_ms = best;
   out->candidates += cand;
@@ -306,6 +316,11 @@ extern "C" int gg_tune_apply(gg_ctx* ctx, gg_mat* A, const gg_tune_result* choic
   if (choice->sell_variant == 0 || choice->sell_variant == 1) {
     A->sell_variant = choice->sell_variant;
     if (A->sell_copy) A->sell_copy->sell_variant = choice->sell_variant;
+  }
+  if (choice->hot_cols > 0) {
+    if (choice->hot_cols > 53248) return set_error(GG_ERR_ARGUMENT, "hot_cols must be at most 53248");
+    A->hot_cols = choice->hot_cols;
+    if (A->sell_copy) A->sell_copy->hot_cols = choice->hot_cols;
   }
   return GG_OK;
 }

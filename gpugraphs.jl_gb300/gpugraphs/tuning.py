@@ -16,7 +16,8 @@ class TuneResult(ctypes.Structure):
                 ("slice_size", ctypes.c_int64), ("sigma", ctypes.c_int64),
                 ("spmv_ms", ctypes.c_double), ("spmv_default_ms", ctypes.c_double),
                 ("mm_cols_per_lane", ctypes.c_int), ("spmm_ms", ctypes.c_double),
-                ("candidates", ctypes.c_int), ("sell_variant", ctypes.c_int)]
+                ("candidates", ctypes.c_int), ("sell_variant", ctypes.c_int),
+                ("hot_cols", ctypes.c_int)]
 
 SELL_VARIANTS = ("registers", "bulk_copy")
 
@@ -38,6 +39,7 @@ def autotune(A, spmm_k=0):
     elif r.spmv_kernel == 2:
         out["slice_size"], out["sigma"] = r.slice_size, r.sigma
         out["sell_variant"] = SELL_VARIANTS[r.sell_variant]
+        out["hot_cols"] = r.hot_cols
     if spmm_k > 0:
         out["spmm_column_tile"] = 32 * r.mm_cols_per_lane
         out["spmm_ms"] = r.spmm_ms
@@ -71,6 +73,7 @@ def apply(A, choice):
     r.sigma = int(choice.get("sigma", 0))
     r.mm_cols_per_lane = int(choice.get("spmm_column_tile", 0)) // 32
     r.sell_variant = SELL_VARIANTS.index(choice["sell_variant"]) if "sell_variant" in choice else -1
+    r.hot_cols = int(choice.get("hot_cols", 0))
     check(L.gg_tune_apply(core.ctx(A.device), A.handle, ctypes.byref(r)), L)
 
 

@@ -361,6 +361,8 @@ typedef struct gg_tune_result {
   int sell_variant;        /* SELL-32 plus-times kernel: 0 = register loads, 1 = matrix stream
                               staged in shared memory by bulk copies (-1 in gg_tune_apply:
                               leave as is) */
+  int hot_cols;            /* most frequent x values staged in shared memory by the register
+                              kernel (0: built-in 32768; at most 53248) */
 } gg_tune_result;
 
 /*
