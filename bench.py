@@ -510,6 +510,51 @@ def cpu_baseline_search(A, kind, s, mcc, levels_full, budget=40):
 
 
 # ---------------------------------------------------------------------------------
+# SpMM: R-MAT scale 22, 32 row-major dense columns
+# ---------------------------------------------------------------------------------
+
+def run_spmm(args):
+    """plus-times Float32 SpMM Y = A X on the R-MAT scale-22 CSR with X of n x 32
+    row-major uniform [0,1) (the SpMM half of the scale-22 configuration).  A step is
+    one gpu_spmm_ call; algorithmic bytes 4(n+1) + 8 nnz + 4nk (X once) + 4nk (Y)."""
+    import torch
+    import gpugraphs as G
+    from gpugraphs import generators as gen
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    A = rmat(22, gen.W_U01_F32, device)
+    n, nnz, k = A.n, A.nnz(), 32
+    X = torch.rand((n, k), dtype=torch.float32, device=device)
+    Y = torch.empty((n, k), dtype=torch.float32, device=device)
+    clk = ClockSampler(local)
+    clk.start()
+    ms = time_steps(lambda: G.gpu_spmm_(Y, A, X), args.steps, warmup=max(args.warmup, 3))
+    clocks = clk.stop()
+    from gpugraphs.tracing import launch_trace
+    with launch_trace(device) as tr:
+        for _ in range(args.steps):
+            G.gpu_spmm_(Y, A, X)
+    B = 4 * (n + 1) + 8 * nnz + 4 * n * k * 2
+    peak, peak_kind = peak_hbm()
+    out = {
+        "metric": "SpMM GB/s (plus-times Float32, CSR, R-MAT scale 22, 32 row-major columns)",
+        "value": round(ws * B / ms / 1e6, 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded R-MAT generator on the device)",
+        "config": {"workload": "spmm_rmat22", "n": n, "nnz": nnz, "k": k, "layout": "row-major",
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": round(B / ms / 1e6, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(B / ms / 1e6 / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                     "algorithmic_bytes": B, "gathered_bytes": nnz * k * 4},
+        "e2e": None, "gpu_launches": tr.launches, "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------------
 # serving: Poisson arrivals over 16 resident graphs, continuous batching
 # ---------------------------------------------------------------------------------
 
@@ -789,6 +834,8 @@ def main():
         if args.steps == 50:
             args.steps = 8
         run_search(args, kind, graph)
+    elif args.workload == "spmm_rmat22":
+        run_spmm(args)
     elif args.workload == "serve":
         run_serve(args)
     elif args.workload == "multigraph":

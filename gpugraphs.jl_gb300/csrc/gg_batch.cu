@@ -142,7 +142,7 @@ static int bb_group(gg_ctx* ctx, int64_t n, const BatchGraph& g, const HubPlan* 
 // batched shortest paths: 32 source columns, lane = source
 // ---------------------------------------------------------------------------------
 template <typename T>
-__global__ void k_bs_init(T* D, int64_t n, const int64_t* src, int64_t S, uint8_t* changed) {
+__global__ void k_bs_init(T* D, int64_t n, const int64_t* src, int64_t S, unsigned* changed) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n * 32;
        t += (int64_t)gridDim.x * blockDim.x)
     D[t] = Lim<T>::max();
@@ -152,11 +152,11 @@ __global__ void k_bs_init(T* D, int64_t n, const int64_t* src, int64_t S, uint8_
 }
 
 template <typename T>
-__global__ void k_bs_seed(T* D, const int64_t* src, int64_t S, uint8_t* changed, int32_t* cq) {
+__global__ void k_bs_seed(T* D, const int64_t* src, int64_t S, unsigned* changed, int32_t* cq) {
   for (int64_t q = threadIdx.x; q < S; q += blockDim.x) {
     const int64_t s = src[q] - 1;
     D[s * 32 + q] = T(0);
-    changed[s] = 1;
+    atomicOr(changed + s, 1u << q);
     cq[q] = (int32_t)s;  // the first round's changed vertices
   }
 }
@@ -176,7 +176,7 @@ __global__ void k_bs_out(const T* D, int64_t n, int64_t S, T* dist, int64_t ld) 
 template <typename T>
 struct BsWork {
   T* D;
-  uint8_t* c[2];
+  unsigned* c[2];  // columns of each vertex that dropped in the previous / this round
   int32_t* cq[2];
   int32_t* vlist;
   unsigned* mark;
@@ -212,7 +212,7 @@ static int bs_group(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
     unsigned long long* ncq_nxt = w.ctr + 1 + (cur ^ 1);
     GG_CUDA(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long), ctx->stream));
     GG_CUDA(cudaMemsetAsync(ncq_nxt, 0, sizeof(unsigned long long), ctx->stream));
-    GG_CUDA(cudaMemsetAsync(w.c[cur ^ 1], 0, (size_t)n, ctx->stream));
+    GG_CUDA(cudaMemsetAsync(w.c[cur ^ 1], 0, (size_t)n * sizeof(unsigned), ctx->stream));
     const bool restricted = nchanged * avg_deg * 4 < nnz;
     if (restricted) {
       GG_CUDA(cudaMemsetAsync(w.mark, 0, ((n + 31) / 32) * sizeof(unsigned), ctx->stream));
@@ -261,10 +261,10 @@ static int sssp_batch_t(gg_ctx* ctx, gg_mat* A, const BatchGraph& g, const int64
   // a hub may enter a changed queue once per piece
   const int64_t qcap = n + hp->npiece + 64;
   BsWork<T> w;
-  uint8_t* c = nullptr;
+  unsigned* c = nullptr;
   int64_t* dsrc = nullptr;
   GG_CUDA(cudaMallocAsync((void**)&w.D, (size_t)n * 32 * sizeof(T), ctx->stream));
-  GG_CUDA(cudaMallocAsync((void**)&c, (size_t)2 * n + 64, ctx->stream));
+  GG_CUDA(cudaMallocAsync((void**)&c, ((size_t)2 * n + 64) * sizeof(unsigned), ctx->stream));
   GG_CUDA(cudaMallocAsync((void**)&w.cq[0], (size_t)qcap * sizeof(int32_t), ctx->stream));
   GG_CUDA(cudaMallocAsync((void**)&w.cq[1], (size_t)qcap * sizeof(int32_t), ctx->stream));
   GG_CUDA(cudaMallocAsync((void**)&w.vlist, (size_t)(n + 64) * sizeof(int32_t), ctx->stream));

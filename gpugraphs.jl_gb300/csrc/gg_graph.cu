@@ -47,6 +47,7 @@ struct GraphAux {
   bool nonneg = false;   // every stored value is >= 0 and not NaN
   PushCSR push[3];       // 0: odd-valued edges, 1: all edges, 2: all edges + weights
   int64_t max_in_deg = -1;  // largest row of the view (-1: not computed yet)
+  double avg_w = -1.0;      // mean stored weight in the distance type (-1: not yet)
 };
 
 void free_graph_aux(gg_mat* A) {
@@ -696,6 +697,7 @@ __global__ void __launch_bounds__(1024)
 static const int kCoopMaxDeg = 64;
 static const int kCoopLo = 1024;   // the single-CTA kernel takes smaller frontiers
 static const int kCoopThreads = 1024;
+static const double kNearFarScale = 8.0;  // near-far band width = this x the mean weight
 
 struct CoopCtl {
   unsigned long long cnt[3];
@@ -834,7 +836,8 @@ struct BfsScratch {
   unsigned* visited;
   unsigned* fb[2];
   int32_t* q[2];
-  int32_t* hq;  // deferred frontier hubs
+  int32_t* hq;  // deferred frontier hubs (the first far list of near-far searches)
+  int32_t* q2;  // the second far list
   Counters* ctr;
   CoopCtl* cc;
 };
@@ -843,7 +846,7 @@ static int bfs_scratch(gg_ctx* ctx, int64_t n, BfsScratch* s) {
   const int64_t nw = (n + 31) / 32 + 1;
   const size_t bm = ((nw * sizeof(unsigned)) + 255) & ~(size_t)255;
   const size_t qb = (((n + 1) * sizeof(int32_t)) + 255) & ~(size_t)255;
-  GG_CHECK(ensure_scratch(ctx, 3 * bm + 3 * qb + 512));
+  GG_CHECK(ensure_scratch(ctx, 3 * bm + 4 * qb + 512));
   char* p = static_cast<char*>(ctx->scratch);
   s->visited = (unsigned*)p;
   s->fb[0] = (unsigned*)(p + bm);
@@ -851,8 +854,9 @@ static int bfs_scratch(gg_ctx* ctx, int64_t n, BfsScratch* s) {
   s->q[0] = (int32_t*)(p + 3 * bm);
   s->q[1] = (int32_t*)(p + 3 * bm + qb);
   s->hq = (int32_t*)(p + 3 * bm + 2 * qb);
-  s->ctr = (Counters*)(p + 3 * bm + 3 * qb);
-  s->cc = (CoopCtl*)(p + 3 * bm + 3 * qb + 256);
+  s->q2 = (int32_t*)(p + 3 * bm + 3 * qb);
+  s->ctr = (Counters*)(p + 3 * bm + 4 * qb);
+  s->cc = (CoopCtl*)(p + 3 * bm + 4 * qb + 256);
   GG_CUDA(cudaMemsetAsync(p, 0, 3 * bm, ctx->stream));
   return GG_OK;
 }
@@ -1364,6 +1368,164 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
   }
 }
 
+// Whole shortest-path search for hub-free graphs in one persistent cooperative
+// launch, near-far ordered: only vertices whose tentative distance is below the
+// threshold thr are relaxed ("near"); improved vertices at or above it wait in the far
+// list; when the near frontier empties, thr grows by delta and the far list is split.
+// On high-diameter graphs with spread weights this avoids most of the repeated
+// relaxations of plain rounds.  The fixpoint is the same (min over paths of the
+// left-folded sums; every improved vertex is relaxed again eventually).  Grid
+// barriers are bounded (coop_grid_sync); the number of steps is bounded by max_steps.
+struct NfCtl {
+  unsigned long long cnt[3];  // near queue lengths, rotating as in CoopCtl
+  unsigned long long fcnt[2];  // far list lengths
+  unsigned bar[4];
+  long long steps_out;
+  int status;  // 1 finished, 2 step budget exhausted
+};
+
+__global__ void k_nf_init(NfCtl* cc, long long nf0) {
+  cc->cnt[0] = 0;
+  cc->cnt[1] = 0;
+  cc->cnt[2] = (unsigned long long)nf0;
+  cc->fcnt[0] = cc->fcnt[1] = 0;
+  cc->bar[0] = cc->bar[1] = cc->bar[2] = cc->bar[3] = 0;
+  cc->steps_out = 0;
+  cc->status = 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kCoopThreads, 1)
+    k_sssp_nearfar(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+                   const T* __restrict__ pw, int32_t* qa, int32_t* qb, int32_t* fa, int32_t* fb,
+                   T* dist, unsigned* inq_a, unsigned* inq_b, unsigned* infar, NfCtl* cc, T delta,
+                   long long max_steps) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+  int32_t* cur = qa;
+  int32_t* nxt = qb;
+  unsigned* icur = inq_a;
+  unsigned* inxt = inq_b;
+  int32_t* far_cur = fa;
+  int32_t* far_nxt = fb;
+  int fc = 0;
+  T thr = delta;
+  for (long long st = 0;; ++st) {
+    const int r = (int)(st % 3);
+    const long long nf = (long long)*((volatile unsigned long long*)&cc->cnt[(r + 2) % 3]);
+    if (st >= max_steps) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        cc->steps_out = st;
+        cc->status = 2;
+      }
+      return;
+    }
+    if (nf == 0) {
+      const long long nfar = (long long)*((volatile unsigned long long*)&cc->fcnt[fc]);
+      if (nfar == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+          cc->steps_out = st;
+          cc->status = 1;
+        }
+        return;
+      }
+      // next distance band: far vertices below the new threshold become the next
+      // frontier (counted and marked like a normal step's output), the others move to
+      // the other far list
+      thr = thr > Lim<T>::max() - delta ? Lim<T>::max() : w_add(thr, delta);
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        cc->cnt[(r + 1) % 3] = 0;
+        cc->fcnt[fc ^ 1] = 0;
+      }
+      for (int64_t i0 = gt - lane; i0 < nfar; i0 += nt) {
+        const int64_t i = i0 + lane;
+        bool to_near = false, to_far = false;
+        int32_t v = 0;
+        if (i < nfar) {
+          v = far_cur[i];
+          if (ld_cg(dist + v) < thr) {
+            atomicAnd(infar + (v >> 5), ~(1u << (v & 31)));
+            const unsigned bit = 1u << (v & 31);
+            to_near = !(atomicOr(inxt + (v >> 5), bit) & bit);
+          } else {
+            to_far = true;
+          }
+        }
+        coop_append(to_near, v, nxt, &cc->cnt[r]);
+        coop_append(to_far, v, far_nxt, &cc->fcnt[fc ^ 1]);
+      }
+      if (!coop_grid_sync(cc->bar, gridDim.x)) return;
+      int32_t* t = cur;
+      cur = nxt;
+      nxt = t;
+      unsigned* tb = icur;
+      icur = inxt;
+      inxt = tb;
+      t = far_cur;
+      far_cur = far_nxt;
+      far_nxt = t;
+      fc ^= 1;
+      continue;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) cc->cnt[(r + 1) % 3] = 0;
+    for (int64_t i0 = gt - lane; i0 < nf; i0 += nt) {
+      const int64_t i = i0 + lane;
+      int32_t k0 = 0, k1 = 0;
+      T du = T(0);
+      if (i < nf) {
+        const int32_t u = cur[i];
+        atomicAnd(icur + (u >> 5), ~(1u << (u & 31)));
+        k0 = __ldg(prow + u);
+        k1 = __ldg(prow + u + 1);
+        du = ld_cg(dist + u);
+      }
+      int32_t dmax = k1 - k0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const int32_t t = __shfl_xor_sync(kFullG, dmax, o);
+        dmax = t > dmax ? t : dmax;
+      }
+      for (int32_t j = 0; j < dmax; ++j) {
+        bool near_add = false, far_add = false;
+        int32_t w = 0;
+        if (k0 + j < k1) {
+          w = __ldg(pcol + k0 + j);
+          const T cand = relax_add(__ldg(pw + k0 + j), du);
+          if (cand < ld_cg(dist + w)) {
+            const T old = atomic_min_t(dist + w, cand);
+            if (cand < old) {
+              const unsigned bit = 1u << (w & 31);
+              if (cand < thr) near_add = !(atomicOr(inxt + (w >> 5), bit) & bit);
+              else far_add = !(atomicOr(infar + (w >> 5), bit) & bit);
+            }
+          }
+        }
+        coop_append(near_add, w, nxt, &cc->cnt[r]);
+        coop_append(far_add, w, far_cur, &cc->fcnt[fc]);
+      }
+    }
+    if (!coop_grid_sync(cc->bar, gridDim.x)) return;
+    int32_t* t = cur;
+    cur = nxt;
+    nxt = t;
+    unsigned* tb = icur;
+    icur = inxt;
+    inxt = tb;
+  }
+}
+
+template <typename T>
+__global__ void k_sum_weights(const T* __restrict__ w, int64_t nnz, double* out) {
+  double s = 0.0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
+       k += (int64_t)gridDim.x * blockDim.x)
+    s += (double)w[k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFullG, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
 // ---------------------------------------------------------------------------------
 // pull rounds for large frontiers: every vertex takes the minimum over its in-edges
 // from vertices that changed in the previous round (membership bitmap chg), in place.
@@ -1513,6 +1675,44 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
     hp = A->hubplan;
   }
   const bool coop_ok = P.max_deg <= kCoopMaxDeg && n >= (1 << 16);
+  if (coop_ok && nf > 0) {
+    // hub-free graph: the whole search in one near-far ordered persistent launch
+    if (g->avg_w < 0) {
+      double* dsum = nullptr;
+      GG_CUDA(cudaMallocAsync((void**)&dsum, sizeof(double), ctx->stream));
+      GG_CUDA(cudaMemsetAsync(dsum, 0, sizeof(double), ctx->stream));
+      k_sum_weights<T><<<gridsz(ctx, P.nnz), 256, 0, ctx->stream>>>(static_cast<const T*>(P.w), P.nnz,
+                                                                    dsum);
+      double hs = 0.0;
+      GG_CUDA(cudaMemcpyAsync(&hs, dsum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      GG_CUDA(cudaStreamSynchronize(ctx->stream));
+      cudaFree(dsum);
+      g->avg_w = P.nnz > 0 ? hs / (double)P.nnz : 1.0;
+    }
+    double dd = g->avg_w * kNearFarScale;
+    if (!(dd > 0.0)) dd = 1.0;
+    T delta = static_cast<T>(dd);
+    if (!(delta > T(0))) delta = T(1);
+    NfCtl* ncc = reinterpret_cast<NfCtl*>(sc.cc);
+    k_nf_init<<<1, 1, 0, ctx->stream>>>(ncc, nf);
+    int32_t* qa = sc.q[cur];
+    int32_t* qb = sc.q[cur ^ 1];
+    unsigned* ia = sc.fb[cur];
+    unsigned* ib = sc.fb[cur ^ 1];
+    const T* pw = static_cast<const T*>(P.w);
+    long long max_steps = 8 * (long long)n + 1024;
+    void* args[] = {&P.rowptr, &P.colval, &pw, &qa, &qb, &sc.hq, &sc.q2, &d, &ia, &ib,
+                    &sc.visited, &ncc, &delta, &max_steps};
+    GG_CUDA(cudaLaunchCooperativeKernel((const void*)k_sssp_nearfar<T>, dim3(ctx->num_sms),
+                                        dim3(kCoopThreads), args, 0, ctx->stream));
+    NfCtl hn;
+    GG_CUDA(cudaMemcpyAsync(&hn, ncc, sizeof(NfCtl), cudaMemcpyDeviceToHost, ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (hn.bar[2]) return set_error(GG_ERR_TIMEOUT, "grid barrier wait ran out");
+    if (hn.status != 1) return set_error(GG_ERR_NOT_CONVERGED, "shortest_path did not converge");
+    if (rounds_out) *rounds_out += hn.steps_out;
+    return GG_OK;
+  }
   const int32_t small_cap = coop_ok ? kCoopLo : kSmallCap;
   const long long coop_hi = n / 8 > kCoopLo ? n / 8 : kCoopLo;
   while (nf > 0) {

@@ -254,38 +254,47 @@ __device__ __forceinline__ T b_weight(const void* nz, int tv, int64_t k) {
 }
 
 // pull over in-edges [k0, k1) of v from in-neighbours that changed last round:
-// per-lane (source column) minimum of D[u] + w
+// per-lane (source column) minimum of D[u] + w.  chg[u] holds the columns of u that
+// dropped in the previous round; only those lanes read D[u], so a vertex whose
+// distances changed for few sources costs few 32-byte sectors.
 template <typename T>
 __device__ __forceinline__ bool bs_pull(const BatchGraph& g, const T* D,
-                                        const uint8_t* __restrict__ chg, int64_t k0, int64_t k1,
+                                        const unsigned* __restrict__ chg, int64_t k0, int64_t k1,
                                         int lane, T& best) {
   bool any = false;
   for (int64_t kb = k0; kb < k1; kb += 32) {
     const int64_t kk = kb + lane;
     int32_t u = -1;
+    unsigned cm = 0;
     if (kk < k1) {
       const int32_t c = __ldg(g.colval + kk) - 1;
-      if (chg[c]) u = c;
+      cm = __ldcg(chg + c);
+      if (cm) u = c;
     }
     unsigned act = __ballot_sync(kFullB, u >= 0);
     while (act) {
       const int src_lane = __ffs(act) - 1;
       act &= act - 1;
       const int32_t uu = __shfl_sync(kFullB, u, src_lane);
-      const T w = b_weight<T>(g.nz, g.tv, kb + src_lane);
-      const T cand = b_relax(w, D[(int64_t)uu * 32 + lane]);
-      if (cand < best) best = cand;
-      any = true;
+      const unsigned m = __shfl_sync(kFullB, cm, src_lane);
+      if ((m >> lane) & 1u) {
+        const T w = b_weight<T>(g.nz, g.tv, kb + src_lane);
+        const T cand = b_relax(w, D[(int64_t)uu * 32 + lane]);
+        if (cand < best) best = cand;
+        any = true;
+      }
     }
   }
   return any;
 }
 
-// Changed-vertex bookkeeping of a round: chg_next[v] = 1 and, when cq is given, v is
-// appended to the changed queue cq (count *ncq) that drives the next round's marking.
-__device__ __forceinline__ void ms_changed(int64_t v, uint8_t* chg_next, unsigned long long* count,
-                                           int32_t* cq, unsigned long long* ncq) {
-  chg_next[v] = 1;
+// Changed-vertex bookkeeping of a round: chg_next[v] gets the columns that dropped and,
+// when cq is given, v is appended to the changed queue cq (count *ncq) that drives the
+// next round's marking.
+__device__ __forceinline__ void ms_changed(int64_t v, unsigned cols, unsigned* chg_next,
+                                           unsigned long long* count, int32_t* cq,
+                                           unsigned long long* ncq) {
+  atomicOr(chg_next + v, cols);
   atomicAdd(count, 1ull);
   if (cq) cq[atomicAdd(ncq, 1ull)] = (int32_t)v;
 }
@@ -296,8 +305,8 @@ __device__ __forceinline__ void ms_changed(int64_t v, uint8_t* chg_next, unsigne
 // Hubs are left to k_ms_round_hub.
 template <typename T>
 __global__ void __launch_bounds__(256)
-    k_ms_round(int64_t n, BatchGraph g, T* D, const uint8_t* __restrict__ chg,
-               uint8_t* chg_next, unsigned long long* count, unsigned* drop,
+    k_ms_round(int64_t n, BatchGraph g, T* D, const unsigned* __restrict__ chg,
+               unsigned* chg_next, unsigned long long* count, unsigned* drop,
                const int32_t* __restrict__ vlist, const unsigned long long* nlist, int32_t* cq,
                unsigned long long* ncq) {
   const int lane = threadIdx.x & 31;
@@ -320,7 +329,7 @@ __global__ void __launch_bounds__(256)
     }
     const unsigned b = __ballot_sync(kFullB, dropped);
     dropped_cols |= b;
-    if (lane == 0 && b) ms_changed(v, chg_next, count, cq, ncq);
+    if (lane == 0 && b) ms_changed(v, b, chg_next, count, cq, ncq);
   }
   if (drop && lane == 0 && dropped_cols) atomicOr(drop, dropped_cols);
 }
@@ -380,8 +389,8 @@ template <> __device__ __forceinline__ double b_atomic_min<double>(double* p, do
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_ms_round_hub(BatchGraph g, const int4* __restrict__ pieces, int64_t npiece,
-                   const int32_t* __restrict__ hubs, T* D, const uint8_t* __restrict__ chg,
-                   uint8_t* chg_next, unsigned long long* count, unsigned* drop,
+                   const int32_t* __restrict__ hubs, T* D, const unsigned* __restrict__ chg,
+                   unsigned* chg_next, unsigned long long* count, unsigned* drop,
                    const unsigned* __restrict__ mark, int32_t* cq, unsigned long long* ncq) {
   const int lane = threadIdx.x & 31;
   unsigned dropped_cols = 0;
@@ -399,7 +408,7 @@ __global__ void __launch_bounds__(256)
     }
     const unsigned b = __ballot_sync(kFullB, dropped);
     dropped_cols |= b;
-    if (lane == 0 && b) ms_changed(v, chg_next, count, cq, ncq);
+    if (lane == 0 && b) ms_changed(v, b, chg_next, count, cq, ncq);
   }
   if (drop && lane == 0 && dropped_cols) atomicOr(drop, dropped_cols);
 }

@@ -127,6 +127,42 @@ __device__ __forceinline__ float4 ld_stream4(const float* p) {
   return r;
 }
 
+// L2 residency hints (createpolicy + .L2::cache_hint): the matrix stream is marked
+// evict-first and the gathered dense operand evict-last, so the operand stays in L2
+// while gigabytes of matrix data flow through it
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_evict_last() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ int32_t ld_stream_p(const int32_t* p, uint64_t pol) {
+  int32_t r;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.s32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ float ld_stream_p(const float* p, uint64_t pol) {
+  float r;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.f32 %0, [%1], %2;" : "=f"(r) : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ float ld_keep(const float* p, uint64_t pol) {
+  float r;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(r) : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ float4 ld_keep4(const float* p, uint64_t pol) {
+  float4 r;
+  asm("ld.global.nc.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+      : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+      : "l"(p), "l"(pol));
+  return r;
+}
+
 // ---------------------------------------------------------------------------------
 // (GPUGraphs_mul, GPUGraphs_add, GPUGraphs_second) on Float32: the headline SpMV.
 // The early exit at +Inf follows monoid_absorb(Float32, GPUGraphs_add) (algebra.jl:45).

@@ -96,11 +96,11 @@ __global__ void k_ss_admit(int64_t n, T* D, unsigned qmask) {
       if ((qmask >> q) & 1u) D[v * kColSlots + q] = Lim<T>::max();
 }
 template <typename T>
-__global__ void k_ss_seed(T* D, uint8_t* chg, const int* slots, const int64_t* srcs, int nslots,
+__global__ void k_ss_seed(T* D, unsigned* chg, const int* slots, const int64_t* srcs, int nslots,
                           int32_t* cq, unsigned long long* ncq) {
   for (int i = threadIdx.x; i < nslots; i += blockDim.x) {
     D[srcs[i] * kColSlots + slots[i]] = T(0);
-    chg[srcs[i]] = 1;
+    atomicOr(chg + srcs[i], 1u << slots[i]);
     cq[atomicAdd(ncq, 1ull)] = (int32_t)srcs[i];  // changed for the next round's marking
   }
 }
@@ -161,7 +161,7 @@ struct Executor {
   unsigned act_host[kBfsW] = {0};  // sources whose frontier is not empty
   // SSSP
   void* D = nullptr;
-  uint8_t *c0 = nullptr, *c1 = nullptr;
+  unsigned *c0 = nullptr, *c1 = nullptr;  // columns of each vertex that dropped
   // frontier-restricted rounds: changed queues, marked vertices (gg_msearch.cuh)
   int32_t* cq[2] = {nullptr, nullptr};
   int32_t* vlist = nullptr;
@@ -237,7 +237,8 @@ static int grid_s(gg_server* S, int64_t work) {
 static size_t exec_bytes(int kind, int64_t n, int dtype) {
   switch (kind) {
     case GG_QUERY_BFS: return (size_t)n * kBfsW * 4 * 3 + 4096;
-    case GG_QUERY_SSSP: return (size_t)n * kColSlots * dtype_size(dtype) + 2 * (size_t)n + 4096;
+    // distances, changed-column masks (2 x 4n), changed queues and marks (~12n)
+    case GG_QUERY_SSSP: return (size_t)n * kColSlots * dtype_size(dtype) + 20 * (size_t)n + 4096;
     default: return (size_t)n * kColSlots * 4 * 2 + 4096;
   }
 }
@@ -333,10 +334,10 @@ static int exec_create(gg_server* S, int gi, int kind, Executor& E) {
     GG_CUDA(cudaMemsetAsync(E.outp, 0, kBfsSlots * sizeof(int32_t*), st));
   } else if (kind == GG_QUERY_SSSP) {
     GG_CUDA(cudaMalloc(&E.D, (size_t)n * kColSlots * dtype_size(dt)));
-    GG_CUDA(cudaMalloc((void**)&E.c0, (size_t)n + 64));
-    GG_CUDA(cudaMalloc((void**)&E.c1, (size_t)n + 64));
-    GG_CUDA(cudaMemsetAsync(E.c0, 0, (size_t)n + 64, st));
-    GG_CUDA(cudaMemsetAsync(E.c1, 0, (size_t)n + 64, st));
+    GG_CUDA(cudaMalloc((void**)&E.c0, ((size_t)n + 64) * sizeof(unsigned)));
+    GG_CUDA(cudaMalloc((void**)&E.c1, ((size_t)n + 64) * sizeof(unsigned)));
+    GG_CUDA(cudaMemsetAsync(E.c0, 0, ((size_t)n + 64) * sizeof(unsigned), st));
+    GG_CUDA(cudaMemsetAsync(E.c1, 0, ((size_t)n + 64) * sizeof(unsigned), st));
     const HubPlan* hp = S->graphs[gi]->hubplan;
     const int64_t qcap = n + hp->npiece + kColSlots + 64;  // a hub may be queued once per piece
     GG_CUDA(cudaMalloc((void**)&E.cq[0], qcap * sizeof(int32_t)));
@@ -500,7 +501,7 @@ static int exec_tick(gg_server* S, int gi, Executor& E) {
     GG_CUDA(cudaMemcpyAsync(E.h_result, E.act + kBfsW, kBfsW * 4, cudaMemcpyDeviceToHost, st));
   } else if (E.kind == GG_QUERY_SSSP) {
     GG_CUDA(cudaMemsetAsync(E.d_amask, 0, 4, st));  // dropped columns of this round
-    GG_CUDA(cudaMemsetAsync(E.c1, 0, (size_t)n, st));
+    GG_CUDA(cudaMemsetAsync(E.c1, 0, (size_t)n * sizeof(unsigned), st));
     const int64_t nnz = S->graphs[gi]->nnz;
     switch (E.dtype) {
       case GG_INT32: ss_round<int32_t>(S, E, sg, hp, nnz); break;

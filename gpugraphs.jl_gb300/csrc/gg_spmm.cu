@@ -28,8 +28,10 @@ struct SRPlusTimesF32MM {
   int64_t ldb, ldc;
   __device__ __forceinline__ T neutral() const { return 0.0f; }
   __device__ __forceinline__ bool is_absorb(T a) const { return a == __int_as_float(0x7f800000); }
+  // the matrix stream evicts first, the gathered rows of B stay in L2
   __device__ __forceinline__ T mulk(int64_t k, int32_t col1, int64_t, int64_t j) const {
-    return __fmul_rn(__ldg(nz + k), __ldg(x + (int64_t)(col1 - 1) * ldb + j));
+    return __fmul_rn(ld_stream_p(nz + k, l2_evict_first()),
+                     ld_keep(x + (int64_t)(col1 - 1) * ldb + j, l2_evict_last()));
   }
   __device__ __forceinline__ T addv(T acc, T v) const { return __fadd_rn(acc, v); }
   __device__ __forceinline__ void write_mm(int64_t row0, int64_t j, T acc) const {
@@ -235,6 +237,7 @@ __global__ void __launch_bounds__(256)
                        int64_t jlo, int64_t jn) {
   const int lane = threadIdx.x & 31;
   const int grp = lane >> 3, sub = lane & 7;
+  const uint64_t pol_s = l2_evict_first(), pol_b = l2_evict_last();
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t base = gw * 4; base < nrows; base += nw * 4) {
@@ -249,10 +252,10 @@ __global__ void __launch_bounds__(256)
       float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
       int32_t k = k0;
       for (; k + 2 <= k1; k += 2) {
-        const int32_t c0 = __ldg(colval + k) - 1, c1 = __ldg(colval + k + 1) - 1;
-        const float a0 = __ldg(nz + k), a1 = __ldg(nz + k + 1);
-        const float4 b0 = __ldg(reinterpret_cast<const float4*>(B + (int64_t)c0 * ldb + j));
-        const float4 b1 = __ldg(reinterpret_cast<const float4*>(B + (int64_t)c1 * ldb + j));
+        const int32_t c0 = ld_stream_p(colval + k, pol_s) - 1, c1 = ld_stream_p(colval + k + 1, pol_s) - 1;
+        const float a0 = ld_stream_p(nz + k, pol_s), a1 = ld_stream_p(nz + k + 1, pol_s);
+        const float4 b0 = ld_keep4(B + (int64_t)c0 * ldb + j, pol_b);
+        const float4 b1 = ld_keep4(B + (int64_t)c1 * ldb + j, pol_b);
         acc.x = __fadd_rn(acc.x, __fmul_rn(a0, b0.x));
         acc.y = __fadd_rn(acc.y, __fmul_rn(a0, b0.y));
         acc.z = __fadd_rn(acc.z, __fmul_rn(a0, b0.z));
@@ -263,9 +266,9 @@ __global__ void __launch_bounds__(256)
         acc.w = __fadd_rn(acc.w, __fmul_rn(a1, b1.w));
       }
       if (k < k1) {
-        const int32_t c0 = __ldg(colval + k) - 1;
-        const float a0 = __ldg(nz + k);
-        const float4 b0 = __ldg(reinterpret_cast<const float4*>(B + (int64_t)c0 * ldb + j));
+        const int32_t c0 = ld_stream_p(colval + k, pol_s) - 1;
+        const float a0 = ld_stream_p(nz + k, pol_s);
+        const float4 b0 = ld_keep4(B + (int64_t)c0 * ldb + j, pol_b);
         acc.x = __fadd_rn(acc.x, __fmul_rn(a0, b0.x));
         acc.y = __fadd_rn(acc.y, __fmul_rn(a0, b0.y));
         acc.z = __fadd_rn(acc.z, __fmul_rn(a0, b0.z));
@@ -401,7 +404,7 @@ static int launch_mm(gg_ctx* ctx, gg_mat* A, const SR& sr, int64_t k, const void
       const int cpl = A->mm_cpl == 4 && jn >= 128 ? 4 : (A->mm_cpl >= 2 && jn >= 64 ? 2 : 1);
       // plus-times Float32 on 16-byte aligned row-major operands: rows of <= 32 entries
       // go to the four-rows-per-warp float4 kernel
-      int32_t skip = 0;
+      int32_t skip = -1;  // rows of at most `skip` entries are left to the short-row kernel
       if (ShortRowsMM<SR>::ok(sr, jlo, jn, mask)) {
         skip = kShortMM;
         ShortRowsMM<SR>::launch(ctx, sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn);

@@ -907,6 +907,7 @@ __global__ void __launch_bounds__(kHotThreads, 1)
   extern __shared__ float sx[];
   for (int i = threadIdx.x; i < hot; i += blockDim.x) sx[i] = __ldg(xr + i);
   __syncthreads();
+  const uint64_t pol_s = l2_evict_first(), pol_x = l2_evict_last();
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -926,15 +927,15 @@ __global__ void __launch_bounds__(kHotThreads, 1)
 #pragma unroll
       for (int u = 0; u < kNarrowCols; ++u) {
         const bool in = u < total;
-        c[u] = in ? ld_stream(colval + d.x + u * 32 + lane) : -1;
-        a[u] = in ? ld_stream(nz + d.x + u * 32 + lane) : 0.0f;
+        c[u] = in ? ld_stream_p(colval + d.x + u * 32 + lane, pol_s) : -1;
+        a[u] = in ? ld_stream_p(nz + d.x + u * 32 + lane, pol_s) : 0.0f;
       }
       float p[kNarrowCols];
 #pragma unroll
       for (int u = 0; u < kNarrowCols; ++u) {
         const int32_t col = c[u];
         float xv = 0.0f;
-        if (col > 0) xv = col <= hot ? sx[col - 1] : __ldg(xr + (col - 1));
+        if (col > 0) xv = col <= hot ? sx[col - 1] : ld_keep(xr + (col - 1), pol_x);
         p[u] = __fmul_rn(a[u], xv);
       }
       int u0 = 0;
@@ -964,8 +965,8 @@ __global__ void __launch_bounds__(kHotThreads, 1)
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const bool in = live && u < d.z;
-      c[u] = in ? ld_stream(colval + pos + u * 32) : -1;
-      a[u] = in ? ld_stream(nz + pos + u * 32) : 0.0f;
+      c[u] = in ? ld_stream_p(colval + pos + u * 32, pol_s) : -1;
+      a[u] = in ? ld_stream_p(nz + pos + u * 32, pol_s) : 0.0f;
     }
     for (int32_t j = 0; j < d.z; j += 8) {
       const int32_t pn = pos + 8 * 32;
@@ -974,15 +975,15 @@ __global__ void __launch_bounds__(kHotThreads, 1)
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const bool in = live && j + 8 + u < d.z;
-        cn[u] = in ? ld_stream(colval + pn + u * 32) : -1;
-        an[u] = in ? ld_stream(nz + pn + u * 32) : 0.0f;
+        cn[u] = in ? ld_stream_p(colval + pn + u * 32, pol_s) : -1;
+        an[u] = in ? ld_stream_p(nz + pn + u * 32, pol_s) : 0.0f;
       }
       float p[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int32_t col = c[u];
         float xv = 0.0f;
-        if (col > 0) xv = col <= hot ? sx[col - 1] : __ldg(xr + (col - 1));
+        if (col > 0) xv = col <= hot ? sx[col - 1] : ld_keep(xr + (col - 1), pol_x);
         p[u] = __fmul_rn(a[u], xv);
       }
 #pragma unroll

@@ -256,3 +256,22 @@ def test_generators_match_oracle():
     rp, cv, nz = O.coo_to_csr(1500, s, d, w, symmetrize=False, drop_loops=False)
     grp, gcv, gnz = csr_host(E)
     assert (grp == rp).all() and (gcv == cv).all() and (gnz == nz).all()
+
+
+@pytest.mark.parametrize("wkind", [gen.W_F32_1_10, gen.W_INT_1_255])
+def test_grid_persistent_paths_exact(wkind):
+    """Grids of >= 65536 vertices (out-degree <= 4) run BFS levels through the
+    persistent cooperative kernel and shortest paths as one near-far ordered
+    persistent search: both equal the oracle exactly."""
+    A = gen.grid(300, 250, seed=61, wkind=wkind)
+    rp, cv, nz = csr_host(A)
+    for s in (1, 37000, 75000):
+        ref, _ = O.sssp(A.n, rp, cv, nz, [s])
+        got = host(G.shortest_path(A, s))
+        assert (got == ref[:, 0]).all(), s
+    P = G.SparseGPUMatrixCSR(A.m, A.n, A.rowptr, A.colval,
+                             torch.ones(A.nnz(), dtype=torch.bool, device="cuda"))
+    pr, pc, pn = csr_host(P)
+    for s in (1, 40000):
+        lv, _ = O.bfs_levels(A.n, pr, pc, pn, s)
+        assert (host(G.bfs_distances(P, s)) == lv).all(), s

@@ -397,12 +397,13 @@ def test_spmm_long_rows_power_law():
             Bl = np.asfortranarray(Bf) if layout == 0 else np.ascontiguousarray(Bf)
             Co = np.zeros((m, k), np.float32, order="F" if layout == 0 else "C")
             O.csr_spmm(m, rowptr, colval, nzval, Co, Bl, layout=layout)
+            # C starts as NaN: every row (the 20% empty ones too) must be written
             if layout == 0:
                 Bd = torch.from_numpy(np.ascontiguousarray(Bf.T)).cuda().T
-                Cd = torch.zeros((k, m), dtype=torch.float32, device="cuda").T
+                Cd = torch.full((k, m), float("nan"), dtype=torch.float32, device="cuda").T
             else:
                 Bd = dev(Bf)
-                Cd = torch.zeros((m, k), dtype=torch.float32, device="cuda")
+                Cd = torch.full((m, k), float("nan"), dtype=torch.float32, device="cuda")
             for rep in range(2):
                 G.gpu_spmm_(Cd, M, Bd)
                 Ch = host(Cd)
@@ -498,3 +499,23 @@ def test_spmv_plus_times_large_csr_sorted_sell_path():
             first = yh
         else:
             assert (yh == first).all()
+
+
+@pytest.mark.parametrize("k", [1, 4, 6, 32])
+def test_spmm_writes_every_row(k):
+    """Row-major plus-times SpMM with 20% empty rows into a NaN-filled C: every row is
+    written (empty rows get the neutral 0), for column counts on and off the
+    four-column kernel's alignment."""
+    m = 2000
+    rowptr, colval, nzval, A = power_law_csr(m, 12)
+    B = np.random.default_rng(k).random((m, k), dtype=np.float32)
+    Co = np.zeros((m, k), np.float32)
+    O.csr_spmm(m, rowptr, colval, nzval, Co, B, layout=1)
+    M = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nzval)
+    Cd = torch.full((m, k), float("nan"), dtype=torch.float32, device="cuda")
+    G.gpu_spmm_(Cd, M, dev(B))
+    Ch = host(Cd)
+    assert not np.isnan(Ch).any()
+    short = np.diff(rowptr) <= SEG_MM
+    assert (Ch[short] == Co[short]).all()
+    np.testing.assert_allclose(Ch, Co, rtol=1e-4, atol=1e-4)
