@@ -199,6 +199,7 @@ static void free_mat_storage(gg_mat* A) {
     cudaFree(A->mmplan->segs);
     cudaFree(A->mmplan->first);
     cudaFree(A->mmplan->rows);
+    cudaFree(A->mmplan->items);
     delete A->mmplan;
     A->mmplan = nullptr;
   }

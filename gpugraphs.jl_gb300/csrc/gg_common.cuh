@@ -356,6 +356,10 @@ struct MMPlan {
   int4* segs = nullptr;
   int32_t* first = nullptr;
   int32_t* rows = nullptr;
+  // CSR: the work of the Float32 item kernel -- every piece (as in segs) and every row
+  // of 33..kSegMM entries as (row, first entry, end entry, -1), longest first
+  int4* items = nullptr;
+  int64_t nitems = 0;
 };
 static const int kSegMM = 256;
 

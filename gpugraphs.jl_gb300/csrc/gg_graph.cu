@@ -814,6 +814,76 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
   }
 }
 
+// BFS levels of hub-free graphs on one thread-block cluster: kClusterCtas CTAs (8 SMs)
+// run level after level separated by the cluster barrier (barrier.cluster, a hardware
+// barrier: no polling), which costs far less than a grid barrier over every SM.  It
+// serves the long tail of small frontiers of high-diameter graphs (a 4096 x 4096 grid
+// has 7439 levels of at most ~8000 vertices); it exits when the frontier is empty or
+// larger than cap.  Same counters, queues and semantics as k_bfs_coop.
+static const int kClusterCtas = 8;
+static const long long kClusterCap = 65536;
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
+
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kCoopThreads, 1)
+    k_bfs_cluster(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol, int32_t* qa,
+                  int32_t* qb, unsigned* visited, int32_t* dist, CoopCtl* cc, int32_t level0,
+                  long long cap) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+  int32_t* cur = qa;
+  int32_t* nxt = qb;
+  for (int st = 0;; ++st) {
+    const int r = st % 3;
+    const long long nf = (long long)*((volatile unsigned long long*)&cc->cnt[(r + 2) % 3]);
+    if (nf == 0 || nf > cap) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        cc->nf_out = nf;
+        cc->level_out = level0 + st;
+        cc->which_out = st & 1;
+      }
+      return;  // every CTA of the cluster reads the same nf and leaves here
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) cc->cnt[(r + 1) % 3] = 0;
+    const int32_t level = level0 + st + 1;
+    for (int64_t i0 = gt - lane; i0 < nf; i0 += nt) {
+      const int64_t i = i0 + lane;
+      int32_t k0 = 0, k1 = 0;
+      if (i < nf) {
+        const int32_t u = cur[i];
+        k0 = __ldg(prow + u);
+        k1 = __ldg(prow + u + 1);
+      }
+      int32_t dmax = k1 - k0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const int32_t t = __shfl_xor_sync(kFullG, dmax, o);
+        dmax = t > dmax ? t : dmax;
+      }
+      for (int32_t j = 0; j < dmax; ++j) {
+        bool claim = false;
+        int32_t w = 0;
+        if (k0 + j < k1) {
+          w = __ldg(pcol + k0 + j);
+          const unsigned bit = 1u << (w & 31);
+          if (!(__ldcg(visited + (w >> 5)) & bit)) claim = !(atomicOr(visited + (w >> 5), bit) & bit);
+          if (claim) dist[w] = level;
+        }
+        coop_append(claim, w, nxt, &cc->cnt[r]);
+      }
+    }
+    __threadfence();
+    cluster_barrier();
+    int32_t* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+}
+
 // sum of out-degrees of a frontier queue (direction heuristic after the small kernel)
 __global__ void k_queue_degree(const int32_t* __restrict__ prow, const int32_t* __restrict__ q,
                                int64_t nf, Counters* ctr) {
@@ -897,6 +967,49 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
   const long long coop_hi = n / 24 > kCoopLo ? n / 24 : kCoopLo;
   CoopCtl* hc = reinterpret_cast<CoopCtl*>(ctx->h_flags);
   while (nf > 0) {
+    if (coop_ok && !pull && nf <= kClusterCap) {
+      // small and medium frontiers of hub-free graphs: one cluster, cluster barriers
+      k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf);
+      k_bfs_cluster<<<kClusterCtas, kCoopThreads, 0, ctx->stream>>>(
+          P.rowptr, P.colval, sc.q[cur], sc.q[cur ^ 1], sc.visited, dist, sc.cc, (int32_t)level,
+          kClusterCap);
+      GG_CUDA(cudaGetLastError());
+      GG_CUDA(cudaMemcpyAsync(hc, sc.cc, sizeof(CoopCtl), cudaMemcpyDeviceToHost, ctx->stream));
+      GG_CUDA(cudaStreamSynchronize(ctx->stream));
+      nf = hc->nf_out;
+      level = hc->level_out;
+      if (hc->which_out) cur ^= 1;
+      if (nf == 0) break;
+      GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+      k_queue_degree<<<gridsz(ctx, nf), 256, 0, ctx->stream>>>(P.rowptr, sc.q[cur], nf, sc.ctr);
+      GG_CUDA(cudaMemcpyAsync(ctx->h_flags, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+      GG_CUDA(cudaStreamSynchronize(ctx->stream));
+      mf = (int64_t)reinterpret_cast<Counters*>(ctx->h_flags)->mf;
+      hc = reinterpret_cast<CoopCtl*>(ctx->h_flags);
+      if (nf <= coop_hi) {
+        // larger frontier: the grid-wide persistent kernel takes it from here
+        k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf);
+        int32_t* qa = sc.q[cur];
+        int32_t* qb = sc.q[cur ^ 1];
+        int32_t lv0 = (int32_t)level;
+        long long lo = kClusterCap / 2, hi = coop_hi;
+        void* args[] = {&P.rowptr, &P.colval, &qa, &qb, &sc.visited, &dist, &sc.cc, &lv0, &lo, &hi};
+        GG_CHECK(coop_launch(ctx, (const void*)k_bfs_coop, args, sc.cc, hc));
+        nf = hc->nf_out;
+        level = hc->level_out;
+        if (hc->which_out) cur ^= 1;
+        if (nf == 0) break;
+        if (nf <= kClusterCap) continue;
+        GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
+        k_queue_degree<<<gridsz(ctx, nf), 256, 0, ctx->stream>>>(P.rowptr, sc.q[cur], nf, sc.ctr);
+        GG_CUDA(cudaMemcpyAsync(ctx->h_flags, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        GG_CUDA(cudaStreamSynchronize(ctx->stream));
+        mf = (int64_t)reinterpret_cast<Counters*>(ctx->h_flags)->mf;
+      }
+      // frontier above the persistent kernels' range: push / pull levels below
+    }
     if (coop_ok && !pull && nf > small_cap && nf <= coop_hi) {
       k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf);
       int32_t* qa = sc.q[cur];

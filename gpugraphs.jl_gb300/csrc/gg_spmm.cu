@@ -11,6 +11,7 @@
 // associative monoid, within rounding for Float32/Float64 sums.
 // With a row-major dense operand (the batched-query layout) each gathered B row is
 // one contiguous 128-byte read.
+#include <algorithm>
 #include <vector>
 
 #include "gg_semiring.cuh"
@@ -279,6 +280,60 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Rows of 33..kSegMM entries and the pieces of longer rows, plus-times Float32 on
+// row-major operands: one warp per item (longest first), lane = dense column.  The
+// warp reads 32 column / value pairs with one coalesced load each, then issues 16
+// gathers of B rows before folding them in storage order, with no per-entry test of
+// the absorbing value; a column whose sum ends NaN is folded again with the
+// reference's stop at +Inf (CSR.jl:49-51), so results equal the sequential fold.
+__global__ void __launch_bounds__(256)
+    k_spmm_items_f32(const int32_t* __restrict__ colval, const float* __restrict__ nz,
+                     const float* __restrict__ B, int64_t ldb, float* __restrict__ C, int64_t ldc,
+                     const int4* __restrict__ items, int64_t nitems, int64_t row_lo, int64_t row_hi,
+                     int64_t jlo, int64_t jn, float* partials) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t pol_s = l2_evict_first(), pol_b = l2_evict_last();
+  for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < nitems;
+       it += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int4 d = items[it];  // row, first entry, end entry, partial slot or -1
+    if (d.x < row_lo || d.x >= row_hi) continue;
+    for (int64_t jb = 0; jb < jn; jb += 32) {
+      const int64_t jj = jb + lane;
+      const bool active = jj < jn;
+      const float* Bj = B + jlo + (active ? jj : 0);
+      float acc = 0.0f;
+      for (int32_t base = d.y; base < d.z; base += 32) {
+        const int32_t kk = base + lane;
+        const int32_t c_l = kk < d.z ? ld_stream_p(colval + kk, pol_s) - 1 : 0;
+        const float a_l = kk < d.z ? ld_stream_p(nz + kk, pol_s) : 0.0f;
+        const int nb = d.z - base < 32 ? d.z - base : 32;
+        for (int i0 = 0; i0 < nb; i0 += 16) {
+          float bv[16], av[16];
+#pragma unroll
+          for (int u = 0; u < 16; ++u) {
+            const int c = __shfl_sync(0xffffffffu, c_l, (i0 + u) & 31);
+            av[u] = __shfl_sync(0xffffffffu, a_l, (i0 + u) & 31);
+            bv[u] = (i0 + u < nb) ? ld_keep(Bj + (int64_t)c * ldb, pol_b) : 0.0f;
+          }
+#pragma unroll
+          for (int u = 0; u < 16; ++u)
+            if (i0 + u < nb) acc = __fadd_rn(acc, __fmul_rn(av[u], bv[u]));
+        }
+      }
+      if (acc != acc) {  // NaN: fold again with the stop at +Inf
+        acc = 0.0f;
+        for (int32_t k = d.y; k < d.z; ++k) {
+          acc = __fadd_rn(acc, __fmul_rn(__ldg(nz + k), __ldg(Bj + (int64_t)(__ldg(colval + k) - 1) * ldb)));
+          if (acc == __int_as_float(0x7f800000)) break;
+        }
+      }
+      if (!active) continue;
+      if (d.w < 0) C[(int64_t)d.x * ldc + jlo + jj] = acc;
+      else partials[(int64_t)d.w * jn + jj] = acc;
+    }
+  }
+}
+
 static int grid_mm(gg_ctx* ctx, int64_t warps);
 
 // which semirings / operands take the short-row kernel
@@ -287,6 +342,8 @@ struct ShortRowsMM {
   static bool ok(const SR&, int64_t, int64_t, const void*) { return false; }
   static void launch(gg_ctx*, const SR&, const int32_t*, const int32_t*, int64_t, int64_t, int64_t,
                      int64_t) {}
+  static void launch_items(gg_ctx*, const SR&, const int32_t*, const MMPlan*, int64_t, int64_t,
+                           int64_t, int64_t, typename SR::T*) {}
 };
 template <>
 struct ShortRowsMM<SRPlusTimesF32MM> {
@@ -300,6 +357,13 @@ struct ShortRowsMM<SRPlusTimesF32MM> {
     k_spmm_short_f32x4<<<grid_mm(ctx, (nrows + 3) / 4), 256, 0, ctx->stream>>>(
         rowptr, colval, sr.nz, sr.x, sr.ldb, sr.y, sr.ldc, row_lo, nrows, jlo, jn);
   }
+  static void launch_items(gg_ctx* ctx, const SRPlusTimesF32MM& sr, const int32_t* colval,
+                           const MMPlan* P, int64_t row_lo, int64_t row_hi, int64_t jlo, int64_t jn,
+                           float* partials) {
+    k_spmm_items_f32<<<grid_mm(ctx, P->nitems), 256, 0, ctx->stream>>>(
+        colval, sr.nz, sr.x, sr.ldb, sr.y, sr.ldc, P->items, P->nitems, row_lo, row_hi, jlo, jn,
+        partials);
+  }
 };
 
 static int grid_mm(gg_ctx* ctx, int64_t warps) {
@@ -312,7 +376,7 @@ static int grid_mm(gg_ctx* ctx, int64_t warps) {
 // long-row pieces, built once per matrix from rowptr (CSR) or slice_ptr (SELL)
 static int build_mm_plan(gg_ctx* ctx, gg_mat* A) {
   if (A->mmplan) return GG_OK;
-  std::vector<int4> segs;
+  std::vector<int4> segs, items;
   std::vector<int32_t> first, rows;
   if (A->format == GG_FMT_CSR) {
     const int64_t m = A->m;
@@ -322,6 +386,7 @@ static int build_mm_plan(gg_ctx* ctx, gg_mat* A) {
     GG_CUDA(cudaStreamSynchronize(ctx->stream));
     for (int64_t r = 0; r < m; ++r) {
       const int64_t k0 = rp[r] - 1, k1 = rp[r + 1] - 1;
+      if (k1 - k0 > kShortMM && k1 - k0 <= kSegMM) items.push_back(make_int4((int)r, (int)k0, (int)k1, -1));
       if (k1 - k0 <= kSegMM) continue;
       rows.push_back((int32_t)r);
       first.push_back((int32_t)segs.size());
@@ -351,7 +416,11 @@ static int build_mm_plan(gg_ctx* ctx, gg_mat* A) {
     }
   }
   first.push_back((int32_t)segs.size());
+  items.insert(items.end(), segs.begin(), segs.end());
+  std::stable_sort(items.begin(), items.end(),
+                   [](const int4& a, const int4& b) { return (a.z - a.y) > (b.z - b.y); });
   MMPlan* P = new MMPlan();
+  P->nitems = A->format == GG_FMT_CSR ? (int64_t)items.size() : 0;
   P->nseg = (int64_t)segs.size();
   P->nlong = (int64_t)rows.size();
   cudaError_t e = cudaSuccess;
@@ -364,11 +433,13 @@ static int build_mm_plan(gg_ctx* ctx, gg_mat* A) {
   up((void**)&P->segs, segs.data(), segs.size() * sizeof(int4));
   up((void**)&P->first, first.data(), first.size() * sizeof(int32_t));
   up((void**)&P->rows, rows.data(), rows.size() * sizeof(int32_t));
+  up((void**)&P->items, items.data(), (size_t)P->nitems * sizeof(int4));
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     cudaFree(P->segs);
     cudaFree(P->first);
     cudaFree(P->rows);
+    cudaFree(P->items);
     delete P;
     return cuda_error(e, "SpMM long-row analysis");
   }
@@ -406,10 +477,14 @@ static int launch_mm(gg_ctx* ctx, gg_mat* A, const SR& sr, int64_t k, const void
       // go to the four-rows-per-warp float4 kernel
       int32_t skip = -1;  // rows of at most `skip` entries are left to the short-row kernel
       if (ShortRowsMM<SR>::ok(sr, jlo, jn, mask)) {
-        skip = kShortMM;
+        // Float32 fast path: short rows four per warp, the rest (medium rows and the
+        // pieces of long rows) by the item kernel
         ShortRowsMM<SR>::launch(ctx, sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn);
         trace_count(ctx, 1);
-      }
+        tr = trace_main_begin(ctx);
+        if (P->nitems > 0)
+          ShortRowsMM<SR>::launch_items(ctx, sr, A->colval, P, row_lo, row_hi, jlo, jn, partials);
+      } else {
       tr = trace_main_begin(ctx);
       if (cpl == 4)
         k_csr_spmm<SR, 4><<<grid_mm(ctx, P->nseg + nrows), 256, 0, ctx->stream>>>(
@@ -423,6 +498,7 @@ static int launch_mm(gg_ctx* ctx, gg_mat* A, const SR& sr, int64_t k, const void
         k_csr_spmm<SR, 1><<<grid_mm(ctx, P->nseg + nrows), 256, 0, ctx->stream>>>(
             sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn, mask, tmask, P->segs, P->nseg, partials,
             skip);
+      }
     } else {
       int64_t s_lo = 0, s_hi = m;
       if (lo > 0) {
