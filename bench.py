@@ -259,13 +259,17 @@ def run_spmv_rmat(args, scale=22):
         dist.init_process_group("nccl", device_id=device)
     A = rmat(scale, gen.W_U01_F32, device)
     x = gen.uniform_vector(A.n, seed=2, device=device)
-    if args.sell_variant or args.hot_cols:
+    if args.sell_variant or args.hot_cols or args.layout == "sell":
         from gpugraphs import tuning
+        tuning.apply(A, {"spmv_kernel": "sell", "slice_size": 32, "sigma": A.m})
         G.gpu_spmv_(torch.zeros(A.n, device=device), A, x)  # builds the SELL-32 copy
         choice = {"sell_variant": args.sell_variant or "registers"}
         if args.hot_cols:
             choice["hot_cols"] = args.hot_cols
         tuning.apply(A, choice)
+    if args.layout == "window_tiles":
+        from gpugraphs import tuning
+        tuning.apply(A, {"spmv_kernel": "window_tiles"})
     n, nnz = A.n, A.nnz()
     y = torch.zeros(n, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
@@ -335,6 +339,14 @@ def run_spmv_rmat(args, scale=22):
     e2e_val = ws * B / (float(e2e_t.item()) * 1e-3) / 1e9
 
     ok = spot_check(A, x, y)
+    layout = G.spmv_layout(A)
+    if layout == "window_tiles":
+        kernel_label = ("k_spmv_pipe (tail rows) + k_spmv_win (column-window tiles: rows sorted "
+                        "by length, x windows of 16384 relabelled columns staged in shared memory)")
+    else:
+        kernel_label = ({"registers": "k_sell_hot32", "bulk_copy": "k_sell_tma32"}[
+            args.sell_variant or "registers"]
+            + " (SELL-32 copy sorted by row length, relabelled columns)")
     secondary = {} if (args.no_secondary or scale != 22) else secondary_rmat22(device, A, x)
     cpu = cpu_baseline_spmv(A, x) if (rank == 0 and not args.no_cpu) else None
     out = {
@@ -351,9 +363,7 @@ def run_spmv_rmat(args, scale=22):
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "peak_kind": peak_kind, "algorithmic_bytes": B,
                      "kernel_ms": round(kernel_ms, 5),
-                     "kernel": {"registers": "k_sell_hot32", "bulk_copy": "k_sell_tma32"}[
-                         args.sell_variant or "registers"]
-                     + " (SELL-32 copy sorted by row length, relabelled columns)"},
+                     "kernel": kernel_label},
         "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * n},
         "gpu_launches": tr.launches,
@@ -820,6 +830,8 @@ def main():
     ap.add_argument("--graphs", type=int, default=1000, help="graph count of --workload multigraph")
     ap.add_argument("--sell-variant", default=None, choices=["registers", "bulk_copy"],
                     help="SpMV workloads: kernel variant over the SELL-32 copy (default: built-in)")
+    ap.add_argument("--layout", default=None, choices=["sell", "window_tiles"],
+                    help="spmv workloads: run this plus-times layout instead of the built-in choice")
     ap.add_argument("--hot-cols", type=int, default=0,
                     help="SpMV workloads: x values staged in shared memory (default: built-in)")
     args = ap.parse_args()

@@ -188,6 +188,7 @@ static void free_mat_storage(gg_mat* A) {
     delete A->colperm;
     A->colperm = nullptr;
   }
+  free_win_plan(A);
   if (A->hubplan) {
     cudaFree(A->hubplan->hubs);
     cudaFree(A->hubplan->pieces);

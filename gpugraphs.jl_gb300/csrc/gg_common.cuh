@@ -387,6 +387,56 @@ struct ColPerm {
   float* xr = nullptr;
 };
 
+// Column-window tiles of a large CSR for the plus-times Float32 SpMV (gg_spmv_win.cu).
+// Rows sorted by length (longest first) are cut into tiles (at most kTileRows rows,
+// fewer where the rows are long); columns are relabelled by decreasing frequency
+// (rank).  Every row of a tile is one or more pieces (long rows are cut so the 32
+// warps of a CTA get even shares); each piece belongs to one warp.  A tile's entries
+// inside the tile's staged windows (kWinCols consecutive ranks, whose x values the CTA
+// copies into shared memory with a bulk copy) are grouped per warp, then per window,
+// then by (piece, original column); an entry is one word (piece << 19 | rank offset
+// inside its window) plus its value.  The other entries form a tail CSR.
+// Work units are segment ranges of one tile, balanced over the CTAs; a tile split
+// into several units leaves one partial row vector per unit (combined in unit order).
+struct WinTile {
+  int32_t row0, rows;  // sorted row range
+  int32_t nv;          // pieces (accumulator slots)
+  int32_t nseg;        // segments
+  int32_t seg0;        // first word of the tile's segment bases in segbase[]
+  int32_t wbase;       // first word of the tile's [32][nseg + 1] entry offsets in wseg[]
+  int32_t vbase;       // first word of the tile's rows + 1 piece offsets in vptr[]
+  int32_t pad;
+};
+struct WinPlan {
+  bool enabled = false;
+  int64_t ntiles = 0, nseg = 0, nunits = 0, nslots = 0, nsplit = 0, nwin = 0, npieces = 0;
+  int grid = 0;
+  int32_t* rowperm = nullptr;  // sorted position -> original row (0-based)
+  int32_t* inv = nullptr;      // rank -> original column (0-based)
+  float* xr = nullptr;         // x in rank order, padded to whole windows
+  uint32_t* idx = nullptr;
+  float* val = nullptr;
+  WinTile* tiles = nullptr;
+  int32_t* segbase = nullptr;  // first rank of every segment | kSegWindow for windows
+  int32_t* wseg = nullptr;     // entry offsets per (tile, warp, segment)
+  int32_t* vptr = nullptr;     // per tile: first piece of every row (rows + 1 words)
+  int4* units = nullptr;       // (tile, first segment, end segment, slot), grouped by CTA
+  int32_t* cta_ptr = nullptr;  // grid + 1
+  int32_t* cta_wptr = nullptr; // grid + 1: each CTA's windows in cta_win
+  int32_t* cta_win = nullptr;  // first rank of every window a CTA stages, in order
+  int4* split = nullptr;       // (tile, first slot, slots, rows)
+  float* partials = nullptr;   // nslots * kWinRows
+  // entries outside every staged window: a CSR over the sorted rows with rank labels
+  // (row-block kernel), its row sums yt (sorted order) added at the end
+  gg_mat* tail = nullptr;
+  float* yt = nullptr;
+};
+static const int kWinRows = 8192;   // pieces per tile (13 bits of the entry word)
+static const int kTileRows = 6144;  // rows per tile
+static const int kWinCols = 16384;
+static const int kWinShift = 19;
+static const int32_t kSegWindow = 1 << 30;
+
 static const int kBlockNnz = 256;
 static const int kShortRow = 32;
 static const int kBlockRows = 256;
@@ -451,10 +501,12 @@ struct gg_mat {
   gg::ColPerm* colperm = nullptr;
   gg::MMPlan* mmplan = nullptr;
   gg::HubPlan* hubplan = nullptr;
+  gg::WinPlan* winplan = nullptr;
   gg_mat* sell_copy = nullptr;  // CSR handles: SELL-32 copy (rows sorted by length) for plus-times
   int64_t max_row_len = -1;
   // tuned choices (gg_tune): plus-times SpMV kernel (0 = built-in rule, 1 = CSR row
-  // blocks, 2 = the SELL copy), rows per row block, SpMM columns per lane (0 = 1)
+  // blocks, 2 = the SELL copy, 3 = column-window tiles), rows per row block, SpMM
+  // columns per lane (0 = 1)
   int tuned_spmv = 0;
   int block_rows = 0;
   int mm_cpl = 0;
@@ -462,6 +514,7 @@ struct gg_mat {
   // staged by bulk copies (k_sell_tma32)
   int sell_variant = 0;
   int hot_cols = 0;  // x values staged in shared memory by the register kernels (0: 32768)
+  int last_layout = 0;  // layout of the last plus-times Float32 SpMV (gg_spmv_layout)
 };
 
 namespace gg {
@@ -476,5 +529,10 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A);
 int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n);  // gg_batch.cu
 int launch_sell_tma(gg_ctx* ctx, gg_mat* A, const float* nzv, const float* xr, float* y,
                     const int32_t* colval);  // gg_spmv_tma.cu
+int launch_pipe_f32(gg_ctx* ctx, gg_mat* A, const float* nz, const float* x, float* y,
+                    const int32_t* colval, bool trace_main);  // gg_spmv.cu
+int build_win_plan(gg_ctx* ctx, gg_mat* A);  // gg_spmv_win.cu
+int launch_spmv_win(gg_ctx* ctx, gg_mat* A, const float* x, float* y);
+void free_win_plan(gg_mat* A);
 int row_stats(gg_ctx* ctx, gg_mat* A);
 }  // namespace gg

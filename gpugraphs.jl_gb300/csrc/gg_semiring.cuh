@@ -150,6 +150,20 @@ __device__ __forceinline__ float ld_stream_p(const float* p, uint64_t pol) {
   asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.f32 %0, [%1], %2;" : "=f"(r) : "l"(p), "l"(pol));
   return r;
 }
+__device__ __forceinline__ int4 ld_stream4_p(const int32_t* p, uint64_t pol) {
+  int4 r;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.v4.s32 {%0,%1,%2,%3}, [%4], %5;"
+      : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+      : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ float4 ld_stream4_p(const float* p, uint64_t pol) {
+  float4 r;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+      : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+      : "l"(p), "l"(pol));
+  return r;
+}
 __device__ __forceinline__ float ld_keep(const float* p, uint64_t pol) {
   float r;
   asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(r) : "l"(p), "l"(pol));

@@ -1043,6 +1043,38 @@ static int launch_sell_hot(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32& sr,
   return GG_OK;
 }
 
+// plus-times Float32 y = A x over a CSR handle with the row-block pipeline kernel
+// (colval: the handle's own or relabelled column labels); trace_main brackets the
+// kernel as the call's main kernel
+int launch_pipe_f32(gg_ctx* ctx, gg_mat* A, const float* nz, const float* x, float* y,
+                    const int32_t* colval, bool trace_main) {
+  GG_CHECK(build_row_blocks(ctx, A));
+  RowBlocks* rb = A->blocks;
+  const int64_t items = rb->nblocks > rb->nsegs ? rb->nblocks : rb->nsegs;
+  if (items == 0) return GG_OK;
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, k_spmv_pipe<SRPlusTimesF32>, kPipeWarps * 32, 0));
+    if (per_sm < 1) per_sm = 1;
+  }
+  SRPlusTimesF32 sr;
+  sr.nz = nz;
+  sr.x = x;
+  sr.y = y;
+  int64_t grid = (items + kPipeWarps - 1) / kPipeWarps;
+  const int64_t cap = (int64_t)ctx->num_sms * per_sm;  // one resident wave
+  if (grid > cap) grid = cap;
+  const int tr = trace_main ? trace_main_begin(ctx) : -1;
+  k_spmv_pipe<SRPlusTimesF32><<<(int)grid, kPipeWarps * 32, 0, ctx->stream>>>(
+      sr, A->rowptr, colval, rb->blocks, rb->nblocks, rb->segs, rb->nsegs,
+      rb->long_first_seg, rb->long_rows, rb->long_count, static_cast<float*>(rb->partials));
+  trace_main_end(ctx, tr);
+  trace_count(ctx, 1);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
 // dispatch of gg_spmv after validation (gg_api.cu); tc = accumulator type
 int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, void* y, int ty,
                   const void* x, int tx, const void* mask, int tmask, int64_t lo, int64_t hi) {
@@ -1054,7 +1086,17 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
     sr.nz = static_cast<const float*>(A->nzval);
     sr.x = static_cast<const float*>(x);
     sr.y = static_cast<float*>(y);
-    const bool use_copy = A->tuned_spmv == 2 || (A->tuned_spmv == 0 && A->m >= (1 << 16));
+    if (A->format == GG_FMT_CSR && A->tuned_spmv == 3) {
+      // column-window tiles (gg_spmv_win.cu), when the column frequencies are skewed
+      // enough for shared-memory windows to pay; otherwise the SELL copy below
+      GG_CHECK(build_win_plan(ctx, A));
+      if (A->winplan->enabled) {
+        A->last_layout = 3;
+        return launch_spmv_win(ctx, A, sr.x, sr.y);
+      }
+    }
+    const bool use_copy = A->tuned_spmv == 2 || ((A->tuned_spmv == 0 || A->tuned_spmv == 3) &&
+                                                 A->m >= (1 << 16));
     if (A->format == GG_FMT_CSR && use_copy) {
       // plus-times over a large CSR runs on a SELL-32 copy with rows sorted by length
       // (built once; gg_tune may pick another C and sigma): slices of equal-length
@@ -1064,6 +1106,7 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
         A->sell_copy->sell_variant = A->sell_variant;  // choices applied before the copy
         A->sell_copy->hot_cols = A->hot_cols;
       }
+      A->last_layout = 2;
       return spmv_dispatch(ctx, A->sell_copy, tc, mul, add, accum, y, ty, x, tx, mask, tmask, lo, hi);
     }
     GG_CHECK(build_colperm(ctx, A));
@@ -1076,28 +1119,10 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
       colval = A->colperm->colval_r;
     }
     if (A->format == GG_FMT_CSR) {
-      GG_CHECK(build_row_blocks(ctx, A));
-      RowBlocks* rb = A->blocks;
-      const int64_t items = rb->nblocks > rb->nsegs ? rb->nblocks : rb->nsegs;
-      if (items == 0) return GG_OK;
-      static int per_sm = 0;
-      if (per_sm == 0) {
-        GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, k_spmv_pipe<SRPlusTimesF32>, kPipeWarps * 32, 0));
-        if (per_sm < 1) per_sm = 1;
-      }
-      int64_t grid = (items + kPipeWarps - 1) / kPipeWarps;
-      const int64_t cap = (int64_t)ctx->num_sms * per_sm;  // one resident wave
-      if (grid > cap) grid = cap;
-      const int tr = trace_main_begin(ctx);
-      k_spmv_pipe<SRPlusTimesF32><<<(int)grid, kPipeWarps * 32, 0, ctx->stream>>>(
-          sr, A->rowptr, colval, rb->blocks, rb->nblocks, rb->segs, rb->nsegs,
-          rb->long_first_seg, rb->long_rows, rb->long_count, static_cast<float*>(rb->partials));
-      trace_main_end(ctx, tr);
-      trace_count(ctx, 1);
-      GG_CUDA(cudaGetLastError());
-      return GG_OK;
+      A->last_layout = 1;
+      return launch_pipe_f32(ctx, A, sr.nz, sr.x, sr.y, colval, true);
     }
+    A->last_layout = 2;
     if (A->colperm->enabled) return launch_sell_hot(ctx, A, sr, colval);
     return launch_sell(ctx, A, sr, nullptr, 0, 0, 0, colval);
   }

@@ -23,6 +23,7 @@
 // Every wait on an mbarrier is bounded: after kTWaitPolls polls the kernel records a
 // timeout in `err`, waits (bounded again) for the copies it issued, and returns.
 #include "gg_semiring.cuh"
+#include "gg_tma.cuh"
 
 namespace gg {
 
@@ -37,34 +38,6 @@ static const size_t kTSmemHot = (size_t)kTHot * 4;
 static const size_t kTSmemStages = (size_t)kTW * kTStages * kTStageWords * 8;
 static const size_t kTSmemBars = (size_t)kTW * kTStages * 8;
 static const size_t kTSmem = kTSmemHot + kTSmemStages + kTSmemBars;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(done)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-      "l"(src), "r"(bytes), "r"(bar)
-      : "memory");
-}
 
 // columns of a work item (groups: the sum of their 4-bit slice widths)
 __device__ __forceinline__ int item_cols(const int4& d) {

@@ -135,6 +135,19 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
         best_rows = R;
       }
     }
+    // column-window tiles (large power-law matrices only)
+    if (rc == GG_OK && A->m >= (1 << 16)) {
+      A->tuned_spmv = 3;
+      double ms = 0;
+      rc = time_median(ctx, &ms, run_spmv, &args);
+      if (rc == GG_OK && A->winplan && A->winplan->enabled) {
+        ++cand;
+        if (ms < best) {
+          best = ms;
+          best_kind = 3;
+        }
+      }
+    }
     // SELL copies
     std::vector<int32_t> rp(A->m + 1), len(A->m);
     if (rc == GG_OK) {
@@ -211,6 +224,12 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
     } else {
       out->block_rows = kBlockRows;
     }
+  } else if (best_kind == 3) {
+    A->tuned_spmv = 3;
+    A->block_rows = 0;
+    if (best_copy) gg_mat_destroy(best_copy);
+    A->sell_copy = nullptr;
+    out->spmv_kernel = 3;
   } else if (best_kind == 1) {
     A->tuned_spmv = 1;
     A->block_rows = best_rows;
@@ -228,6 +247,7 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
     out->sell_variant = best_variant;
     out->hot_cols = best_hot;
   }
+  if (A->tuned_spmv != 3) free_win_plan(A);  // keep the window layout only when chosen
   out->spmv_ms = best;
   out->candidates += cand;
   cudaFree(x);
@@ -286,6 +306,8 @@ extern "C" int gg_tune(gg_ctx* ctx, gg_mat* A, int64_t spmm_k, gg_tune_result* o
   return GG_OK;
 }
 
+extern "C" int gg_spmv_layout(const gg_mat* A) { return A ? A->last_layout : 0; }
+
 extern "C" int gg_tune_apply(gg_ctx* ctx, gg_mat* A, const gg_tune_result* choice) {
   if (!ctx || !A || !choice) return set_error(GG_ERR_ARGUMENT, "NULL argument");
   const int cpl = choice->mm_cols_per_lane;
@@ -309,8 +331,14 @@ extern "C" int gg_tune_apply(gg_ctx* ctx, gg_mat* A, const gg_tune_result* choic
     A->sell_copy = S;
     A->tuned_spmv = 2;
     A->block_rows = 0;
+  } else if (choice->spmv_kernel == 3) {
+    if (A->format != GG_FMT_CSR) return set_error(GG_ERR_ARGUMENT, "window tiles need a CSR handle");
+    if (A->sell_copy) gg_mat_destroy(A->sell_copy);
+    A->sell_copy = nullptr;
+    A->tuned_spmv = 3;
+    A->block_rows = 0;
   } else if (choice->spmv_kernel != 0 && choice->spmv_kernel != 2) {
-    return set_error(GG_ERR_ARGUMENT, "spmv_kernel must be 0, 1 or 2");
+    return set_error(GG_ERR_ARGUMENT, "spmv_kernel must be 0, 1, 2 or 3");
   }
   if (cpl) A->mm_cpl = cpl;
   if (choice->sell_variant == 0 || choice->sell_variant == 1) {

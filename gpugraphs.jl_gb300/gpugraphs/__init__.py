@@ -19,11 +19,11 @@ from .errors import (ArgumentError, BoundsError, DimensionMismatch, GPUGraphsErr
 from .ops import gpu_spmm_, gpu_spmv_, synchronize
 from .storage import (AbstractSparseGPUMatrix, SparseGPUMatrixCSR, SparseGPUMatrixSELL,
                       sprand_gpu)
-from .tuning import autotune
+from .tuning import autotune, spmv_layout
 
 __all__ = [
     "AbstractSparseGPUMatrix", "SparseGPUMatrixCSR", "SparseGPUMatrixSELL", "gpu_spmv_",
-    "gpu_spmm_", "sprand_gpu", "autotune", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
+    "gpu_spmm_", "sprand_gpu", "autotune", "spmv_layout", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
     "bfs_parents_", "shortest_path", "shortest_path_", "monoid_neutral", "monoid_absorb", "synchronize",
     "GPUGraphs_add", "GPUGraphs_safe_add", "GPUGraphs_mul", "GPUGraphs_second",
     "GPUGraphs_band", "GPUGraphs_bor", "GPUGraphs_any", "GPUGraphs_secondi", "GPUGraphs_max",

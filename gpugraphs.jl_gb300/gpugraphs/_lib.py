@@ -54,6 +54,7 @@ SIGNATURES = {
     "gg_multigraph_sssp": [P, P, P, P, I, PI64],
     "gg_tune": [P, P, I64, P],
     "gg_tune_apply": [P, P, P],
+    "gg_spmv_layout": [P],
     "gg_bfs_levels_noalloc": [P, P, P, I, I64, I64, I64, P, P, PI64],
     "gg_gen_rmat_edges": [P, I, I64, D, D, D, U64, I, P, P, P],
     "gg_gen_er_edges": [P, I64, I64, U64, I, P, P, P],

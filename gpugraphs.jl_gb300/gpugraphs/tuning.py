@@ -2,9 +2,10 @@
 
 The reference's storage layouts are fixed when a matrix is built (SELL slice height
 chosen by the caller, no row sorting: src/storage/SELL.jl:99-181).  autotune() times
-the library's own kernels on the matrix -- CSR row blocks of 32..256 rows, SELL-C-sigma
-layouts with C in {8, 16, 32} and sigma in {1, 64, 1024, m}, and the SpMM column tile
--- and keeps the fastest on the handle, so later gpu_spmv_ / gpu_spmm_ calls use it."""
+the library's own kernels on the matrix -- the built-in choice (column-window tiles
+for a large power-law CSR), CSR row blocks of 32..256 rows, SELL-C-sigma layouts with
+C in {8, 16, 32} and sigma in {1, 64, 1024, m}, and the SpMM column tile -- and keeps
+the fastest on the handle, so later gpu_spmv_ / gpu_spmm_ calls use it."""
 import ctypes
 
 from . import core
@@ -20,18 +21,19 @@ class TuneResult(ctypes.Structure):
                 ("hot_cols", ctypes.c_int)]
 
 SELL_VARIANTS = ("registers", "bulk_copy")
+KERNELS = {1: "csr_row_blocks", 2: "sell", 3: "window_tiles"}
 
 
 def autotune(A, spmm_k=0):
     """Tune A (a Float32 SparseGPUMatrixCSR / SELL) for plus-times SpMV and, when
     spmm_k > 0, SpMM with a row-major n x spmm_k operand.  Returns the choice as a
-    dict: spmv_kernel ("csr_row_blocks" or "sell"), block_rows or (slice_size,
+    dict: spmv_kernel ("csr_row_blocks", "sell" or "window_tiles"), block_rows or (slice_size,
     sigma), the chosen and built-in median times in ms, the SpMM column tile, and
     the number of configurations timed."""
     L = core.lib()
     r = TuneResult()
     check(L.gg_tune(core.ctx(A.device), A.handle, int(spmm_k), ctypes.byref(r)), L)
-    out = {"spmv_kernel": {1: "csr_row_blocks", 2: "sell"}.get(r.spmv_kernel, "none"),
+    out = {"spmv_kernel": KERNELS.get(r.spmv_kernel, "none"),
            "spmv_ms": r.spmv_ms, "spmv_default_ms": r.spmv_default_ms,
            "candidates": r.candidates}
     if r.spmv_kernel == 1:
@@ -67,7 +69,7 @@ def apply(A, choice):
     L = core.lib()
     r = TuneResult()
     kind = choice.get("spmv_kernel")
-    r.spmv_kernel = {"csr_row_blocks": 1, "sell": 2}.get(kind, 0)
+    r.spmv_kernel = {v: k for k, v in KERNELS.items()}.get(kind, 0)
     r.block_rows = int(choice.get("block_rows", 0))
     r.slice_size = int(choice.get("slice_size", 0))
     r.sigma = int(choice.get("sigma", 0))
@@ -87,3 +89,9 @@ def autotune_cached(A, spmm_k=0):
     res = autotune(A, spmm_k)
     _CACHE[key] = res
     return dict(res, cached=False)
+
+
+def spmv_layout(A):
+    """Layout the last plus-times Float32 gpu_spmv_ of A ran on: None (no such call
+    yet), "csr_row_blocks", "sell" or "window_tiles"."""
+    return KERNELS.get(core.lib().gg_spmv_layout(A.handle))

@@ -349,7 +349,7 @@ int gg_multigraph_sssp(gg_ctx* ctx, gg_multigraph* mg, const int64_t* sources, v
  *      src/storage/SELL.jl:99-181) -------------------------------------------------- */
 
 typedef struct gg_tune_result {
-  int spmv_kernel;         /* 1 = CSR row blocks, 2 = a SELL-C-sigma layout */
+  int spmv_kernel;         /* 1 = CSR row blocks, 2 = a SELL-C-sigma layout, 3 = column-window tiles */
   int block_rows;          /* rows per row block (spmv_kernel 1) */
   int64_t slice_size;      /* C (spmv_kernel 2) */
   int64_t sigma;           /* sigma (spmv_kernel 2) */
@@ -376,9 +376,14 @@ typedef struct gg_tune_result {
 int gg_tune(gg_ctx* ctx, gg_mat* A, int64_t spmm_k, gg_tune_result* out);
 /* Applies a choice (e.g. one cached from an earlier gg_tune of the same matrix)
  * without timing: spmv_kernel 1 with block_rows, 2 with slice_size and sigma (a SELL
- * copy of a CSR handle is built), 0 leaves SpMV as is; mm_cols_per_lane 1, 2 or 4
+ * copy of a CSR handle is built), 3 column-window tiles (CSR handles; built on the
+ * next call), 0 leaves SpMV as is; mm_cols_per_lane 1, 2 or 4
  * (0 leaves SpMM as is).  Synchronous. */
 int gg_tune_apply(gg_ctx* ctx, gg_mat* A, const gg_tune_result* choice);
+/* Layout the last plus-times Float32 gg_spmv of A ran on: 0 = none yet, 1 = CSR row
+ * blocks, 2 = a SELL-C-sigma layout (the handle itself or a copy), 3 = column-window
+ * tiles.  No reference counterpart (introspection of the layouts gg_tune chooses). */
+int gg_spmv_layout(const gg_mat* A);
 
 /* ---- seeded synthetic inputs (no reference counterpart: the reference's benchmark
  *      draws its inputs with Julia's sprand / Graphs.jl generators,

@@ -48,6 +48,7 @@ def spmv_check(A, rp, cv, nz, x):
     {"spmv_kernel": "sell", "slice_size": 8, "sigma": 64},
     {"spmv_kernel": "sell", "slice_size": 16, "sigma": 1024},
     {"spmv_kernel": "sell", "slice_size": 32, "sigma": 16384},
+    {"spmv_kernel": "window_tiles"},
 ])
 def test_every_spmv_layout_matches_oracle(rmat14, choice):
     A, rp, cv, nz, x = rmat14
@@ -74,7 +75,7 @@ def test_every_spmm_tile_matches_oracle(rmat14, tile):
 def test_autotune_picks_and_keeps_a_choice(rmat14):
     A, rp, cv, nz, x = rmat14
     res = G.autotune(A, spmm_k=64)
-    assert res["spmv_kernel"] in ("csr_row_blocks", "sell")
+    assert res["spmv_kernel"] in ("csr_row_blocks", "sell", "window_tiles")
     assert res["candidates"] >= 6
     assert res["spmv_ms"] <= res["spmv_default_ms"] * 1.0001
     assert res["spmm_column_tile"] in (32, 64)
