@@ -209,6 +209,8 @@ static void free_mat_storage(gg_mat* A) {
     cudaFree(A->sellplan->multi);
     cudaFree(A->sellplan->partials);
     cudaFree(A->sellplan->pitems);
+    cudaFree(A->sellplan->narrow);
+    cudaFree(A->sellplan->wide);
     delete A->sellplan;
     A->sellplan = nullptr;
   }

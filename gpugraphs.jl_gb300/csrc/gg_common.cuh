@@ -341,7 +341,13 @@ struct SellPlan {
   // -(slices), widths packed 4 bits per slice)
   int4* pitems = nullptr;
   int64_t npitems = 0;
+  // the chunked slices (multi) split by width for the plus-times Float32 combine:
+  // at most kNarrowChunks chunks (a thread per row) and wider (a warp per row)
+  int4* narrow = nullptr;
+  int4* wide = nullptr;
+  int64_t nnarrow = 0, nwide = 0;
 };
+static const int kNarrowChunks = 8;
 static const int kNarrowCols = 8;
 static const int kSellChunk = 128;
 

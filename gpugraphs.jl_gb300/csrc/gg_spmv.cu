@@ -539,7 +539,7 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
   GG_CUDA(cudaMemcpyAsync(sp.data(), A->slice_ptr, (ns + 1) * sizeof(int32_t),
                           cudaMemcpyDeviceToHost, ctx->stream));
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
-  std::vector<int4> items, multi, pitems;
+  std::vector<int4> items, multi, pitems, narrow, wide;
   int32_t np = 0;
   // narrow-slice groups of the warp kernel (C == 32 only)
   int64_t g_first = -1, g_cols = 0, g_count = 0;
@@ -569,6 +569,7 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
       continue;
     }
     const int32_t nch = (int32_t)((L + kSellChunk - 1) / kSellChunk);
+    (nch <= kNarrowChunks ? narrow : wide).push_back(make_int4((int)s, np, nch, 0));
     multi.push_back(make_int4((int)s, np, nch, 0));
     for (int32_t c = 0; c < nch; ++c) {
       const int64_t jb = (int64_t)c * kSellChunk;
@@ -583,10 +584,20 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
   P->npitems = (int64_t)pitems.size();
   P->nitems = (int64_t)items.size();
   P->nmulti = (int64_t)multi.size();
+  P->nnarrow = (int64_t)narrow.size();
+  P->nwide = (int64_t)wide.size();
   cudaError_t e = cudaMalloc((void**)&P->items, (items.size() + 1) * sizeof(int4));
   if (e == cudaSuccess) e = cudaMalloc((void**)&P->multi, (multi.size() + 1) * sizeof(int4));
   if (e == cudaSuccess) e = cudaMalloc(&P->partials, ((int64_t)np * C + 1) * 8);
   if (e == cudaSuccess) e = cudaMalloc((void**)&P->pitems, (pitems.size() + 1) * sizeof(int4));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&P->narrow, (narrow.size() + 1) * sizeof(int4));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&P->wide, (wide.size() + 1) * sizeof(int4));
+  if (e == cudaSuccess && !narrow.empty())
+    e = cudaMemcpyAsync(P->narrow, narrow.data(), narrow.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                        ctx->stream);
+  if (e == cudaSuccess && !wide.empty())
+    e = cudaMemcpyAsync(P->wide, wide.data(), wide.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                        ctx->stream);
   if (e == cudaSuccess && !pitems.empty())
     e = cudaMemcpyAsync(P->pitems, pitems.data(), pitems.size() * sizeof(int4),
                         cudaMemcpyHostToDevice, ctx->stream);
@@ -602,6 +613,8 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
     cudaFree(P->multi);
     cudaFree(P->partials);
     cudaFree(P->pitems);
+    cudaFree(P->narrow);
+    cudaFree(P->wide);
     delete P;
     return cuda_error(e, "SELL analysis");
   }
@@ -895,6 +908,49 @@ static int launch_sell(gg_ctx* ctx, gg_mat* A, const SR& sr, const void* mask, i
   return GG_OK;
 }
 
+// Plus-times Float32 combine of SELL-32 slices of at most kNarrowChunks chunks, one
+// thread per row, in exactly the order of k_sell_combine: there lane l folds the
+// chunks c = l mod 32 (here at most one each) and lane 0 ends with the butterfly
+// sum, i.e. a pairwise tree over the lanes' values in bit-reversed lane order.
+__global__ void k_sell_combine_narrow(const int4* __restrict__ narrow, int64_t nnarrow,
+                                      const float* __restrict__ partials,
+                                      const int32_t* __restrict__ perm, int64_t m,
+                                      float* __restrict__ y) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nnarrow * 32;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int4 d = narrow[t >> 5];  // slice, first partial, chunks
+    const int o = (int)(t & 31);
+    const int64_t srow = (int64_t)d.x * 32 + o;
+    if (srow >= m) continue;
+    float v[kNarrowChunks];
+#pragma unroll
+    for (int c = 0; c < kNarrowChunks; ++c)
+      v[c] = c < d.z ? __fadd_rn(0.0f, partials[(int64_t)(d.y + c) * 32 + o]) : 0.0f;
+    float stk[5];
+    int lvl[5];
+    int top = 0;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      const int l = (int)(__brev((unsigned)k) >> 27);
+      float s = l < kNarrowChunks ? v[l] : 0.0f;
+      int lv = 0;
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        if (top > 0 && lvl[top - 1] == lv) {
+          s = __fadd_rn(stk[top - 1], s);
+          --top;
+          ++lv;
+        }
+      }
+      stk[top] = s;
+      lvl[top] = lv;
+      ++top;
+    }
+    const int32_t r1 = perm ? perm[srow] : (int32_t)(srow + 1);
+    __stcs(y + (r1 - 1), stk[0]);
+  }
+}
+
 // SELL-32 variant: one warp per work item (lane = row of the slice), with the item's
 // first position, first stored row, width and partial slot precomputed, and the next
 // item's descriptor loaded while the current one runs -- rows of one or two entries
@@ -1033,9 +1089,19 @@ static int launch_sell_hot(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32& sr,
     trace_main_end(ctx, tr);
     trace_count(ctx, 1);
   }
-  if (P->nmulti > 0) {
-    k_sell_combine<SRPlusTimesF32><<<grid_for(ctx, P->nmulti * C * 32, 256), 256, 0, ctx->stream>>>(
-        sr, A->sigma > 1 ? A->perm : nullptr, C, A->m, P->multi, P->nmulti,
+  // SELL-32: narrow chunked slices a thread per row, the wide ones a warp per row
+  const bool split = C == 32;
+  if (split && P->nnarrow > 0) {
+    k_sell_combine_narrow<<<grid_for(ctx, P->nnarrow * 32, 256), 256, 0, ctx->stream>>>(
+        P->narrow, P->nnarrow, static_cast<const float*>(P->partials),
+        A->sigma > 1 ? A->perm : nullptr, A->m, sr.y);
+    trace_count(ctx, 1);
+  }
+  const int4* cl = split ? P->wide : P->multi;
+  const int64_t ncl = split ? P->nwide : P->nmulti;
+  if (ncl > 0) {
+    k_sell_combine<SRPlusTimesF32><<<grid_for(ctx, ncl * C * 32, 256), 256, 0, ctx->stream>>>(
+        sr, A->sigma > 1 ? A->perm : nullptr, C, A->m, cl, ncl,
         static_cast<const float*>(P->partials), 0, 0, nullptr, 0);
     trace_count(ctx, 1);
   }
