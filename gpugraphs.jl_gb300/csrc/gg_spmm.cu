@@ -231,6 +231,31 @@ __global__ void __launch_bounds__(256)
 // in flight instead of one.  Each column is still folded in storage order.
 static const int kShortMM = 32;
 
+// A column of a float4 accumulator whose sum ended NaN is folded again with the
+// reference's stop at +Inf (CSR.jl:49-51), so results equal the sequential fold.
+__device__ __noinline__ float4 spmm_refold4(float4 acc, const int32_t* __restrict__ colval,
+                                           const float* __restrict__ nz, const float* Bj,
+                                           int64_t ldb, int32_t k0, int32_t k1) {
+  float r[4] = {acc.x, acc.y, acc.z, acc.w};
+  for (int q = 0; q < 4; ++q) {
+    if (r[q] == r[q]) continue;
+    float s = 0.0f;
+    for (int32_t k = k0; k < k1; ++k) {
+      s = __fadd_rn(s, __fmul_rn(__ldg(nz + k), __ldg(Bj + (int64_t)(__ldg(colval + k) - 1) * ldb + q)));
+      if (s == __int_as_float(0x7f800000)) break;
+    }
+    r[q] = s;
+  }
+  return make_float4(r[0], r[1], r[2], r[3]);
+}
+
+__device__ __forceinline__ void fold4(float4& acc, float a, const float4& b) {
+  acc.x = __fadd_rn(acc.x, __fmul_rn(a, b.x));
+  acc.y = __fadd_rn(acc.y, __fmul_rn(a, b.y));
+  acc.z = __fadd_rn(acc.z, __fmul_rn(a, b.z));
+  acc.w = __fadd_rn(acc.w, __fmul_rn(a, b.w));
+}
+
 __global__ void __launch_bounds__(256)
     k_spmm_short_f32x4(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colval,
                        const float* __restrict__ nz, const float* __restrict__ B, int64_t ldb,
@@ -275,61 +300,70 @@ __global__ void __launch_bounds__(256)
         acc.z = __fadd_rn(acc.z, __fmul_rn(a0, b0.z));
         acc.w = __fadd_rn(acc.w, __fmul_rn(a0, b0.w));
       }
+      if (acc.x != acc.x || acc.y != acc.y || acc.z != acc.z || acc.w != acc.w)
+        acc = spmm_refold4(acc, colval, nz, B + j, ldb, k0, k1);
       *reinterpret_cast<float4*>(C + r * ldc + j) = acc;
     }
   }
 }
 
 // Rows of 33..kSegMM entries and the pieces of longer rows, plus-times Float32 on
-// row-major operands: one warp per item (longest first), lane = dense column.  The
-// warp reads 32 column / value pairs with one coalesced load each, then issues 16
-// gathers of B rows before folding them in storage order, with no per-entry test of
-// the absorbing value; a column whose sum ends NaN is folded again with the
-// reference's stop at +Inf (CSR.jl:49-51), so results equal the sequential fold.
+// 16-byte aligned row-major operands: four items per warp (longest first, so the four
+// have about the same length), 8 lanes per item, each lane 4 dense columns with float4
+// loads of B; every item is folded in storage order (4 entries per step, the next
+// step's column / value words loaded while the current B rows are in flight).
 __global__ void __launch_bounds__(256)
-    k_spmm_items_f32(const int32_t* __restrict__ colval, const float* __restrict__ nz,
-                     const float* __restrict__ B, int64_t ldb, float* __restrict__ C, int64_t ldc,
-                     const int4* __restrict__ items, int64_t nitems, int64_t row_lo, int64_t row_hi,
-                     int64_t jlo, int64_t jn, float* partials) {
+    k_spmm_items_f32x4(const int32_t* __restrict__ colval, const float* __restrict__ nz,
+                       const float* __restrict__ B, int64_t ldb, float* __restrict__ C, int64_t ldc,
+                       const int4* __restrict__ items, int64_t nitems, int64_t row_lo,
+                       int64_t row_hi, int64_t jlo, int64_t jn, float* partials) {
   const int lane = threadIdx.x & 31;
+  const int grp = lane >> 3, sub = lane & 7;
   const uint64_t pol_s = l2_evict_first(), pol_b = l2_evict_last();
-  for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < nitems;
-       it += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const int4 d = items[it];  // row, first entry, end entry, partial slot or -1
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = gw * 4; base < nitems; base += nw * 4) {
+    const int64_t t = base + grp;
+    if (t >= nitems) continue;
+    const int4 d = items[t];  // row, first entry, end entry, partial slot or -1
     if (d.x < row_lo || d.x >= row_hi) continue;
     for (int64_t jb = 0; jb < jn; jb += 32) {
-      const int64_t jj = jb + lane;
-      const bool active = jj < jn;
-      const float* Bj = B + jlo + (active ? jj : 0);
-      float acc = 0.0f;
-      for (int32_t base = d.y; base < d.z; base += 32) {
-        const int32_t kk = base + lane;
-        const int32_t c_l = kk < d.z ? ld_stream_p(colval + kk, pol_s) - 1 : 0;
-        const float a_l = kk < d.z ? ld_stream_p(nz + kk, pol_s) : 0.0f;
-        const int nb = d.z - base < 32 ? d.z - base : 32;
-        for (int i0 = 0; i0 < nb; i0 += 16) {
-          float bv[16], av[16];
+      const int64_t jj = jb + 4 * sub;
+      if (jj >= jn) continue;
+      const float* Bj = B + jlo + jj;
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      int32_t c[4], cn[4];
+      float a[4], an[4];
 #pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            const int c = __shfl_sync(0xffffffffu, c_l, (i0 + u) & 31);
-            av[u] = __shfl_sync(0xffffffffu, a_l, (i0 + u) & 31);
-            bv[u] = (i0 + u < nb) ? ld_keep(Bj + (int64_t)c * ldb, pol_b) : 0.0f;
-          }
+      for (int u = 0; u < 4; ++u) {
+        const bool in = d.y + u < d.z;
+        c[u] = in ? ld_stream_p(colval + d.y + u, pol_s) - 1 : 0;
+        a[u] = in ? ld_stream_p(nz + d.y + u, pol_s) : 0.0f;
+      }
+      for (int32_t k = d.y; k < d.z; k += 4) {
 #pragma unroll
-          for (int u = 0; u < 16; ++u)
-            if (i0 + u < nb) acc = __fadd_rn(acc, __fmul_rn(av[u], bv[u]));
+        for (int u = 0; u < 4; ++u) {
+          const bool in = k + 4 + u < d.z;
+          cn[u] = in ? ld_stream_p(colval + k + 4 + u, pol_s) - 1 : 0;
+          an[u] = in ? ld_stream_p(nz + k + 4 + u, pol_s) : 0.0f;
+        }
+        float4 b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          b[u] = k + u < d.z ? ld_keep4(Bj + (int64_t)c[u] * ldb, pol_b) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (k + u < d.z) fold4(acc, a[u], b[u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          c[u] = cn[u];
+          a[u] = an[u];
         }
       }
-      if (acc != acc) {  // NaN: fold again with the stop at +Inf
-        acc = 0.0f;
-        for (int32_t k = d.y; k < d.z; ++k) {
-          acc = __fadd_rn(acc, __fmul_rn(__ldg(nz + k), __ldg(Bj + (int64_t)(__ldg(colval + k) - 1) * ldb)));
-          if (acc == __int_as_float(0x7f800000)) break;
-        }
-      }
-      if (!active) continue;
-      if (d.w < 0) C[(int64_t)d.x * ldc + jlo + jj] = acc;
-      else partials[(int64_t)d.w * jn + jj] = acc;
+      if (acc.x != acc.x || acc.y != acc.y || acc.z != acc.z || acc.w != acc.w)
+        acc = spmm_refold4(acc, colval, nz, Bj, ldb, d.y, d.z);
+      float* out = d.w < 0 ? C + (int64_t)d.x * ldc + jlo + jj : partials + (int64_t)d.w * jn + jj;
+      *reinterpret_cast<float4*>(out) = acc;
     }
   }
 }
@@ -360,7 +394,7 @@ struct ShortRowsMM<SRPlusTimesF32MM> {
   static void launch_items(gg_ctx* ctx, const SRPlusTimesF32MM& sr, const int32_t* colval,
                            const MMPlan* P, int64_t row_lo, int64_t row_hi, int64_t jlo, int64_t jn,
                            float* partials) {
-    k_spmm_items_f32<<<grid_mm(ctx, P->nitems), 256, 0, ctx->stream>>>(
+    k_spmm_items_f32x4<<<grid_mm(ctx, (P->nitems + 3) / 4), 256, 0, ctx->stream>>>(
         colval, sr.nz, sr.x, sr.ldb, sr.y, sr.ldc, P->items, P->nitems, row_lo, row_hi, jlo, jn,
         partials);
   }

@@ -574,6 +574,29 @@ def test_spmv_layout_choices_on_large_csr():
     assert G.spmv_layout(E) == "sell"
 
 
+@pytest.mark.parametrize("k", [4, 32, 36])
+def test_spmm_special_values_fold_like_the_reference(k):
+    """Row-major plus-times SpMM with +Inf, -Inf and NaN in B: every row of <= 256
+    entries (short rows, medium rows of the four-items-per-warp kernel) equals the
+    oracle's sequential fold, including its stop at +Inf (NaN-aware comparison)."""
+    m = 3000
+    rowptr, colval, nzval, A = power_law_csr(m, 31)
+    rng = np.random.default_rng(k)
+    B = rng.random((m, k), dtype=np.float32)
+    B[rng.random((m, k)) < 0.002] = np.inf
+    B[rng.random((m, k)) < 0.001] = -np.inf
+    B[rng.random((m, k)) < 0.001] = np.nan
+    Co = np.zeros((m, k), np.float32)
+    O.csr_spmm(m, rowptr, colval, nzval, Co, B, layout=1)
+    M = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nzval)
+    Cd = torch.zeros((m, k), dtype=torch.float32, device="cuda")
+    G.gpu_spmm_(Cd, M, dev(B))
+    Ch = host(Cd)
+    short = np.diff(rowptr) <= SEG_MM
+    np.testing.assert_array_equal(Ch[short], Co[short])
+    assert (np.isposinf(Co) & short[:, None]).any() and (np.isnan(Co) & short[:, None]).any()
+
+
 @pytest.mark.parametrize("k", [1, 4, 6, 32])
 def test_spmm_writes_every_row(k):
     """Row-major plus-times SpMM with 20% empty rows into a NaN-filled C: every row is
