@@ -569,11 +569,26 @@ static const int kLightDeg = 4;
 static const int kBatch = 4;
 static const int kHubDeg = 1024;  // beyond this a frontier vertex gets the whole block
 
+// The single-CTA kernels stop once a frontier's out-edges exceed kSmallEdges (a hub
+// reached early would otherwise be walked by one SM): the frontier and its edge count
+// go back to the host, whose grid-wide kernels take over.
+static const unsigned long long kSmallEdges = 32768;
+
 __device__ __forceinline__ void small_append(int32_t w, int32_t* nxt, int32_t* qg, int32_t cap,
-                                             int32_t* s_nn) {
+                                             int32_t* s_nn, const int32_t* __restrict__ prow,
+                                             unsigned long long* s_ne) {
   const int32_t pos = atomicAdd(s_nn, 1);
   if (pos < cap) nxt[pos] = w;
   else qg[pos] = w;
+  atomicAdd(s_ne, (unsigned long long)(__ldg(prow + w + 1) - __ldg(prow + w)));
+}
+
+// out-edges of the first nf vertices of q, summed into *s_ne (block-wide)
+__device__ __forceinline__ void small_edges(const int32_t* q, int32_t nf,
+                                            const int32_t* __restrict__ prow,
+                                            unsigned long long* s_ne) {
+  for (int32_t i = threadIdx.x; i < nf; i += blockDim.x)
+    atomicAdd(s_ne, (unsigned long long)(__ldg(prow + q[i] + 1) - __ldg(prow + q[i])));
 }
 
 // Small-frontier BFS: one CTA runs top-down levels back to back while the frontier
@@ -589,15 +604,29 @@ __global__ void __launch_bounds__(1024)
   int32_t* nxt = smem + cap;
   int32_t* heavy = smem + 2 * cap;
   __shared__ int32_t s_nn, s_nh;
+  __shared__ unsigned long long s_ne;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) s_ne = 0;
   for (int32_t i = threadIdx.x; i < nf0; i += blockDim.x) cur[i] = qg[i];
   int32_t nf = nf0, level = level0;
+  __syncthreads();
+  small_edges(cur, nf0, prow, &s_ne);
+  __syncthreads();
+  if (s_ne > kSmallEdges) {  // the starting frontier is already too heavy for one CTA
+    if (threadIdx.x == 0) {
+      ctr->nf = (unsigned long long)nf0;
+      ctr->mf = s_ne;
+      ctr->level = (unsigned long long)level0;
+    }
+    return;
+  }
   __syncthreads();
   for (;;) {
     ++level;
     if (threadIdx.x == 0) {
       s_nn = 0;
       s_nh = 0;
+      s_ne = 0;
     }
     __syncthreads();
     for (int32_t i0 = threadIdx.x; i0 < nf; i0 += blockDim.x * kBatch) {
@@ -635,7 +664,7 @@ __global__ void __launch_bounds__(1024)
         for (int j = 0; j < kLightDeg; ++j)
           if (w[b][j] >= 0 && !((old[b][j] >> (w[b][j] & 31)) & 1u)) {
             dist[w[b][j]] = level;
-            small_append(w[b][j], nxt, qg, cap, &s_nn);
+            small_append(w[b][j], nxt, qg, cap, &s_nn, prow, &s_ne);
           }
     }
     __syncthreads();
@@ -650,7 +679,7 @@ __global__ void __launch_bounds__(1024)
         const unsigned bit = 1u << (w & 31);
         if (atomicOr(visited + (w >> 5), bit) & bit) continue;
         dist[w] = level;
-        small_append(w, nxt, qg, cap, &s_nn);
+        small_append(w, nxt, qg, cap, &s_nn, prow, &s_ne);
       }
     }
     for (int32_t h = 0; h < nh; ++h) {
@@ -662,17 +691,17 @@ __global__ void __launch_bounds__(1024)
         const unsigned bit = 1u << (w & 31);
         if (atomicOr(visited + (w >> 5), bit) & bit) continue;
         dist[w] = level;
-        small_append(w, nxt, qg, cap, &s_nn);
+        small_append(w, nxt, qg, cap, &s_nn, prow, &s_ne);
       }
     }
     __syncthreads();
     const int32_t nn = s_nn;
-    if (nn == 0 || nn > cap) {
-      if (nn > cap)
-        for (int32_t i = threadIdx.x; i < cap; i += blockDim.x) qg[i] = nxt[i];
+    const unsigned long long ne = s_ne;
+    if (nn == 0 || nn > cap || ne > kSmallEdges) {
+      for (int32_t i = threadIdx.x; i < (nn < cap ? nn : cap); i += blockDim.x) qg[i] = nxt[i];
       if (threadIdx.x == 0) {
         ctr->nf = (unsigned long long)nn;
-        ctr->mf = 0;
+        ctr->mf = ne;
         ctr->level = (unsigned long long)level;
       }
       return;
@@ -1031,7 +1060,7 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
       }
       continue;
     }
-    if (!pull && nf <= small_cap) {
+    if (!pull && nf <= small_cap && mf <= (int64_t)kSmallEdges) {
       k_bfs_small<<<1, kSmallThreads, kSmallSmem, ctx->stream>>>(
           P.rowptr, P.colval, sc.q[cur], (int32_t)nf, (int32_t)level, small_cap, sc.visited, dist,
           sc.ctr);
@@ -1041,11 +1070,8 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
       nf = (int64_t)h->nf;
       level = (int64_t)h->level;
       if (nf == 0) break;
-      // the frontier of `level` is in q[cur]; its out-degree sum feeds the heuristic
-      GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
-      k_queue_degree<<<gridsz(ctx, nf), 256, 0, ctx->stream>>>(P.rowptr, sc.q[cur], nf, sc.ctr);
-      GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
-      GG_CUDA(cudaStreamSynchronize(ctx->stream));
+      // the frontier of `level` is in q[cur]; its out-degree sum (counted by the kernel)
+      // feeds the heuristic and keeps heavy frontiers on the grid-wide kernels
       mf = (int64_t)h->mf;
       explored += mf;
       continue;
@@ -1256,18 +1282,33 @@ __global__ void __launch_bounds__(1024)
   int32_t* nxt = smem + cap;
   int32_t* heavy = smem + 2 * cap;
   __shared__ int32_t s_nn, s_nh;
+  __shared__ unsigned long long s_ne;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) s_ne = 0;
   for (int32_t i = threadIdx.x; i < nf0; i += blockDim.x) cur[i] = qg[i];
   int32_t nf = nf0;
   unsigned* ic = inq_a;
   unsigned* in = inq_b;
   unsigned long long rounds = 0;
   __syncthreads();
+  small_edges(cur, nf0, prow, &s_ne);
+  __syncthreads();
+  if (s_ne > kSmallEdges) {  // the starting frontier is already too heavy for one CTA
+    if (threadIdx.x == 0) {
+      ctr->nf = (unsigned long long)nf0;
+      ctr->mf = s_ne;
+      ctr->level = 0;
+      ctr->status = 0;  // its membership bits are still in inq_a
+    }
+    return;
+  }
+  __syncthreads();
   for (;;) {
     ++rounds;
     if (threadIdx.x == 0) {
       s_nn = 0;
       s_nh = 0;
+      s_ne = 0;
     }
     __syncthreads();
     for (int32_t i0 = threadIdx.x; i0 < nf; i0 += blockDim.x * kBatch) {
@@ -1313,7 +1354,7 @@ __global__ void __launch_bounds__(1024)
         for (int j = 0; j < kLightDeg; ++j)
           if (w[b][j] >= 0) {
             const unsigned bit = 1u << (w[b][j] & 31);
-            if (!(atomicOr(in + (w[b][j] >> 5), bit) & bit)) small_append(w[b][j], nxt, qg, cap, &s_nn);
+            if (!(atomicOr(in + (w[b][j] >> 5), bit) & bit)) small_append(w[b][j], nxt, qg, cap, &s_nn, prow, &s_ne);
           }
     }
     __syncthreads();
@@ -1330,7 +1371,7 @@ __global__ void __launch_bounds__(1024)
         if (!(cand < atomic_min_t(dist + w, cand))) continue;
         const unsigned bit = 1u << (w & 31);
         if (atomicOr(in + (w >> 5), bit) & bit) continue;
-        small_append(w, nxt, qg, cap, &s_nn);
+        small_append(w, nxt, qg, cap, &s_nn, prow, &s_ne);
       }
     }
     for (int32_t h = 0; h < nh; ++h) {
@@ -1345,18 +1386,20 @@ __global__ void __launch_bounds__(1024)
         if (!(cand < atomic_min_t(dist + w, cand))) continue;
         const unsigned bit = 1u << (w & 31);
         if (atomicOr(in + (w >> 5), bit) & bit) continue;
-        small_append(w, nxt, qg, cap, &s_nn);
+        small_append(w, nxt, qg, cap, &s_nn, prow, &s_ne);
       }
     }
     __syncthreads();
     const int32_t nn = s_nn;
-    if (nn == 0 || nn > cap || (max_rounds > 0 && (int64_t)rounds >= max_rounds)) {
+    const unsigned long long ne = s_ne;
+    if (nn == 0 || nn > cap || ne > kSmallEdges || (max_rounds > 0 && (int64_t)rounds >= max_rounds)) {
       if (nn > cap)
         for (int32_t i = threadIdx.x; i < cap; i += blockDim.x) qg[i] = nxt[i];
       else
         for (int32_t i = threadIdx.x; i < nn; i += blockDim.x) qg[i] = nxt[i];
       if (threadIdx.x == 0) {
         ctr->nf = (unsigned long long)nn;
+        ctr->mf = ne;
         ctr->level = rounds;
         ctr->status = (in == inq_b) ? 1ull : 0ull;  // which bitmap holds the frontier bits
       }
@@ -1854,7 +1897,7 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
       }
       continue;
     }
-    if (nf <= small_cap) {
+    if (nf <= small_cap && mf <= (int64_t)kSmallEdges) {
       GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
       k_sssp_small<T><<<1, kSmallThreads, kSmallSmem, ctx->stream>>>(
           P.rowptr, P.colval, static_cast<const T*>(P.w), sc.q[cur], (int32_t)nf, small_cap, d,
@@ -1866,18 +1909,13 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
       rounds += (int64_t)h->level;
       // the remaining frontier is in q[cur]; its membership bits are in fb[cur] when
       // status == 0, else in fb[cur ^ 1] -- then swap roles so bits and queue agree
+      // out-edges of the remaining frontier (counted by the kernel), for the direction
+      // choice; a frontier above kSmallEdges goes to the grid-wide rounds
+      mf = nf > 0 ? (int64_t)h->mf : 0;
       if (nf > 0 && h->status == 1) {
         cur ^= 1;
         GG_CUDA(cudaMemcpyAsync(sc.q[cur], sc.q[cur ^ 1], nf * sizeof(int32_t),
                                 cudaMemcpyDeviceToDevice, ctx->stream));
-      }
-      mf = 0;
-      if (nf > 0) {  // out-edges of the remaining frontier, for the direction choice
-        GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
-        k_queue_degree<<<gridsz(ctx, nf), 256, 0, ctx->stream>>>(P.rowptr, sc.q[cur], nf, sc.ctr);
-        GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
-        GG_CUDA(cudaStreamSynchronize(ctx->stream));
-        mf = (int64_t)h->mf;
       }
       continue;
     }
