@@ -430,9 +430,10 @@ def run_search(args, kind, graph):
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
-    if graph == "rmat24":
-        A = rmat(24, gen.W_PATTERN if kind == "bfs" else gen.W_INT_1_255, device)
-        cfg = "R-MAT scale 24, edge factor 16, symmetrised" + (
+    if graph.startswith("rmat"):
+        sc = int(graph[4:])
+        A = rmat(sc, gen.W_PATTERN if kind == "bfs" else gen.W_INT_1_255, device)
+        cfg = "R-MAT scale %d, edge factor 16, symmetrised" % sc + (
             ", Bool pattern" if kind == "bfs" else ", Int32 weights 1..255")
     else:
         A = gen.grid(4096, 4096, seed=4, wkind=gen.W_PATTERN if kind == "bfs" else gen.W_F32_1_10,
@@ -841,7 +842,8 @@ def main():
         run_spmv_rmat(args, 22)
     elif args.workload == "spmv_csr_rmat24":
         run_spmv_rmat(args, 24)
-    elif args.workload in ("bfs_rmat24", "sssp_rmat24", "bfs_grid4096", "sssp_grid4096"):
+    elif args.workload in ("bfs_rmat24", "sssp_rmat24", "bfs_grid4096", "sssp_grid4096",
+                           "bfs_rmat22", "sssp_rmat22"):
         kind, graph = args.workload.split("_")
         if args.steps == 50:
             args.steps = 8

@@ -572,23 +572,35 @@ static const int kHubDeg = 1024;  // beyond this a frontier vertex gets the whol
 // The single-CTA kernels stop once a frontier's out-edges exceed kSmallEdges (a hub
 // reached early would otherwise be walked by one SM): the frontier and its edge count
 // go back to the host, whose grid-wide kernels take over.
-static const unsigned long long kSmallEdges = 32768;
+static const unsigned long long kSmallEdges = 8192;
 
+
+// appends w to the next frontier; `edges` (per thread) sums the out-degrees appended
 __device__ __forceinline__ void small_append(int32_t w, int32_t* nxt, int32_t* qg, int32_t cap,
                                              int32_t* s_nn, const int32_t* __restrict__ prow,
-                                             unsigned long long* s_ne) {
+                                             unsigned long long& edges) {
   const int32_t pos = atomicAdd(s_nn, 1);
   if (pos < cap) nxt[pos] = w;
   else qg[pos] = w;
-  atomicAdd(s_ne, (unsigned long long)(__ldg(prow + w + 1) - __ldg(prow + w)));
+  edges += (unsigned long long)(__ldg(prow + w + 1) - __ldg(prow + w));
+}
+
+// adds every thread's `edges` into *s_ne (one shared atomic per warp; all threads)
+__device__ __forceinline__ void small_edges_flush(unsigned long long& edges, unsigned long long* s_ne) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) edges += __shfl_xor_sync(0xffffffffu, edges, o);
+  if ((threadIdx.x & 31) == 0 && edges) atomicAdd(s_ne, edges);
+  edges = 0;
 }
 
 // out-edges of the first nf vertices of q, summed into *s_ne (block-wide)
 __device__ __forceinline__ void small_edges(const int32_t* q, int32_t nf,
                                             const int32_t* __restrict__ prow,
                                             unsigned long long* s_ne) {
+  unsigned long long e = 0;
   for (int32_t i = threadIdx.x; i < nf; i += blockDim.x)
-    atomicAdd(s_ne, (unsigned long long)(__ldg(prow + q[i] + 1) - __ldg(prow + q[i])));
+    e += (unsigned long long)(__ldg(prow + q[i] + 1) - __ldg(prow + q[i]));
+  small_edges_flush(e, s_ne);
 }
 
 // Small-frontier BFS: one CTA runs top-down levels back to back while the frontier
@@ -598,13 +610,14 @@ __device__ __forceinline__ void small_edges(const int32_t* q, int32_t nf,
 __global__ void __launch_bounds__(1024)
     k_bfs_small(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol, int32_t* qg,
                 int32_t nf0, int32_t level0, int32_t cap, unsigned* visited, int32_t* dist,
-                Counters* ctr) {
+                Counters* ctr, unsigned long long budget) {
   extern __shared__ int32_t smem[];
   int32_t* cur = smem;
   int32_t* nxt = smem + cap;
   int32_t* heavy = smem + 2 * cap;
   __shared__ int32_t s_nn, s_nh;
   __shared__ unsigned long long s_ne;
+  unsigned long long edges = 0;  // out-degrees this thread appended in the current level
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) s_ne = 0;
   for (int32_t i = threadIdx.x; i < nf0; i += blockDim.x) cur[i] = qg[i];
@@ -612,7 +625,7 @@ __global__ void __launch_bounds__(1024)
   __syncthreads();
   small_edges(cur, nf0, prow, &s_ne);
   __syncthreads();
-  if (s_ne > kSmallEdges) {  // the starting frontier is already too heavy for one CTA
+  if (s_ne > budget) {  // the starting frontier is already too heavy for one CTA
     if (threadIdx.x == 0) {
       ctr->nf = (unsigned long long)nf0;
       ctr->mf = s_ne;
@@ -664,7 +677,7 @@ __global__ void __launch_bounds__(1024)
         for (int j = 0; j < kLightDeg; ++j)
           if (w[b][j] >= 0 && !((old[b][j] >> (w[b][j] & 31)) & 1u)) {
             dist[w[b][j]] = level;
-            small_append(w[b][j], nxt, qg, cap, &s_nn, prow, &s_ne);
+            small_append(w[b][j], nxt, qg, cap, &s_nn, prow, edges);
           }
     }
     __syncthreads();
@@ -679,7 +692,7 @@ __global__ void __launch_bounds__(1024)
         const unsigned bit = 1u << (w & 31);
         if (atomicOr(visited + (w >> 5), bit) & bit) continue;
         dist[w] = level;
-        small_append(w, nxt, qg, cap, &s_nn, prow, &s_ne);
+        small_append(w, nxt, qg, cap, &s_nn, prow, edges);
       }
     }
     for (int32_t h = 0; h < nh; ++h) {
@@ -691,13 +704,14 @@ __global__ void __launch_bounds__(1024)
         const unsigned bit = 1u << (w & 31);
         if (atomicOr(visited + (w >> 5), bit) & bit) continue;
         dist[w] = level;
-        small_append(w, nxt, qg, cap, &s_nn, prow, &s_ne);
+        small_append(w, nxt, qg, cap, &s_nn, prow, edges);
       }
     }
+    small_edges_flush(edges, &s_ne);
     __syncthreads();
     const int32_t nn = s_nn;
     const unsigned long long ne = s_ne;
-    if (nn == 0 || nn > cap || ne > kSmallEdges) {
+    if (nn == 0 || nn > cap || ne > budget) {
       for (int32_t i = threadIdx.x; i < (nn < cap ? nn : cap); i += blockDim.x) qg[i] = nxt[i];
       if (threadIdx.x == 0) {
         ctr->nf = (unsigned long long)nn;
@@ -1063,7 +1077,7 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
     if (!pull && nf <= small_cap && mf <= (int64_t)kSmallEdges) {
       k_bfs_small<<<1, kSmallThreads, kSmallSmem, ctx->stream>>>(
           P.rowptr, P.colval, sc.q[cur], (int32_t)nf, (int32_t)level, small_cap, sc.visited, dist,
-          sc.ctr);
+          sc.ctr, kSmallEdges);
       GG_CUDA(cudaGetLastError());
       GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
       GG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1276,13 +1290,15 @@ template <typename T>
 __global__ void __launch_bounds__(1024)
     k_sssp_small(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
                  const T* __restrict__ pw, int32_t* qg, int32_t nf0, int32_t cap, T* dist,
-                 unsigned* inq_a, unsigned* inq_b, Counters* ctr, int64_t max_rounds) {
+                 unsigned* inq_a, unsigned* inq_b, Counters* ctr, int64_t max_rounds,
+                 unsigned long long budget) {
   extern __shared__ int32_t smem[];
   int32_t* cur = smem;
   int32_t* nxt = smem + cap;
   int32_t* heavy = smem + 2 * cap;
   __shared__ int32_t s_nn, s_nh;
   __shared__ unsigned long long s_ne;
+  unsigned long long edges = 0;  // out-degrees this thread appended in the current level
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) s_ne = 0;
   for (int32_t i = threadIdx.x; i < nf0; i += blockDim.x) cur[i] = qg[i];
@@ -1293,7 +1309,7 @@ __global__ void __launch_bounds__(1024)
   __syncthreads();
   small_edges(cur, nf0, prow, &s_ne);
   __syncthreads();
-  if (s_ne > kSmallEdges) {  // the starting frontier is already too heavy for one CTA
+  if (s_ne > budget) {  // the starting frontier is already too heavy for one CTA
     if (threadIdx.x == 0) {
       ctr->nf = (unsigned long long)nf0;
       ctr->mf = s_ne;
@@ -1354,7 +1370,7 @@ __global__ void __launch_bounds__(1024)
         for (int j = 0; j < kLightDeg; ++j)
           if (w[b][j] >= 0) {
             const unsigned bit = 1u << (w[b][j] & 31);
-            if (!(atomicOr(in + (w[b][j] >> 5), bit) & bit)) small_append(w[b][j], nxt, qg, cap, &s_nn, prow, &s_ne);
+            if (!(atomicOr(in + (w[b][j] >> 5), bit) & bit)) small_append(w[b][j], nxt, qg, cap, &s_nn, prow, edges);
           }
     }
     __syncthreads();
@@ -1371,7 +1387,7 @@ __global__ void __launch_bounds__(1024)
         if (!(cand < atomic_min_t(dist + w, cand))) continue;
         const unsigned bit = 1u << (w & 31);
         if (atomicOr(in + (w >> 5), bit) & bit) continue;
-        small_append(w, nxt, qg, cap, &s_nn, prow, &s_ne);
+        small_append(w, nxt, qg, cap, &s_nn, prow, edges);
       }
     }
     for (int32_t h = 0; h < nh; ++h) {
@@ -1386,13 +1402,14 @@ __global__ void __launch_bounds__(1024)
         if (!(cand < atomic_min_t(dist + w, cand))) continue;
         const unsigned bit = 1u << (w & 31);
         if (atomicOr(in + (w >> 5), bit) & bit) continue;
-        small_append(w, nxt, qg, cap, &s_nn, prow, &s_ne);
+        small_append(w, nxt, qg, cap, &s_nn, prow, edges);
       }
     }
+    small_edges_flush(edges, &s_ne);
     __syncthreads();
     const int32_t nn = s_nn;
     const unsigned long long ne = s_ne;
-    if (nn == 0 || nn > cap || ne > kSmallEdges || (max_rounds > 0 && (int64_t)rounds >= max_rounds)) {
+    if (nn == 0 || nn > cap || ne > budget || (max_rounds > 0 && (int64_t)rounds >= max_rounds)) {
       if (nn > cap)
         for (int32_t i = threadIdx.x; i < cap; i += blockDim.x) qg[i] = nxt[i];
       else
@@ -1901,7 +1918,7 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
       GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
       k_sssp_small<T><<<1, kSmallThreads, kSmallSmem, ctx->stream>>>(
           P.rowptr, P.colval, static_cast<const T*>(P.w), sc.q[cur], (int32_t)nf, small_cap, d,
-          sc.fb[cur], sc.fb[cur ^ 1], sc.ctr, max_rounds - rounds);
+          sc.fb[cur], sc.fb[cur ^ 1], sc.ctr, max_rounds - rounds, kSmallEdges);
       GG_CUDA(cudaGetLastError());
       GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
       GG_CUDA(cudaStreamSynchronize(ctx->stream));
