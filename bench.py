@@ -524,6 +524,48 @@ def cpu_baseline_search(A, kind, s, mcc, levels_full, budget=40):
 # SpMM: R-MAT scale 22, 32 row-major dense columns
 # ---------------------------------------------------------------------------------
 
+def run_batch(args):
+    """Batched searches on R-MAT scale 22: 256 BFS sources as one bit-packed search and
+    64 Int32 shortest-path sources as two 32-column groups, against the same sources
+    one at a time (queries/s, results compared column by column)."""
+    import statistics
+    import torch
+    import gpugraphs as G
+    from gpugraphs import generators as gen
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    P = rmat(22, gen.W_PATTERN, device)
+    src = sources_for(P, 256, 7)
+    steps = max(1, min(args.steps, 5))
+    tb = time_host(lambda i: G.bfs_distances_batch(P, src), steps, warmup=max(args.warmup, 1))
+    ts = time_host(lambda i: G.bfs_distances(P, int(src[i % 16])), 16)
+    Db = G.bfs_distances_batch(P, src)
+    same_bfs = all(bool((Db[:, q] == G.bfs_distances(P, int(src[q]))).all()) for q in range(0, 256, 37))
+    del P
+    W = rmat(22, gen.W_INT_1_255, device)
+    tsb = time_host(lambda i: G.shortest_path(W, src[:64]), steps, warmup=1)
+    tss = time_host(lambda i: G.shortest_path(W, int(src[i % 16])), 6)
+    Ds = G.shortest_path(W, src[:64])
+    same_sssp = all(bool((Ds[:, q] == G.shortest_path(W, int(src[q]))).all()) for q in (0, 21, 63))
+    qb, q1 = 256 / statistics.median(tb), 1 / statistics.median(ts)
+    qsb, qs1 = 64 / statistics.median(tsb), 1 / statistics.median(tss)
+    out = {
+        "metric": "batched BFS queries/s (256 sources, R-MAT scale 22)", "value": round(qb, 1),
+        "unit": "queries/s", "n_gpus": 1, "steps": steps, "warmup": max(args.warmup, 1),
+        "ms_per_step": round(statistics.median(tb) * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded R-MAT generator on the device)",
+        "config": {"workload": "batch_rmat22", "bfs_sources": 256, "sssp_sources": 64},
+        "bfs": {"batch_queries_per_s": round(qb, 1), "single_queries_per_s": round(q1, 1),
+                "speedup": round(qb / q1, 2), "equal_to_single": same_bfs},
+        "sssp_int32": {"batch_queries_per_s": round(qsb, 1), "single_queries_per_s": round(qs1, 1),
+                       "speedup": round(qsb / qs1, 2), "equal_to_single": same_sssp},
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def run_spmm(args):
     """plus-times Float32 SpMM Y = A X on the R-MAT scale-22 CSR with X of n x 32
     row-major uniform [0,1) (the SpMM half of the scale-22 configuration).  A step is
@@ -848,6 +890,8 @@ def main():
         if args.steps == 50:
             args.steps = 8
         run_search(args, kind, graph)
+    elif args.workload == "batch_rmat22":
+        run_batch(args)
     elif args.workload == "spmm_rmat22":
         run_spmm(args)
     elif args.workload == "serve":

@@ -266,22 +266,41 @@ __device__ __forceinline__ bool bs_pull(const BatchGraph& g, const T* D,
     const int64_t kk = kb + lane;
     int32_t u = -1;
     unsigned cm = 0;
+    T wl = T(0);
     if (kk < k1) {
       const int32_t c = __ldg(g.colval + kk) - 1;
       cm = __ldcg(chg + c);
-      if (cm) u = c;
+      if (cm) {
+        u = c;
+        wl = b_weight<T>(g.nz, g.tv, kk);
+      }
     }
     unsigned act = __ballot_sync(kFullB, u >= 0);
+    // changed in-neighbours 8 at a time: their rows of D are read together, so a warp
+    // keeps up to 8 reads in flight (the minimum does not depend on the order)
     while (act) {
-      const int src_lane = __ffs(act) - 1;
-      act &= act - 1;
-      const int32_t uu = __shfl_sync(kFullB, u, src_lane);
-      const unsigned m = __shfl_sync(kFullB, cm, src_lane);
-      if ((m >> lane) & 1u) {
-        const T w = b_weight<T>(g.nz, g.tv, kb + src_lane);
-        const T cand = b_relax(w, D[(int64_t)uu * 32 + lane]);
-        if (cand < best) best = cand;
-        any = true;
+      int32_t su[8];
+      unsigned sm[8];
+      T sw[8], dv[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int src_lane = act ? __ffs(act) - 1 : 0;
+        const bool valid = act != 0;
+        act &= act - 1;
+        su[t] = __shfl_sync(kFullB, u, src_lane);
+        sm[t] = valid ? __shfl_sync(kFullB, cm, src_lane) : 0u;
+        sw[t] = __shfl_sync(kFullB, wl, src_lane);
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t)
+        dv[t] = ((sm[t] >> lane) & 1u) ? D[(int64_t)su[t] * 32 + lane] : Lim<T>::max();
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        if ((sm[t] >> lane) & 1u) {
+          const T cand = b_relax(sw[t], dv[t]);
+          if (cand < best) best = cand;
+          any = true;
+        }
       }
     }
   }
