@@ -1744,12 +1744,21 @@ __global__ void __launch_bounds__(256)
     const bool hub = k1 - k0 > kHubDegB;  // relaxed by k_sssp_pull_hub
     T best = Lim<T>::max();
     if (v < n && !hub && k1 - k0 <= 32) {
-      for (int64_t k = k0; k < k1; ++k) {
-        const int32_t u = __ldg(cv + k) - 1;
-        if (bit_of(chg, u)) {
-          const T c = relax_add(view_weight<T>(nz, tv, k), ld_cg(dist + u));
-          best = c < best ? c : best;
-        }
+      // 8 in-edges at a time: their columns, membership bits and (weight, distance)
+      // pairs are each loaded together, so a row costs ceil(deg / 8) load chains
+      for (int64_t kb = k0; kb < k1; kb += 8) {
+        int32_t u[8];
+        bool on[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) u[t] = kb + t < k1 ? __ldg(cv + kb + t) - 1 : -1;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) on[t] = u[t] >= 0 && bit_of(chg, u[t]);
+        T c[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+          c[t] = on[t] ? relax_add(view_weight<T>(nz, tv, kb + t), ld_cg(dist + u[t])) : Lim<T>::max();
+#pragma unroll
+        for (int t = 0; t < 8; ++t) best = c[t] < best ? c[t] : best;
       }
     }
     // vertices with 33..kPushHub in-edges: the whole warp scans each
