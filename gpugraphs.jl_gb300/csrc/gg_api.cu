@@ -193,6 +193,7 @@ static void free_mat_storage(gg_mat* A) {
     cudaFree(A->hubplan->hubs);
     cudaFree(A->hubplan->pieces);
     cudaFree(A->hubplan->acc);
+    cudaFree(A->hubplan->mid);
     delete A->hubplan;
     A->hubplan = nullptr;
   }

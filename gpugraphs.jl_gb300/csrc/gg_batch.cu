@@ -42,10 +42,11 @@ int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n) {
   GG_CUDA(cudaMemcpyAsync(rp.data(), rowptr, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost,
                           ctx->stream));
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
-  std::vector<int32_t> hubs;
+  std::vector<int32_t> hubs, mid;
   std::vector<int4> pieces;
   for (int64_t v = 0; v < n; ++v) {
     const int64_t k0 = rp[v] - 1, k1 = rp[v + 1] - 1;
+    if (k1 - k0 > 32 && k1 - k0 <= kHubDegB) mid.push_back((int32_t)v);
     if (k1 - k0 <= kHubDegB) continue;
     const int hi = (int)hubs.size();
     hubs.push_back((int32_t)v);
@@ -55,9 +56,12 @@ int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n) {
   // largest pieces first for the round-robin warp assignment
   std::stable_sort(pieces.begin(), pieces.end(),
                    [](const int4& a, const int4& b) { return (a.z - a.y) > (b.z - b.y); });
+  std::stable_sort(mid.begin(), mid.end(),
+                   [&](int32_t a, int32_t b) { return rp[a + 1] - rp[a] > rp[b + 1] - rp[b]; });
   HubPlan* P = new HubPlan();
   P->nhub = (int64_t)hubs.size();
   P->npiece = (int64_t)pieces.size();
+  P->nmid = (int64_t)mid.size();
   cudaError_t e = cudaSuccess;
   auto up = [&](void** dst, const void* src, size_t bytes) {
     if (e != cudaSuccess) return;
@@ -67,12 +71,14 @@ int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n) {
   };
   up((void**)&P->hubs, hubs.data(), hubs.size() * sizeof(int32_t));
   up((void**)&P->pieces, pieces.data(), pieces.size() * sizeof(int4));
+  up((void**)&P->mid, mid.data(), mid.size() * sizeof(int32_t));
   if (e == cudaSuccess) e = cudaMalloc(&P->acc, (P->nhub + 1) * kMaxW * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     cudaFree(P->hubs);
     cudaFree(P->pieces);
     cudaFree(P->acc);
+    cudaFree(P->mid);
     delete P;
     return cuda_error(e, "hub analysis");
   }

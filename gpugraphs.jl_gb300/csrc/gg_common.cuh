@@ -377,6 +377,9 @@ struct HubPlan {
   int32_t* hubs = nullptr;
   int4* pieces = nullptr;
   void* acc = nullptr;  // per-hub accumulators of the batched BFS (8 words per hub)
+  // rows of 33..kHubDegB entries (0-based), longest first: a warp each in pull rounds
+  int32_t* mid = nullptr;
+  int64_t nmid = 0;
 };
 static const int kHubDegB = 2048;
 static const int kHubPieceB = 2048;

@@ -1761,31 +1761,71 @@ __global__ void __launch_bounds__(256)
         for (int t = 0; t < 8; ++t) best = c[t] < best ? c[t] : best;
       }
     }
-    // vertices with 33..kPushHub in-edges: the whole warp scans each
-    unsigned coop = __ballot_sync(kFullG, v < n && !hub && k1 - k0 > 32);
-    while (coop) {
-      const int h = __ffs(coop) - 1;
-      coop &= coop - 1;
-      const int64_t h0 = __shfl_sync(kFullG, k0, h), h1 = __shfl_sync(kFullG, k1, h);
-      T b = Lim<T>::max();
-      for (int64_t k = h0 + lane; k < h1; k += 32) {
-        const int32_t u = __ldg(cv + k) - 1;
-        if (bit_of(chg, u)) {
-          const T c = relax_add(view_weight<T>(nz, tv, k), ld_cg(dist + u));
-          b = c < b ? c : b;
-        }
-      }
-      b = warp_min_t(b);
-      if (lane == h) best = b;
-    }
+    // rows of 33..kHubDegB in-edges are left to k_sssp_pull_mid (a warp each, spread
+    // over the grid): done here by the vertex's own warp, R-MAT's long rows (low vertex
+    // ids) kept a few SMs busy long after the others had finished
     bool changed = false;
-    if (v < n && !hub && best < dist[v]) {
+    if (v < n && !hub && k1 - k0 <= 32 && best < dist[v]) {
       dist[v] = best;
       changed = true;
     }
     const unsigned word = __ballot_sync(kFullG, changed);
     if (lane == 0 && base + threadIdx.x - lane < n) chg_next[v >> 5] = word;
     warp_append(changed, (int32_t)v, changed ? prow[v + 1] - prow[v] : 0, qn, ctr);
+  }
+}
+
+// rows of 33..kHubDegB in-edges of a pull round (the hub plan's mid list, longest
+// first): a warp takes 32 of them, scans each with the whole warp (128 in-edges per
+// step, loads grouped), keeps row j's minimum in lane j, then lowers the distances
+// (each row has this one writer) and appends the changed rows in one go
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_sssp_pull_mid(const int32_t* __restrict__ rp, const int32_t* __restrict__ cv, const void* nz,
+                    int tv, const unsigned* __restrict__ chg, T* dist, unsigned* chg_next,
+                    int32_t* qn, Counters* ctr, const int32_t* __restrict__ prow,
+                    const int32_t* __restrict__ mid, int64_t nmid) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t g0 = gw * 32; g0 < nmid; g0 += nw * 32) {
+    const int cnt = nmid - g0 < 32 ? (int)(nmid - g0) : 32;
+    T mine = Lim<T>::max();
+    int32_t myv = -1;
+    for (int j = 0; j < cnt; ++j) {
+      const int32_t v = mid[g0 + j];
+      const int64_t k0 = (int64_t)rp[v] - 1, k1 = (int64_t)rp[v + 1] - 1;
+      T b = Lim<T>::max();
+      for (int64_t kb = k0; kb < k1; kb += 128) {
+        int32_t u[4];
+        bool on[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int64_t k = kb + t * 32 + lane;
+          u[t] = k < k1 ? __ldg(cv + k) - 1 : -1;
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) on[t] = u[t] >= 0 && bit_of(chg, u[t]);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const T c = on[t] ? relax_add(view_weight<T>(nz, tv, kb + t * 32 + lane), ld_cg(dist + u[t]))
+                            : Lim<T>::max();
+          b = c < b ? c : b;
+        }
+      }
+      b = warp_min_t(b);
+      if (lane == j) {
+        mine = b;
+        myv = v;
+      }
+    }
+    bool changed = false;
+    if (myv >= 0 && mine < dist[myv]) {
+      dist[myv] = mine;
+      changed = true;
+      atomicOr(chg_next + (myv >> 5), 1u << (myv & 31));
+    }
+    warp_append(changed, myv, changed ? prow[myv + 1] - prow[myv] : 0, qn, ctr);
   }
 }
 
@@ -1852,7 +1892,7 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
   }
   // rows with more than kHubDegB in-edges: relaxed in pieces during pull rounds
   const HubPlan* hp = nullptr;
-  if (g->max_in_deg > kHubDegB) {
+  if (g->max_in_deg > 32) {  // rows the pull kernel's thread-per-vertex path leaves out
     GG_CHECK(build_hub_plan(ctx, A, g->vrowptr, n));
     hp = A->hubplan;
   }
@@ -1952,6 +1992,10 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
       k_sssp_pull<T><<<gridsz(ctx, n), 256, 0, ctx->stream>>>(
           n, g->vrowptr, g->vcolval, g->vnz, A->dtype, sc.fb[cur], d, sc.fb[cur ^ 1], sc.q[cur ^ 1],
           sc.ctr, P.rowptr);
+      if (hp && hp->nmid > 0)
+        k_sssp_pull_mid<T><<<gridsz(ctx, hp->nmid), 256, 0, ctx->stream>>>(
+            g->vrowptr, g->vcolval, g->vnz, A->dtype, sc.fb[cur], d, sc.fb[cur ^ 1], sc.q[cur ^ 1],
+            sc.ctr, P.rowptr, hp->mid, hp->nmid);
       if (hp && hp->npiece > 0)
         k_sssp_pull_hub<T><<<gridsz(ctx, hp->npiece * 32), 256, 0, ctx->stream>>>(
             g->vcolval, g->vnz, A->dtype, sc.fb[cur], d, sc.fb[cur ^ 1], sc.q[cur ^ 1], sc.ctr,
