@@ -177,6 +177,8 @@ __global__ void k_bs_out(const T* D, int64_t n, int64_t S, T* dist, int64_t ld) 
   }
 }
 
+static const int kBsStreams = 8;  // 32-source groups run at once (8 x 32 bytes of ctx->h_flags)
+
 // Work buffers of one batched shortest-path call.  ctr: [0] vertices changed this
 // round, [1] / [2] lengths of the changed queues cq[0] / cq[1], [3] marked vertices.
 template <typename T>
@@ -192,66 +194,104 @@ struct BsWork {
 // Rounds run over every vertex while many vertices change, and over the marked
 // out-neighbours of the changed ones (k_ms_mark) once few do: a round's work then
 // follows the frontier instead of the whole graph.  Both kinds compute the same
-// in-place relaxation, so the fixpoint is unchanged.
+// in-place relaxation, so the fixpoint is unchanged.  One BsRun is one group of up to
+// 32 sources; several groups run at once, each on its own stream, because a single
+// group's rounds are latency-bound and leave most of the GPU idle.
 template <typename T>
-static int bs_group(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, const HubPlan* hp,
-                    const int32_t* prow, const int32_t* pcol, const int64_t* dsrc, int64_t S,
-                    T* dist, int64_t ld, BsWork<T>& w, int64_t* rounds) {
+struct BsRun {
+  BsWork<T> w;
+  cudaStream_t st = nullptr;
+  unsigned long long* h = nullptr;  // pinned counters of the last round
+  const int64_t* dsrc = nullptr;
+  int64_t S = 0, nchanged = 0, r = 0;
+  T* dist = nullptr;
+  int cur = 0;
+  bool restricted = false, done = false;
+};
+
+template <typename T>
+static int bs_alloc(BsWork<T>& w, int64_t n, int64_t qcap, cudaStream_t st) {
+  unsigned* c = nullptr;
+  GG_CUDA(cudaMallocAsync((void**)&w.D, (size_t)n * 32 * sizeof(T), st));
+  GG_CUDA(cudaMallocAsync((void**)&c, ((size_t)2 * n + 64) * sizeof(unsigned), st));
+  GG_CUDA(cudaMallocAsync((void**)&w.cq[0], (size_t)qcap * sizeof(int32_t), st));
+  GG_CUDA(cudaMallocAsync((void**)&w.cq[1], (size_t)qcap * sizeof(int32_t), st));
+  GG_CUDA(cudaMallocAsync((void**)&w.vlist, (size_t)(n + 64) * sizeof(int32_t), st));
+  GG_CUDA(cudaMallocAsync((void**)&w.mark, (size_t)((n + 31) / 32 + 2) * sizeof(unsigned), st));
+  GG_CUDA(cudaMallocAsync((void**)&w.ctr, 64, st));
+  w.c[0] = c;
+  w.c[1] = c + n;
+  return GG_OK;
+}
+
+template <typename T>
+static void bs_free(BsWork<T>& w, cudaStream_t st) {
+  cudaFreeAsync(w.D, st);
+  cudaFreeAsync(w.c[0], st);
+  cudaFreeAsync(w.cq[0], st);
+  cudaFreeAsync(w.cq[1], st);
+  cudaFreeAsync(w.vlist, st);
+  cudaFreeAsync(w.mark, st);
+  cudaFreeAsync(w.ctr, st);
+}
+
+template <typename T>
+static int bs_start(gg_ctx* ctx, int64_t n, BsRun<T>& R) {
+  int64_t gb = (n * 32 + 255) / 256;
+  if (gb > (int64_t)ctx->num_sms * 8) gb = (int64_t)ctx->num_sms * 8;
+  k_bs_init<T><<<(int)gb, 256, 0, R.st>>>(R.w.D, n, R.dsrc, R.S, R.w.c[0]);
+  k_bs_seed<T><<<1, 64, 0, R.st>>>(R.w.D, R.dsrc, R.S, R.w.c[0], R.w.cq[0]);
+  GG_CUDA(cudaGetLastError());
+  R.h[0] = 0;
+  R.h[1] = (unsigned long long)R.S;
+  R.h[2] = 0;
+  R.h[3] = 0;
+  GG_CUDA(cudaMemcpyAsync(R.w.ctr, R.h, 4 * sizeof(unsigned long long), cudaMemcpyHostToDevice, R.st));
+  R.nchanged = R.S;
+  return GG_OK;
+}
+
+// one round of group R, enqueued on its stream; the counters land in R.h
+template <typename T>
+static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, const HubPlan* hp,
+                    const int32_t* prow, const int32_t* pcol, BsRun<T>& R) {
   int64_t gb = (n * 32 + 255) / 256;
   if (gb > (int64_t)ctx->num_sms * 8) gb = (int64_t)ctx->num_sms * 8;
   int64_t pb = (hp->npiece * 32 + 255) / 256;
   if (pb > (int64_t)ctx->num_sms * 8) pb = (int64_t)ctx->num_sms * 8;
   if (pb < 1) pb = 1;
   const int64_t gcap = (int64_t)ctx->num_sms * 8;
-  k_bs_init<T><<<(int)gb, 256, 0, ctx->stream>>>(w.D, n, dsrc, S, w.c[0]);
-  k_bs_seed<T><<<1, 64, 0, ctx->stream>>>(w.D, dsrc, S, w.c[0], w.cq[0]);
-  GG_CUDA(cudaGetLastError());
-  unsigned long long hs[4] = {0, (unsigned long long)S, 0, 0};
-  GG_CUDA(cudaMemcpyAsync(w.ctr, hs, sizeof(hs), cudaMemcpyHostToDevice, ctx->stream));
-  unsigned long long* h = reinterpret_cast<unsigned long long*>(ctx->h_flags);
   const int64_t avg_deg = n > 0 ? (nnz + n - 1) / n : 1;
-  int64_t nchanged = S;
-  int cur = 0;
-  for (int64_t r = 0;; ++r) {
-    if (r > n + 1) return set_error(GG_ERR_NOT_CONVERGED, "batched shortest paths did not converge");
-    unsigned long long* ncq_cur = w.ctr + 1 + cur;
-    unsigned long long* ncq_nxt = w.ctr + 1 + (cur ^ 1);
-    GG_CUDA(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long), ctx->stream));
-    GG_CUDA(cudaMemsetAsync(ncq_nxt, 0, sizeof(unsigned long long), ctx->stream));
-    GG_CUDA(cudaMemsetAsync(w.c[cur ^ 1], 0, (size_t)n * sizeof(unsigned), ctx->stream));
-    const bool restricted = nchanged * avg_deg * 4 < nnz;
-    if (restricted) {
-      GG_CUDA(cudaMemsetAsync(w.mark, 0, ((n + 31) / 32) * sizeof(unsigned), ctx->stream));
-      GG_CUDA(cudaMemsetAsync(w.ctr + 3, 0, sizeof(unsigned long long), ctx->stream));
-      int64_t mb = (nchanged * 32 + 255) / 256;
-      if (mb > gcap) mb = gcap;
-      k_ms_mark<<<(int)(mb < 1 ? 1 : mb), 256, 0, ctx->stream>>>(prow, pcol, w.cq[cur], ncq_cur,
-                                                                 w.mark, w.vlist, w.ctr + 3);
-      k_ms_round<T><<<(int)gcap, 256, 0, ctx->stream>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr,
-                                                        nullptr, w.vlist, w.ctr + 3,
-                                                        w.cq[cur ^ 1], ncq_nxt);
-    } else {
-      k_ms_round<T><<<(int)gb, 256, 0, ctx->stream>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr,
-                                                      nullptr, nullptr, nullptr, w.cq[cur ^ 1],
-                                                      ncq_nxt);
-    }
-    GG_CUDA(cudaGetLastError());
-    if (hp->npiece > 0) {
-      k_ms_round_hub<T><<<(int)pb, 256, 0, ctx->stream>>>(
-          g, hp->pieces, hp->npiece, hp->hubs, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr,
-          restricted ? w.mark : nullptr, w.cq[cur ^ 1], ncq_nxt);
-      GG_CUDA(cudaGetLastError());
-    }
-    GG_CUDA(cudaMemcpyAsync(h, w.ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                            ctx->stream));
-    GG_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (rounds) *rounds += 1;
-    if (h[0] == 0) break;
-    nchanged = (int64_t)h[1 + (cur ^ 1)];
-    cur ^= 1;
+  BsWork<T>& w = R.w;
+  const int cur = R.cur;
+  unsigned long long* ncq_cur = w.ctr + 1 + cur;
+  unsigned long long* ncq_nxt = w.ctr + 1 + (cur ^ 1);
+  GG_CUDA(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long), R.st));
+  GG_CUDA(cudaMemsetAsync(ncq_nxt, 0, sizeof(unsigned long long), R.st));
+  GG_CUDA(cudaMemsetAsync(w.c[cur ^ 1], 0, (size_t)n * sizeof(unsigned), R.st));
+  R.restricted = R.nchanged * avg_deg * 4 < nnz;
+  if (R.restricted) {
+    GG_CUDA(cudaMemsetAsync(w.mark, 0, ((n + 31) / 32) * sizeof(unsigned), R.st));
+    GG_CUDA(cudaMemsetAsync(w.ctr + 3, 0, sizeof(unsigned long long), R.st));
+    int64_t mb = (R.nchanged * 32 + 255) / 256;
+    if (mb > gcap) mb = gcap;
+    k_ms_mark<<<(int)(mb < 1 ? 1 : mb), 256, 0, R.st>>>(prow, pcol, w.cq[cur], ncq_cur, w.mark,
+                                                        w.vlist, w.ctr + 3);
+    k_ms_round<T><<<(int)gcap, 256, 0, R.st>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr,
+                                               w.vlist, w.ctr + 3, w.cq[cur ^ 1], ncq_nxt);
+  } else {
+    k_ms_round<T><<<(int)gb, 256, 0, R.st>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr,
+                                             nullptr, nullptr, w.cq[cur ^ 1], ncq_nxt);
   }
-  k_bs_out<T><<<(int)gb, 256, 0, ctx->stream>>>(w.D, n, S, dist, ld);
   GG_CUDA(cudaGetLastError());
+  if (hp->npiece > 0) {
+    k_ms_round_hub<T><<<(int)pb, 256, 0, R.st>>>(g, hp->pieces, hp->npiece, hp->hubs, w.D,
+                                                 w.c[cur], w.c[cur ^ 1], w.ctr, nullptr,
+                                                 R.restricted ? w.mark : nullptr, w.cq[cur ^ 1],
+                                                 ncq_nxt);
+    GG_CUDA(cudaGetLastError());
+  }
+  GG_CUDA(cudaMemcpyAsync(R.h, w.ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, R.st));
   return GG_OK;
 }
 
@@ -266,34 +306,87 @@ static int sssp_batch_t(gg_ctx* ctx, gg_mat* A, const BatchGraph& g, const int64
   const HubPlan* hp = A->hubplan;
   // a hub may enter a changed queue once per piece
   const int64_t qcap = n + hp->npiece + 64;
-  BsWork<T> w;
-  unsigned* c = nullptr;
+  const int64_t nnz = (int64_t)A->nnz;
+  const int64_t ngroups = (S + 31) / 32;
+  const int64_t conc = ngroups < kBsStreams ? ngroups : kBsStreams;  // groups at once
   int64_t* dsrc = nullptr;
-  GG_CUDA(cudaMallocAsync((void**)&w.D, (size_t)n * 32 * sizeof(T), ctx->stream));
-  GG_CUDA(cudaMallocAsync((void**)&c, ((size_t)2 * n + 64) * sizeof(unsigned), ctx->stream));
-  GG_CUDA(cudaMallocAsync((void**)&w.cq[0], (size_t)qcap * sizeof(int32_t), ctx->stream));
-  GG_CUDA(cudaMallocAsync((void**)&w.cq[1], (size_t)qcap * sizeof(int32_t), ctx->stream));
-  GG_CUDA(cudaMallocAsync((void**)&w.vlist, (size_t)(n + 64) * sizeof(int32_t), ctx->stream));
-  GG_CUDA(cudaMallocAsync((void**)&w.mark, (size_t)((n + 31) / 32 + 2) * sizeof(unsigned), ctx->stream));
-  GG_CUDA(cudaMallocAsync((void**)&w.ctr, 64, ctx->stream));
   GG_CUDA(cudaMallocAsync((void**)&dsrc, (size_t)S * sizeof(int64_t) + 8, ctx->stream));
   GG_CUDA(cudaMemcpyAsync(dsrc, sources, S * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
-  w.c[0] = c;
-  w.c[1] = c + n;
-  const int64_t nnz = (int64_t)A->nnz;
+  cudaEvent_t ready;
+  GG_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  GG_CUDA(cudaEventRecord(ready, ctx->stream));
+  std::vector<BsRun<T>> runs(conc);
+  unsigned long long* hbase = reinterpret_cast<unsigned long long*>(ctx->h_flags);
   int rc = GG_OK;
-  for (int64_t q0 = 0; q0 < S && rc == GG_OK; q0 += 32) {
-    const int64_t Sg = S - q0 < 32 ? S - q0 : 32;
-    rc = bs_group<T>(ctx, n, nnz, g, hp, prow, pcol, dsrc + q0, Sg, dist + q0 * ld, ld, w, rounds);
+  for (int64_t i = 0; i < conc && rc == GG_OK; ++i) {
+    BsRun<T>& R = runs[i];
+    if (cudaStreamCreateWithFlags(&R.st, cudaStreamNonBlocking) != cudaSuccess) {
+      R.st = nullptr;
+      rc = set_error(GG_ERR_CUDA, "stream creation failed");
+      break;
+    }
+    R.h = hbase + 4 * i;
+    if (cudaStreamWaitEvent(R.st, ready, 0) != cudaSuccess) rc = set_error(GG_ERR_CUDA, "stream wait");
+    if (rc == GG_OK) rc = bs_alloc<T>(R.w, n, qcap, R.st);
+    R.done = true;  // not started
   }
-  cudaFreeAsync(w.D, ctx->stream);
-  cudaFreeAsync(c, ctx->stream);
-  cudaFreeAsync(w.cq[0], ctx->stream);
-  cudaFreeAsync(w.cq[1], ctx->stream);
-  cudaFreeAsync(w.vlist, ctx->stream);
-  cudaFreeAsync(w.mark, ctx->stream);
-  cudaFreeAsync(w.ctr, ctx->stream);
+  int64_t next_group = 0;
+  auto start_next = [&](BsRun<T>& R) -> int {
+    if (next_group >= ngroups) return GG_OK;
+    const int64_t q0 = next_group * 32;
+    R.S = S - q0 < 32 ? S - q0 : 32;
+    R.dsrc = dsrc + q0;
+    R.dist = dist + q0 * ld;
+    R.cur = 0;
+    R.r = 0;
+    R.done = false;
+    ++next_group;
+    return bs_start<T>(ctx, n, R);
+  };
+  for (int64_t i = 0; i < conc && rc == GG_OK; ++i) rc = start_next(runs[i]);
+  int64_t gb = (n * 32 + 255) / 256;
+  if (gb > (int64_t)ctx->num_sms * 8) gb = (int64_t)ctx->num_sms * 8;
+  bool active = rc == GG_OK;
+  while (active && rc == GG_OK) {
+    active = false;
+    for (auto& R : runs)
+      if (!R.done && rc == GG_OK) rc = bs_issue<T>(ctx, n, nnz, g, hp, prow, pcol, R);
+    for (auto& R : runs) {
+      if (R.done || rc != GG_OK) continue;
+      if (cudaStreamSynchronize(R.st) != cudaSuccess) {
+        rc = cuda_error(cudaGetLastError(), "batched shortest paths");
+        break;
+      }
+      if (rounds) *rounds += 1;
+      ++R.r;
+      if (R.h[0] == 0) {  // converged: write the group out, take the next one
+        k_bs_out<T><<<(int)gb, 256, 0, R.st>>>(R.w.D, n, R.S, R.dist, ld);
+        R.done = true;
+        rc = start_next(R);
+      } else if (R.r > n + 1) {
+        rc = set_error(GG_ERR_NOT_CONVERGED, "batched shortest paths did not converge");
+      } else {
+        R.nchanged = (int64_t)R.h[1 + (R.cur ^ 1)];
+        R.cur ^= 1;
+      }
+      if (!R.done) active = true;
+    }
+  }
+  // join: the caller's stream waits for every group's last work
+  for (auto& R : runs) {
+    if (!R.st) continue;
+    bs_free<T>(R.w, R.st);
+    cudaEvent_t fin;
+    if (cudaEventCreateWithFlags(&fin, cudaEventDisableTiming) == cudaSuccess) {
+      cudaEventRecord(fin, R.st);
+      cudaStreamWaitEvent(ctx->stream, fin, 0);
+      cudaEventDestroy(fin);
+    }
+    cudaStreamDestroy(R.st);
+  }
+  cudaEventDestroy(ready);
   cudaFreeAsync(dsrc, ctx->stream);
+  if (rc == GG_OK) GG_CUDA(cudaGetLastError());
   return rc;
 }
 

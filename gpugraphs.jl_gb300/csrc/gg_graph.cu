@@ -1786,7 +1786,8 @@ __global__ void __launch_bounds__(256)
                     int32_t* qn, Counters* ctr, const int32_t* __restrict__ prow,
                     const int32_t* __restrict__ mid, int64_t nmid) {
   const int lane = threadIdx.x & 31;
-  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // warps numbered block-major: the longest groups go to different SMs
+  const int64_t gw = (int64_t)(threadIdx.x >> 5) * gridDim.x + blockIdx.x;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t g0 = gw * 32; g0 < nmid; g0 += nw * 32) {
     const int cnt = nmid - g0 < 32 ? (int)(nmid - g0) : 32;
