@@ -646,12 +646,13 @@ def run_serve(args):
             g = int(rng.choice(flts))
         return kind, g, int(rng.integers(1, graphs[g].n + 1))
 
-    # plain path: one query at a time
+    # plain path: one query at a time, every graph's per-matrix analysis built first
+    # (each kind runs once per graph before the timed queries)
     plain_lat = []
     nplain = max(30, args.steps)
-    for _ in range(3):
-        kind, g, s = draw()
-        _single(G, graphs, xs, kind, g, s)
+    for g in range(16):
+        for kind in ((0, 1) if g in ints else (1, 2)):
+            _single(G, graphs, xs, kind, g, 1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(nplain):

@@ -368,6 +368,70 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// One dense column (a served SpMV iteration runs as an n x 1 SpMM so that it folds
+// exactly like a column of the 32-column executor): a thread per row of <= 32 entries
+// and a thread per item (rows of 33..kSegMM entries, pieces of longer rows), each
+// folded in storage order 8 entries per load group, NaN sums folded again with the
+// stop at +Inf.  The warp-per-row kernel leaves 31 of 32 lanes idle on one column.
+__device__ __forceinline__ float col1_fold(const int32_t* __restrict__ colval,
+                                           const float* __restrict__ nz, const float* B, int64_t ldb,
+                                           int32_t k0, int32_t k1, uint64_t pol_s, uint64_t pol_b) {
+  float acc = 0.0f;
+  for (int32_t kb = k0; kb < k1; kb += 8) {
+    int32_t c[8];
+    float a[8], b[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const bool in = kb + t < k1;
+      c[t] = in ? ld_stream_p(colval + kb + t, pol_s) - 1 : 0;
+      a[t] = in ? ld_stream_p(nz + kb + t, pol_s) : 0.0f;
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) b[t] = kb + t < k1 ? ld_keep(B + (int64_t)c[t] * ldb, pol_b) : 0.0f;
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (kb + t < k1) acc = __fadd_rn(acc, __fmul_rn(a[t], b[t]));
+  }
+  if (acc != acc) {
+    acc = 0.0f;
+    for (int32_t k = k0; k < k1; ++k) {
+      acc = __fadd_rn(acc, __fmul_rn(__ldg(nz + k), __ldg(B + (int64_t)(__ldg(colval + k) - 1) * ldb)));
+      if (acc == __int_as_float(0x7f800000)) break;
+    }
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(256)
+    k_spmm_col1_short(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colval,
+                      const float* __restrict__ nz, const float* __restrict__ B, int64_t ldb,
+                      float* __restrict__ C, int64_t ldc, int64_t row_lo, int64_t nrows) {
+  const uint64_t pol_s = l2_evict_first(), pol_b = l2_evict_last();
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nrows;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = row_lo + t;
+    const int32_t k0 = __ldg(rowptr + r) - 1, k1 = __ldg(rowptr + r + 1) - 1;
+    if (k1 - k0 > kShortMM) continue;
+    C[r * ldc] = col1_fold(colval, nz, B, ldb, k0, k1, pol_s, pol_b);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_spmm_col1_items(const int32_t* __restrict__ colval, const float* __restrict__ nz,
+                      const float* __restrict__ B, int64_t ldb, float* __restrict__ C, int64_t ldc,
+                      const int4* __restrict__ items, int64_t nitems, int64_t row_lo, int64_t row_hi,
+                      float* partials) {
+  const uint64_t pol_s = l2_evict_first(), pol_b = l2_evict_last();
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nitems;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int4 d = items[t];  // row, first entry, end entry, partial slot or -1
+    if (d.x < row_lo || d.x >= row_hi) continue;
+    const float v = col1_fold(colval, nz, B, ldb, d.y, d.z, pol_s, pol_b);
+    if (d.w < 0) C[(int64_t)d.x * ldc] = v;
+    else partials[d.w] = v;
+  }
+}
+
 static int grid_mm(gg_ctx* ctx, int64_t warps);
 
 // which semirings / operands take the short-row kernel
@@ -378,6 +442,9 @@ struct ShortRowsMM {
                      int64_t) {}
   static void launch_items(gg_ctx*, const SR&, const int32_t*, const MMPlan*, int64_t, int64_t,
                            int64_t, int64_t, typename SR::T*) {}
+  static bool ok1(const SR&, int64_t, const void*) { return false; }
+  static void launch1(gg_ctx*, const SR&, const int32_t*, const int32_t*, const MMPlan*, int64_t,
+                      int64_t, int64_t, typename SR::T*) {}
 };
 template <>
 struct ShortRowsMM<SRPlusTimesF32MM> {
@@ -390,6 +457,19 @@ struct ShortRowsMM<SRPlusTimesF32MM> {
                      const int32_t* colval, int64_t row_lo, int64_t nrows, int64_t jlo, int64_t jn) {
     k_spmm_short_f32x4<<<grid_mm(ctx, (nrows + 3) / 4), 256, 0, ctx->stream>>>(
         rowptr, colval, sr.nz, sr.x, sr.ldb, sr.y, sr.ldc, row_lo, nrows, jlo, jn);
+  }
+  // one dense column, no mask: the thread-per-row kernels
+  static bool ok1(const SRPlusTimesF32MM&, int64_t jn, const void* mask) { return !mask && jn == 1; }
+  static void launch1(gg_ctx* ctx, const SRPlusTimesF32MM& sr, const int32_t* rowptr,
+                      const int32_t* colval, const MMPlan* P, int64_t row_lo, int64_t row_hi,
+                      int64_t jlo, float* partials) {
+    const int64_t nrows = row_hi - row_lo;
+    k_spmm_col1_short<<<grid_mm(ctx, (nrows + 31) / 32), 256, 0, ctx->stream>>>(
+        rowptr, colval, sr.nz, sr.x + jlo, sr.ldb, sr.y + jlo, sr.ldc, row_lo, nrows);
+    if (P->nitems > 0)
+      k_spmm_col1_items<<<grid_mm(ctx, (P->nitems + 31) / 32), 256, 0, ctx->stream>>>(
+          colval, sr.nz, sr.x + jlo, sr.ldb, sr.y + jlo, sr.ldc, P->items, P->nitems, row_lo, row_hi,
+          partials);
   }
   static void launch_items(gg_ctx* ctx, const SRPlusTimesF32MM& sr, const int32_t* colval,
                            const MMPlan* P, int64_t row_lo, int64_t row_hi, int64_t jlo, int64_t jn,
@@ -510,7 +590,11 @@ static int launch_mm(gg_ctx* ctx, gg_mat* A, const SR& sr, int64_t k, const void
       // plus-times Float32 on 16-byte aligned row-major operands: rows of <= 32 entries
       // go to the four-rows-per-warp float4 kernel
       int32_t skip = -1;  // rows of at most `skip` entries are left to the short-row kernel
-      if (ShortRowsMM<SR>::ok(sr, jlo, jn, mask)) {
+      if (ShortRowsMM<SR>::ok1(sr, jn, mask)) {
+        tr = trace_main_begin(ctx);
+        ShortRowsMM<SR>::launch1(ctx, sr, A->rowptr, A->colval, P, row_lo, row_hi, jlo, partials);
+        if (P->nitems > 0) trace_count(ctx, 1);  // the second of the two kernels
+      } else if (ShortRowsMM<SR>::ok(sr, jlo, jn, mask)) {
         // Float32 fast path: short rows four per warp, the rest (medium rows and the
         // pieces of long rows) by the item kernel
         ShortRowsMM<SR>::launch(ctx, sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn);
