@@ -691,6 +691,29 @@ def run_serve(args):
         sweep.append({"lambda": lam, "requests": nreq, "offered_qps": round(nreq / t_sub, 1),
                       "qps": round(nreq / t_all, 1), "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
                       "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3)})
+    # per kind at saturation (every request submitted at once) against the same kind
+    # one query at a time
+    per_kind = {}
+    for kind, name in ((0, "bfs"), (1, "sssp")):
+        pool = ints if kind == 0 else list(range(16))
+        reqs = [(int(rng.choice(pool)),) for _ in range(1500)]
+        reqs = [(g, int(rng.integers(1, graphs[g].n + 1))) for (g,) in reqs]
+        t0 = time.perf_counter()
+        for g, s in reqs:
+            (srv.submit_bfs if kind == 0 else srv.submit_sssp)(ids[g], s)
+        done = srv.wait(timeout=600)
+        t_all = time.perf_counter() - t0
+        lat = np.array(sorted(v[1] for v in done.values()))
+        tp = time.perf_counter()
+        for g, s in reqs[:40]:
+            _single(G, graphs, xs, kind, g, s)
+            torch.cuda.synchronize()
+        plain_k = 40 / (time.perf_counter() - tp)
+        per_kind[name] = {"served_qps": round(len(reqs) / t_all, 1),
+                          "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                          "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3),
+                          "plain_qps": round(plain_k, 1),
+                          "speedup_vs_plain": round(len(reqs) / t_all / plain_k, 2)}
     clocks = clk.stop()
     st = srv.stats()
     srv.close()
@@ -707,6 +730,7 @@ def run_serve(args):
         "plain_path": {"qps": round(plain_qps, 1), "p50_ms": round(float(np.percentile(pl, 50)) * 1e3, 3),
                        "p99_ms": round(float(np.percentile(pl, 99)) * 1e3, 3), "queries": nplain},
         "speedup_vs_plain": round(best["qps"] / plain_qps, 2),
+        "per_kind_saturation": per_kind,
         "server_stats": st,
         "e2e": None, "gpu_launches": None, "clocks": clocks,
     }
