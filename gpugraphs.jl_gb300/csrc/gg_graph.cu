@@ -865,6 +865,30 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
 // larger than cap.  Same counters, queues and semantics as k_bfs_coop.
 static const int kClusterCtas = 8;
 static const long long kClusterCap = 65536;
+static const int kStageCap = 8192;  // per-CTA shared staging of a level's new vertices
+
+// appends to the CTA's shared staging buffer (one shared atomic per warp); claims past
+// kStageCap go straight to the global queue
+__device__ __forceinline__ void stage_append(bool want, int32_t v, int32_t* sbuf, int* scnt,
+                                             int32_t* q, unsigned long long* cnt) {
+  const int lane = threadIdx.x & 31;
+  const unsigned b = __ballot_sync(kFullG, want);
+  if (!b) return;
+  const int leader = __ffs(b) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(scnt, __popc(b));
+  base = __shfl_sync(kFullG, base, leader);
+  const int pos = base + __popc(b & ((1u << lane) - 1u));
+  const bool fits = pos < kStageCap;
+  if (want && fits) sbuf[pos] = v;
+  const unsigned over = __ballot_sync(kFullG, want && !fits);
+  if (!over) return;
+  const int l2 = __ffs(over) - 1;
+  unsigned long long gbase = 0;
+  if (lane == l2) gbase = atomicAdd(cnt, (unsigned long long)__popc(over));
+  gbase = __shfl_sync(kFullG, gbase, l2);
+  if (want && !fits) q[gbase + __popc(over & ((1u << lane) - 1u))] = v;
+}
 
 __device__ __forceinline__ void cluster_barrier() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
@@ -875,6 +899,9 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kCoopThre
     k_bfs_cluster(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol, int32_t* qa,
                   int32_t* qb, unsigned* visited, int32_t* dist, CoopCtl* cc, int32_t level0,
                   long long cap) {
+  __shared__ int32_t sbuf[kStageCap];
+  __shared__ int scnt;
+  __shared__ unsigned long long sbase;
   const int lane = threadIdx.x & 31;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nt = (int64_t)gridDim.x * blockDim.x;
@@ -892,6 +919,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kCoopThre
       return;  // every CTA of the cluster reads the same nf and leaves here
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) cc->cnt[(r + 1) % 3] = 0;
+    if (threadIdx.x == 0) scnt = 0;
+    __syncthreads();
     const int32_t level = level0 + st + 1;
     for (int64_t i0 = gt - lane; i0 < nf; i0 += nt) {
       const int64_t i = i0 + lane;
@@ -913,12 +942,19 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kCoopThre
         if (k0 + j < k1) {
           w = __ldg(pcol + k0 + j);
           const unsigned bit = 1u << (w & 31);
-          if (!(__ldcg(visited + (w >> 5)) & bit)) claim = !(atomicOr(visited + (w >> 5), bit) & bit);
+          // claimed by the atomic alone: one L2 round trip on this level's critical path
+          claim = !(atomicOr(visited + (w >> 5), bit) & bit);
           if (claim) dist[w] = level;
         }
-        coop_append(claim, w, nxt, &cc->cnt[r]);
+        stage_append(claim, w, sbuf, &scnt, nxt, &cc->cnt[r]);
       }
     }
+    // the CTA's staged vertices: one global reservation, then a coalesced copy
+    __syncthreads();
+    const int ns = scnt < kStageCap ? scnt : kStageCap;
+    if (threadIdx.x == 0) sbase = ns ? atomicAdd(&cc->cnt[r], (unsigned long long)ns) : 0ull;
+    __syncthreads();
+    for (int i = threadIdx.x; i < ns; i += blockDim.x) nxt[sbase + i] = sbuf[i];
     __threadfence();
     cluster_barrier();
     int32_t* t = cur;
