@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "gg_semiring.cuh"
+#include "gg_tma.cuh"
 
 namespace gg {
 
@@ -862,21 +863,44 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
 // barrier: no polling), which costs far less than a grid barrier over every SM.  It
 // serves the long tail of small frontiers of high-diameter graphs (a 4096 x 4096 grid
 // has 7439 levels of at most ~8000 vertices); it exits when the frontier is empty or
-// larger than cap.  Same counters, queues and semantics as k_bfs_coop.
+// larger than cap.  The frontier never leaves the cluster: every CTA keeps the
+// vertices it claimed in its own shared memory, the CTAs read each other's queues and
+// counts through distributed shared memory (mapa + ld.shared::cluster), and the
+// barrier's release / acquire orders them -- a level costs the L2 round trips of its
+// row pointers, columns and visited bits, not also a queue and counter in global
+// memory and a fence.  A CTA's claims past kStageCap spill to qb (global counter
+// cc->cnt[1]) and end the kernel after that level.  On exit the frontier is written
+// to qa (CTA shares in rank order, then the spills).
 static const int kClusterCtas = 8;
-static const long long kClusterCap = 65536;
-static const int kStageCap = 8192;  // per-CTA shared staging of a level's new vertices
+static const long long kClusterCap = 32768;
+static const int kStageCap = 4096;  // per-CTA queue (kClusterCap / kClusterCtas)
+static const int kSpillBit = 1 << 30;
 
-// appends to the CTA's shared staging buffer (one shared atomic per warp); claims past
-// kStageCap go straight to the global queue
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
+__device__ __forceinline__ uint32_t dsmem_addr(const void* p, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ int32_t dsmem_ld(uint32_t a) {
+  int32_t v;
+  asm volatile("ld.shared::cluster.b32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+  return v;
+}
+
+// appends to the CTA's queue (one shared atomic per warp); claims past kStageCap go to
+// the spill queue (one global atomic per warp) and mark the count with kSpillBit
 __device__ __forceinline__ void stage_append(bool want, int32_t v, int32_t* sbuf, int* scnt,
-                                             int32_t* q, unsigned long long* cnt) {
+                                             int32_t* spill, unsigned long long* nspill) {
   const int lane = threadIdx.x & 31;
   const unsigned b = __ballot_sync(kFullG, want);
   if (!b) return;
   const int leader = __ffs(b) - 1;
   int base = 0;
-  if (lane == leader) base = atomicAdd(scnt, __popc(b));
+  if (lane == leader) base = atomicAdd(scnt, __popc(b)) & (kSpillBit - 1);
   base = __shfl_sync(kFullG, base, leader);
   const int pos = base + __popc(b & ((1u << lane) - 1u));
   const bool fits = pos < kStageCap;
@@ -885,48 +909,77 @@ __device__ __forceinline__ void stage_append(bool want, int32_t v, int32_t* sbuf
   if (!over) return;
   const int l2 = __ffs(over) - 1;
   unsigned long long gbase = 0;
-  if (lane == l2) gbase = atomicAdd(cnt, (unsigned long long)__popc(over));
+  if (lane == l2) {
+    gbase = atomicAdd(nspill, (unsigned long long)__popc(over));
+    atomicOr(scnt, kSpillBit);
+  }
   gbase = __shfl_sync(kFullG, gbase, l2);
-  if (want && !fits) q[gbase + __popc(over & ((1u << lane) - 1u))] = v;
-}
-
-__device__ __forceinline__ void cluster_barrier() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
-                   : "memory");
+  if (want && !fits) spill[gbase + __popc(over & ((1u << lane) - 1u))] = v;
 }
 
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kCoopThreads, 1)
     k_bfs_cluster(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol, int32_t* qa,
                   int32_t* qb, unsigned* visited, int32_t* dist, CoopCtl* cc, int32_t level0,
                   long long cap) {
-  __shared__ int32_t sbuf[kStageCap];
-  __shared__ int scnt;
-  __shared__ unsigned long long sbase;
+  __shared__ int32_t sq[2][kStageCap];
+  __shared__ int s_cnt[2];
+  __shared__ int s_pre[kClusterCtas + 1];
+  __shared__ int s_spill;
+  const int rank = blockIdx.x;  // the grid is one cluster
   const int lane = threadIdx.x & 31;
-  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t nt = (int64_t)gridDim.x * blockDim.x;
-  int32_t* cur = qa;
-  int32_t* nxt = qb;
+  const int64_t gt = (int64_t)rank * blockDim.x + threadIdx.x;
+  const int64_t nt = (int64_t)kClusterCtas * blockDim.x;
+  {  // an even share of the starting frontier (at most kClusterCap) per CTA
+    const long long nf0 = (long long)*((volatile unsigned long long*)&cc->cnt[2]);
+    const long long lo = nf0 * rank / kClusterCtas, hi = nf0 * (rank + 1) / kClusterCtas;
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) sq[0][i - lo] = qa[i];
+    if (threadIdx.x == 0) {
+      s_cnt[0] = (int)(hi - lo);
+      s_cnt[1] = 0;
+    }
+  }
+  cluster_barrier();
   for (int st = 0;; ++st) {
-    const int r = st % 3;
-    const long long nf = (long long)*((volatile unsigned long long*)&cc->cnt[(r + 2) % 3]);
-    if (nf == 0 || nf > cap) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const int p = st & 1;
+    // every CTA's count of this level's frontier, through distributed shared memory
+    if (threadIdx.x < kClusterCtas) s_pre[threadIdx.x + 1] = dsmem_ld(dsmem_addr(&s_cnt[p], threadIdx.x));
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int sp = 0;
+      s_pre[0] = 0;
+      for (int c = 0; c < kClusterCtas; ++c) {
+        const int v = s_pre[c + 1];
+        sp |= v & kSpillBit;
+        const int k = v & (kSpillBit - 1);
+        s_pre[c + 1] = s_pre[c] + (k < kStageCap ? k : kStageCap);
+      }
+      s_spill = sp;
+      s_cnt[p ^ 1] = 0;  // next level's queue (nobody reads it during this level)
+    }
+    __syncthreads();
+    const long long nsp = s_spill ? (long long)*((volatile unsigned long long*)&cc->cnt[1]) : 0;
+    const long long nf = (long long)s_pre[kClusterCtas] + nsp;
+    if (nf == 0 || nf > cap || s_spill) {
+      const int mine = s_pre[rank + 1] - s_pre[rank];
+      for (int i = threadIdx.x; i < mine; i += blockDim.x) qa[s_pre[rank] + i] = sq[p][i];
+      for (long long i = gt; i < nsp; i += nt) qa[s_pre[kClusterCtas] + i] = qb[i];
+      if (rank == 0 && threadIdx.x == 0) {
         cc->nf_out = nf;
         cc->level_out = level0 + st;
-        cc->which_out = st & 1;
+        cc->which_out = 0;
       }
-      return;  // every CTA of the cluster reads the same nf and leaves here
+      cluster_barrier();  // no CTA leaves while another may still read its queue
+      return;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) cc->cnt[(r + 1) % 3] = 0;
-    if (threadIdx.x == 0) scnt = 0;
-    __syncthreads();
     const int32_t level = level0 + st + 1;
+    int32_t* nxt = sq[p ^ 1];
     for (int64_t i0 = gt - lane; i0 < nf; i0 += nt) {
       const int64_t i = i0 + lane;
       int32_t k0 = 0, k1 = 0;
       if (i < nf) {
-        const int32_t u = cur[i];
+        int r = 0;
+        while (r + 1 < kClusterCtas && s_pre[r + 1] <= i) ++r;
+        const int32_t u = dsmem_ld(dsmem_addr(&sq[p][i - s_pre[r]], (uint32_t)r));
         k0 = __ldg(prow + u);
         k1 = __ldg(prow + u + 1);
       }
@@ -946,20 +999,10 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kCoopThre
           claim = !(atomicOr(visited + (w >> 5), bit) & bit);
           if (claim) dist[w] = level;
         }
-        stage_append(claim, w, sbuf, &scnt, nxt, &cc->cnt[r]);
+        stage_append(claim, w, nxt, &s_cnt[p ^ 1], qb, &cc->cnt[1]);
       }
     }
-    // the CTA's staged vertices: one global reservation, then a coalesced copy
-    __syncthreads();
-    const int ns = scnt < kStageCap ? scnt : kStageCap;
-    if (threadIdx.x == 0) sbase = ns ? atomicAdd(&cc->cnt[r], (unsigned long long)ns) : 0ull;
-    __syncthreads();
-    for (int i = threadIdx.x; i < ns; i += blockDim.x) nxt[sbase + i] = sbuf[i];
-    __threadfence();
     cluster_barrier();
-    int32_t* t = cur;
-    cur = nxt;
-    nxt = t;
   }
 }
 
