@@ -492,10 +492,25 @@ def run_search(args, kind, graph):
     value = mcc / t / 1e9
     B = (bfs_bytes if kind == "bfs" else sssp_bytes)(n, nnz)
     peak, peak_kind = peak_hbm()
-    # e2e: the result copied back to pinned host memory each query
-    host = torch.empty(n, dtype=d0.dtype).pin_memory()
-    te = time_host(lambda i: host.copy_(run(i)), max(3, args.steps // 2), warmup=1)
-    e2e = mcc / (sum(te) / len(te)) / 1e9
+    # e2e: every query's result copied back to pinned host memory; the copy of query i
+    # runs on a side stream while query i + 1 searches (two host buffers)
+    host = [torch.empty(n, dtype=d0.dtype).pin_memory() for _ in range(2)]
+    side = torch.cuda.Stream(device)
+    cur_s = torch.cuda.current_stream(device)
+
+    def e2e_run(k):
+        t0 = time.perf_counter()
+        for i in range(k):
+            d = run(i)
+            side.wait_stream(cur_s)
+            with torch.cuda.stream(side):
+                host[i & 1].copy_(d, non_blocking=True)
+                d.record_stream(side)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / k
+
+    e2e_run(1)
+    e2e = mcc / e2e_run(max(3, args.steps // 2)) / 1e9
     out = {
         "metric": "%s GTEPS (%s)" % ("BFS" if kind == "bfs" else "Bellman-Ford", cfg),
         "value": round(value * ws, 3), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
@@ -508,7 +523,9 @@ def run_search(args, kind, graph):
                      "frac": round(B / t / 1e9 / peak, 4), "traffic": traffic_from_profiles("%s_%s" % (kind, graph)),
                      "peak_kind": peak_kind, "algorithmic_bytes": B},
         "e2e": {"value": round(e2e * ws, 3), "unit": "GTEPS", "h2d_bytes_per_step": 8,
-                "d2h_bytes_per_step": n * d0.element_size()},
+                "d2h_bytes_per_step": n * d0.element_size(),
+                "schedule": "each query's result copied to pinned host memory on a side stream "
+                            "while the next query searches"},
         "gpu_launches": None,
         "clocks": clocks,
     }
