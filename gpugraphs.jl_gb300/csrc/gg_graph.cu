@@ -1030,6 +1030,7 @@ struct BfsScratch {
   int32_t* q[2];
   int32_t* hq;  // deferred frontier hubs (the first far list of near-far searches)
   int32_t* q2;  // the second far list
+  int32_t* q3;  // the third far list
   Counters* ctr;
   CoopCtl* cc;
 };
@@ -1038,7 +1039,7 @@ static int bfs_scratch(gg_ctx* ctx, int64_t n, BfsScratch* s) {
   const int64_t nw = (n + 31) / 32 + 1;
   const size_t bm = ((nw * sizeof(unsigned)) + 255) & ~(size_t)255;
   const size_t qb = (((n + 1) * sizeof(int32_t)) + 255) & ~(size_t)255;
-  GG_CHECK(ensure_scratch(ctx, 3 * bm + 4 * qb + 512));
+  GG_CHECK(ensure_scratch(ctx, 3 * bm + 5 * qb + 512));
   char* p = static_cast<char*>(ctx->scratch);
   s->visited = (unsigned*)p;
   s->fb[0] = (unsigned*)(p + bm);
@@ -1047,8 +1048,9 @@ static int bfs_scratch(gg_ctx* ctx, int64_t n, BfsScratch* s) {
   s->q[1] = (int32_t*)(p + 3 * bm + qb);
   s->hq = (int32_t*)(p + 3 * bm + 2 * qb);
   s->q2 = (int32_t*)(p + 3 * bm + 3 * qb);
-  s->ctr = (Counters*)(p + 3 * bm + 4 * qb);
-  s->cc = (CoopCtl*)(p + 3 * bm + 4 * qb + 256);
+  s->q3 = (int32_t*)(p + 3 * bm + 4 * qb);
+  s->ctr = (Counters*)(p + 3 * bm + 5 * qb);
+  s->cc = (CoopCtl*)(p + 3 * bm + 5 * qb + 256);
   GG_CUDA(cudaMemsetAsync(p, 0, 3 * bm, ctx->stream));
   return GG_OK;
 }
@@ -1630,7 +1632,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
 // barriers are bounded (coop_grid_sync); the number of steps is bounded by max_steps.
 struct NfCtl {
   unsigned long long cnt[3];  // near queue lengths, rotating as in CoopCtl
-  unsigned long long fcnt[2];  // far list lengths
+  unsigned long long fcnt[3];  // far list lengths (three lists in rotation)
   unsigned bar[4];
   long long steps_out;
   int status;  // 1 finished, 2 step budget exhausted
@@ -1640,7 +1642,7 @@ __global__ void k_nf_init(NfCtl* cc, long long nf0) {
   cc->cnt[0] = 0;
   cc->cnt[1] = 0;
   cc->cnt[2] = (unsigned long long)nf0;
-  cc->fcnt[0] = cc->fcnt[1] = 0;
+  cc->fcnt[0] = cc->fcnt[1] = cc->fcnt[2] = 0;
   cc->bar[0] = cc->bar[1] = cc->bar[2] = cc->bar[3] = 0;
   cc->steps_out = 0;
   cc->status = 0;
@@ -1650,8 +1652,8 @@ template <typename T>
 __global__ void __launch_bounds__(kCoopThreads, 1)
     k_sssp_nearfar(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
                    const T* __restrict__ pw, int32_t* qa, int32_t* qb, int32_t* fa, int32_t* fb,
-                   T* dist, unsigned* inq_a, unsigned* inq_b, unsigned* infar, NfCtl* cc, T delta,
-                   long long max_steps) {
+                   int32_t* fz, T* dist, unsigned* inq_a, unsigned* inq_b, unsigned* infar,
+                   NfCtl* cc, T delta, long long max_steps) {
   const int lane = threadIdx.x & 31;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nt = (int64_t)gridDim.x * blockDim.x;
@@ -1659,8 +1661,10 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
   int32_t* nxt = qb;
   unsigned* icur = inq_a;
   unsigned* inxt = inq_b;
-  int32_t* far_cur = fa;
-  int32_t* far_nxt = fb;
+  // three far lists in rotation: steps append to list fc; a band change reads list fc
+  // and writes the remainder to list fc + 1; every step zeroes the counter of list
+  // fc + 2, which nobody touches before it is next written
+  int32_t* const fl[3] = {fa, fb, fz};
   int fc = 0;
   T thr = delta;
   for (long long st = 0;; ++st) {
@@ -1675,6 +1679,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
     }
     if (nf == 0) {
       const long long nfar = (long long)*((volatile unsigned long long*)&cc->fcnt[fc]);
+      const int fn = fc == 2 ? 0 : fc + 1;
       if (nfar == 0) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
           cc->steps_out = st;
@@ -1688,14 +1693,14 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
       thr = thr > Lim<T>::max() - delta ? Lim<T>::max() : w_add(thr, delta);
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         cc->cnt[(r + 1) % 3] = 0;
-        cc->fcnt[fc ^ 1] = 0;
+        cc->fcnt[(fc + 2) % 3] = 0;
       }
       for (int64_t i0 = gt - lane; i0 < nfar; i0 += nt) {
         const int64_t i = i0 + lane;
         bool to_near = false, to_far = false;
         int32_t v = 0;
         if (i < nfar) {
-          v = far_cur[i];
+          v = fl[fc][i];
           if (ld_cg(dist + v) < thr) {
             atomicAnd(infar + (v >> 5), ~(1u << (v & 31)));
             const unsigned bit = 1u << (v & 31);
@@ -1705,7 +1710,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
           }
         }
         coop_append(to_near, v, nxt, &cc->cnt[r]);
-        coop_append(to_far, v, far_nxt, &cc->fcnt[fc ^ 1]);
+        coop_append(to_far, v, fl[fn], &cc->fcnt[fn]);
       }
       if (!coop_grid_sync(cc->bar, gridDim.x)) return;
       int32_t* t = cur;
@@ -1714,13 +1719,13 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
       unsigned* tb = icur;
       icur = inxt;
       inxt = tb;
-      t = far_cur;
-      far_cur = far_nxt;
-      far_nxt = t;
-      fc ^= 1;
+      fc = fn;
       continue;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) cc->cnt[(r + 1) % 3] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      cc->cnt[(r + 1) % 3] = 0;
+      cc->fcnt[(fc + 2) % 3] = 0;
+    }
     for (int64_t i0 = gt - lane; i0 < nf; i0 += nt) {
       const int64_t i = i0 + lane;
       int32_t k0 = 0, k1 = 0;
@@ -1754,7 +1759,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
           }
         }
         coop_append(near_add, w, nxt, &cc->cnt[r]);
-        coop_append(far_add, w, far_cur, &cc->fcnt[fc]);
+        coop_append(far_add, w, fl[fc], &cc->fcnt[fc]);
       }
     }
     if (!coop_grid_sync(cc->bar, gridDim.x)) return;
@@ -2003,7 +2008,7 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
     unsigned* ib = sc.fb[cur ^ 1];
     const T* pw = static_cast<const T*>(P.w);
     long long max_steps = 8 * (long long)n + 1024;
-    void* args[] = {&P.rowptr, &P.colval, &pw, &qa, &qb, &sc.hq, &sc.q2, &d, &ia, &ib,
+    void* args[] = {&P.rowptr, &P.colval, &pw, &qa, &qb, &sc.hq, &sc.q2, &sc.q3, &d, &ia, &ib,
                     &sc.visited, &ncc, &delta, &max_steps};
     GG_CUDA(cudaLaunchCooperativeKernel((const void*)k_sssp_nearfar<T>, dim3(ctx->num_sms),
                                         dim3(kCoopThreads), args, 0, ctx->stream));
