@@ -276,29 +276,34 @@ __global__ void __launch_bounds__(256)
       const int64_t j = jlo + jb + 4 * sub;
       if (jb + 4 * sub >= jn) continue;
       float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-      int32_t k = k0;
-      for (; k + 2 <= k1; k += 2) {
-        const int32_t c0 = ld_stream_p(colval + k, pol_s) - 1, c1 = ld_stream_p(colval + k + 1, pol_s) - 1;
-        const float a0 = ld_stream_p(nz + k, pol_s), a1 = ld_stream_p(nz + k + 1, pol_s);
-        const float4 b0 = ld_keep4(B + (int64_t)c0 * ldb + j, pol_b);
-        const float4 b1 = ld_keep4(B + (int64_t)c1 * ldb + j, pol_b);
-        acc.x = __fadd_rn(acc.x, __fmul_rn(a0, b0.x));
-        acc.y = __fadd_rn(acc.y, __fmul_rn(a0, b0.y));
-        acc.z = __fadd_rn(acc.z, __fmul_rn(a0, b0.z));
-        acc.w = __fadd_rn(acc.w, __fmul_rn(a0, b0.w));
-        acc.x = __fadd_rn(acc.x, __fmul_rn(a1, b1.x));
-        acc.y = __fadd_rn(acc.y, __fmul_rn(a1, b1.y));
-        acc.z = __fadd_rn(acc.z, __fmul_rn(a1, b1.z));
-        acc.w = __fadd_rn(acc.w, __fmul_rn(a1, b1.w));
+      // 4 entries per step in storage order, the next step's words loaded ahead
+      int32_t c[4], cn[4];
+      float a[4], an[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const bool in = k0 + u < k1;
+        c[u] = in ? ld_stream_p(colval + k0 + u, pol_s) - 1 : 0;
+        a[u] = in ? ld_stream_p(nz + k0 + u, pol_s) : 0.0f;
       }
-      if (k < k1) {
-        const int32_t c0 = ld_stream_p(colval + k, pol_s) - 1;
-        const float a0 = ld_stream_p(nz + k, pol_s);
-        const float4 b0 = ld_keep4(B + (int64_t)c0 * ldb + j, pol_b);
-        acc.x = __fadd_rn(acc.x, __fmul_rn(a0, b0.x));
-        acc.y = __fadd_rn(acc.y, __fmul_rn(a0, b0.y));
-        acc.z = __fadd_rn(acc.z, __fmul_rn(a0, b0.z));
-        acc.w = __fadd_rn(acc.w, __fmul_rn(a0, b0.w));
+      for (int32_t k = k0; k < k1; k += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const bool in = k + 4 + u < k1;
+          cn[u] = in ? ld_stream_p(colval + k + 4 + u, pol_s) - 1 : 0;
+          an[u] = in ? ld_stream_p(nz + k + 4 + u, pol_s) : 0.0f;
+        }
+        float4 b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          b[u] = k + u < k1 ? ld_keep4(B + (int64_t)c[u] * ldb + j, pol_b) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (k + u < k1) fold4(acc, a[u], b[u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          c[u] = cn[u];
+          a[u] = an[u];
+        }
       }
       if (acc.x != acc.x || acc.y != acc.y || acc.z != acc.z || acc.w != acc.w)
         acc = spmm_refold4(acc, colval, nz, B + j, ldb, k0, k1);
