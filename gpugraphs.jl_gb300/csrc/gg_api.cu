@@ -189,6 +189,7 @@ static void free_mat_storage(gg_mat* A) {
     A->colperm = nullptr;
   }
   free_win_plan(A);
+  free_spv_plan(A);
   if (A->hubplan) {
     cudaFree(A->hubplan->hubs);
     cudaFree(A->hubplan->pieces);

@@ -325,6 +325,7 @@ struct RowBlocks {
 };
 
 struct GraphAux;  // graph-algorithm analysis (gg_graph.cu)
+struct SpvPlan;   // column index and workspace of SpMSpV (gg_spmspv.cu)
 
 // Work list of a SELL matrix: slices cut into chunks of at most kSellChunk stored
 // columns.  items: (slice, first column, end column, partial index or -1 when the
@@ -511,6 +512,7 @@ struct gg_mat {
   gg::MMPlan* mmplan = nullptr;
   gg::HubPlan* hubplan = nullptr;
   gg::WinPlan* winplan = nullptr;
+  gg::SpvPlan* spv = nullptr;
   gg_mat* sell_copy = nullptr;  // CSR handles: SELL-32 copy (rows sorted by length) for plus-times
   int64_t max_row_len = -1;
   // tuned choices (gg_tune): plus-times SpMV kernel (0 = built-in rule, 1 = CSR row
@@ -543,5 +545,8 @@ int launch_pipe_f32(gg_ctx* ctx, gg_mat* A, const float* nz, const float* x, flo
 int build_win_plan(gg_ctx* ctx, gg_mat* A);  // gg_spmv_win.cu
 int launch_spmv_win(gg_ctx* ctx, gg_mat* A, const float* x, float* y);
 void free_win_plan(gg_mat* A);
+void free_spv_plan(gg_mat* A);  // gg_spmspv.cu
+// out[0..n] = base + exclusive prefix sums of cnt (gg_graph.cu; synchronises the stream)
+int scan_counts(gg_ctx* ctx, const int32_t* cnt, int64_t n, int32_t* out, int32_t base);
 int row_stats(gg_ctx* ctx, gg_mat* A);
 }  // namespace gg

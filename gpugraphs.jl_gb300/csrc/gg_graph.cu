@@ -140,7 +140,7 @@ __global__ void k_scan_add(int32_t* out, int64_t n, const int32_t* bsum, const i
 }
 
 // out[0..n] = base + exclusive prefix sums of cnt[0..n-1]; out[n] = base + total
-static int scan_counts(gg_ctx* ctx, const int32_t* cnt, int64_t n, int32_t* out, int32_t base) {
+int scan_counts(gg_ctx* ctx, const int32_t* cnt, int64_t n, int32_t* out, int32_t base) {
   const int64_t nb = (n + 1023) / 1024;
   int32_t* tmp = nullptr;
   GG_CUDA(cudaMalloc((void**)&tmp, (nb + 2) * sizeof(int32_t)));

@@ -16,14 +16,17 @@ from .algorithms import (bfs_distances, bfs_distances_, bfs_distances_batch, bfs
                          shortest_path, shortest_path_)
 from .errors import (ArgumentError, BoundsError, DimensionMismatch, GPUGraphsError,
                      SpmmAssertionError, UnsupportedError)
-from .ops import gpu_spmm_, gpu_spmv_, synchronize
+from .ewise import gpu_apply_, gpu_ewise_, gpu_reduce
+from .ops import gpu_spmm_, gpu_spmspv, gpu_spmspv_, gpu_spmv_, gpu_spmv_rows_, synchronize
 from .storage import (AbstractSparseGPUMatrix, SparseGPUMatrixCSR, SparseGPUMatrixSELL,
                       sprand_gpu)
 from .tuning import autotune, spmv_layout
+from .vectors import SparseGPUVector
 
 __all__ = [
     "AbstractSparseGPUMatrix", "SparseGPUMatrixCSR", "SparseGPUMatrixSELL", "gpu_spmv_",
-    "gpu_spmm_", "sprand_gpu", "autotune", "spmv_layout", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
+    "gpu_spmm_", "SparseGPUVector", "gpu_spmspv_", "gpu_spmspv", "gpu_spmv_rows_",
+    "gpu_ewise_", "gpu_apply_", "gpu_reduce", "sprand_gpu", "autotune", "spmv_layout", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
     "bfs_parents_", "shortest_path", "shortest_path_", "monoid_neutral", "monoid_absorb", "synchronize",
     "GPUGraphs_add", "GPUGraphs_safe_add", "GPUGraphs_mul", "GPUGraphs_second",
     "GPUGraphs_band", "GPUGraphs_bor", "GPUGraphs_any", "GPUGraphs_secondi", "GPUGraphs_max",

@@ -35,6 +35,11 @@ SIGNATURES = {
     "gg_mat_arrays": [P, PP, PP, PP, PP],
     "gg_spmv": [P, P, I, I, I, P, I, I64, P, I, I64, P, I, I64, I64, I64],
     "gg_spmm": [P, P, I, I, I, P, I, I64, I64, P, I, I64, I64, I64, I, P, I, I64, I64, I64],
+    "gg_spmspv": [P, P, I, I, I, P, I, I64, P, P, I, I64, I64, P, PI64],
+    "gg_spmv_rows": [P, P, I, I, I, P, I, I64, P, I, I64, P, I64],
+    "gg_ewise": [P, I, P, I, P, I, P, I, I64, P, I],
+    "gg_apply": [P, I, P, I, P, I, P, I, I, I64, P, I],
+    "gg_reduce": [P, I, P, I, I64, P],
     "gg_bfs_levels": [P, P, I64, P, I64, PI64],
     "gg_bfs_parents": [P, P, I64, P, I64, I, PI64],
     "gg_sssp": [P, P, P, I64, P, P, I, I64, PI64],

@@ -17,7 +17,8 @@ import torch
 from . import core
 from .algebra import GPUGraphs_add, GPUGraphs_mul, GPUGraphs_second, op_code
 from .errors import ArgumentError, DimensionMismatch, SpmmAssertionError, check
-from .storage import AbstractSparseGPUMatrix
+from .storage import AbstractSparseGPUMatrix, SparseGPUMatrixCSR
+from .vectors import SparseGPUVector
 
 
 def _range_bounds(rng):
@@ -125,6 +126,73 @@ def gpu_spmm_(C, A, B, mul=GPUGraphs_mul, add=GPUGraphs_add, accum=GPUGraphs_sec
         check(L.gg_spmm(c, A.handle, op_code(mul), op_code(add), op_code(accum), core.ptr(C),
                         core.dtype_code(C), C.shape[0], ldc, core.ptr(B), core.dtype_code(B),
                         B.shape[0], ldb, B.shape[1], lb, mp, mcode, mlen, lo, hi), L)
+    return None
+
+
+def gpu_spmspv_(C, A, B, mul=GPUGraphs_mul, add=GPUGraphs_add, accum=GPUGraphs_second):
+    """Semiring SpMV over a sparse input vector, the drop-in of gpu_spmspv!
+    (src/spmspv.jl:23-54) over A's CSR storage.  B is a SparseGPUVector; C a dense
+    device vector of length size(A, 1).  Every row i holding an entry whose column
+    carries an entry of B gets C[i] = accum(C[i], add over those entries, in storage
+    order, of mul(A[i, j], B[j], i, j, j, 1)) (absorb early exit as gpu_spmv!); other
+    rows are untouched.  Returns the 1-based rows written, ascending (Int32 device
+    tensor).  Synchronous.  DimensionMismatch as gpu_spmspv!; ArgumentError when B's
+    indices are not strictly increasing inside 1:n."""
+    if not isinstance(A, SparseGPUMatrixCSR):
+        raise ArgumentError("gpu_spmspv! takes a SparseGPUMatrixCSR")
+    if not isinstance(B, SparseGPUVector):
+        raise ArgumentError("B must be a SparseGPUVector")
+    if A.size(2) != B.n:
+        raise DimensionMismatch("Matrix dimensions must agree")
+    if not isinstance(C, torch.Tensor) or C.shape[0] != A.size(1):
+        raise DimensionMismatch("Matrix dimensions must agree")
+    core.device_vector(C, "C")
+    tv, tx, ty = A.dtype_code, core.dtype_code(B.nzval), core.dtype_code(C)
+    if core.promote_code(tv, tx) != ty:
+        raise ArgumentError("Result type must be able to hold the result of the multiplication")
+    out = torch.empty(max(A.size(1), 1), dtype=torch.int32, device=A.device)
+    cnt = ctypes.c_int64(0)
+    L = core.lib()
+    with torch.cuda.device(A.device):
+        c = core.ctx(A.device)
+        check(L.gg_spmspv(c, A.handle, op_code(mul), op_code(add), op_code(accum), core.ptr(C), ty,
+                          C.numel(), core.ptr(B.nzind), core.ptr(B.nzval), tx, B.nnz(), B.n,
+                          core.ptr(out), ctypes.byref(cnt)), L)
+    return out[:cnt.value]
+
+
+def gpu_spmspv(A, B, mul=GPUGraphs_mul, add=GPUGraphs_add):
+    """Allocating form: the SparseGPUVector of length size(A, 1) holding, for the rows
+    that have a contributing entry, add over mul(A[i, j], B[j]) (no accum)."""
+    tc = core.CODE2TORCH[core.promote_code(A.dtype_code, core.dtype_code(B.nzval))]
+    C = torch.zeros(A.size(1), dtype=tc, device=A.device)
+    rows = gpu_spmspv_(C, A, B, mul=mul, add=add, accum=GPUGraphs_second)
+    return SparseGPUVector(A.size(1), rows, C[rows.long() - 1], device=A.device)
+
+
+def gpu_spmv_rows_(C, A, B, rows, mul=GPUGraphs_mul, add=GPUGraphs_add, accum=GPUGraphs_second):
+    """SpMV of the listed rows only: sparse_masked_csr_spmv_kernel! (src/spmv/CSR.jl:90-115),
+    whose mask is a list of 1-based row ids.  C[r] = accum(C[r], add over row r of
+    mul(A[r, j], B[j], r, j, j, 1)) for r in rows; other rows untouched.  Synchronous;
+    BoundsError for a row outside 1:size(A, 1)."""
+    if not isinstance(A, SparseGPUMatrixCSR):
+        raise ArgumentError("the row-list SpMV takes a SparseGPUMatrixCSR")
+    if A.size(2) != B.numel() or C.shape[0] != A.size(1):
+        raise DimensionMismatch("Matrix dimensions must agree")
+    for t, name in ((B, "B"), (C, "C")):
+        core.device_vector(t, name)
+    tv, tx, ty = A.dtype_code, core.dtype_code(B), core.dtype_code(C)
+    if core.promote_code(tv, tx) != ty:
+        raise ArgumentError("Result type must be able to hold the result of the multiplication")
+    if not isinstance(rows, torch.Tensor):
+        rows = torch.as_tensor(rows, dtype=torch.int32)
+    rows = rows.to(device=A.device, dtype=torch.int32).contiguous()
+    L = core.lib()
+    with torch.cuda.device(A.device):
+        c = core.ctx(A.device)
+        check(L.gg_spmv_rows(c, A.handle, op_code(mul), op_code(add), op_code(accum), core.ptr(C),
+                             ty, C.numel(), core.ptr(B), tx, B.numel(), core.ptr(rows),
+                             rows.numel()), L)
     return None
 
 

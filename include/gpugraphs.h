@@ -199,6 +199,66 @@ int gg_spmm(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* C, 
             int64_t ldb, int64_t k, int layout, const void* mask, int mask_dtype,
             int64_t mask_len, int64_t range_lo, int64_t range_hi);
 
+/*
+ * Semiring SpMV over a sparse input vector: replaces gpu_spmspv!(C, A, B, mul, add,
+ * accum) (src/spmspv.jl:23-54, written for CSC and never finished there), over the CSR
+ * storage of A (A_T of the graph) like every other entry point.  x is the sparse vector
+ * (x_len, x_ind[0..x_nnz), x_val) with 1-based, strictly increasing device indices
+ * (SparseGPUVector's nzind / nzval, src/GPUGraphsVector.jl:12-24).  For every row i
+ * with at least one entry whose column carries an entry of x,
+ *     y[i] = accum(y[i], add over those entries k, in storage order, of
+ *                        mul(A[k], x[col], i, col, col, 1))
+ * with the absorb early exit of src/spmv/CSR.jl:31-54; other rows of the dense y are
+ * not written.  y_ind (device, capacity m, may be NULL) receives the 1-based rows
+ * written, ascending; *y_nnz (may be NULL) their count.  The first call builds a column
+ * index of A (kept on the handle).  Errors: GG_ERR_DIMENSION as gpu_spmspv! (n != x_len,
+ * m != y_len), GG_ERR_TYPE / GG_ERR_UNSUPPORTED as gg_spmv, GG_ERR_ARGUMENT for indices
+ * that are not increasing or outside 1:n (nothing written), GG_ERR_UNSUPPORTED for a
+ * SELL handle.  Synchronous.
+ */
+int gg_spmspv(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* y, int y_dtype,
+              int64_t y_len, const int32_t* x_ind, const void* x_val, int x_dtype,
+              int64_t x_nnz, int64_t x_len, int32_t* y_ind, int64_t* y_nnz);
+
+/*
+ * SpMV of the listed rows only: replaces sparse_masked_csr_spmv_kernel!
+ * (src/spmv/CSR.jl:90-115), whose mask is a list of row ids.  For every 1-based row r of
+ * rows[0..nrows) (device), y[r] = accum(y[r], add over row r in storage order of
+ * mul(A[k], x[col], r, col, col, 1)) with the absorb early exit; other rows are not
+ * written.  Rows should be distinct (a repeated row applies accum once per listing).
+ * GG_ERR_BOUNDS when a listed row is outside 1:m (the other rows are written);
+ * GG_ERR_UNSUPPORTED for a SELL handle.  Synchronous.
+ */
+int gg_spmv_rows(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* y,
+                 int y_dtype, int64_t y_len, const void* x, int x_dtype, int64_t x_len,
+                 const int32_t* rows, int64_t nrows);
+
+/* ---- element-wise, apply, reduce ---------------------------------------------- */
+/*
+ * The reference's src/e_wise_ops.jl and src/map_and_reduce.jl are empty; its
+ * algorithms use Julia broadcasts for these steps (bfs.jl:60-70, shortest_path.jl:72-79).
+ * Operators and element types are those of the semiring calls, with Julia's scalar
+ * semantics; the computation type is promote_type of the two operands (Int32 / Int64
+ * at least for the index operators, as in gg_spmv), and the result type must hold it
+ * (GG_ERR_TYPE otherwise); an operator without a method for that type returns
+ * GG_ERR_UNSUPPORTED.  Index operators see vector entry i as (row i, column 1).
+ * Entries where mask (optional, any element type) is zero are not written.
+ */
+/* z[i] = op(x[i], y[i]) for i in 0..n-1.  Asynchronous on the context's stream. */
+int gg_ewise(gg_ctx* ctx, int op, void* z, int z_dtype, const void* x, int x_dtype,
+             const void* y, int y_dtype, int64_t n, const void* mask, int mask_dtype);
+/* z[i] = op(x[i], s), or op(s, x[i]) when s_first != 0; s points to one host value of
+   s_dtype.  Asynchronous on the context's stream. */
+int gg_apply(gg_ctx* ctx, int op, void* z, int z_dtype, const void* x, int x_dtype,
+             const void* s, int s_dtype, int s_first, int64_t n, const void* mask,
+             int mask_dtype);
+/* *out (host, x_dtype) = add over x[0..n) starting from add's neutral element
+   (GG_ERR_UNSUPPORTED when add is not a monoid of x_dtype).  Order: chunks of 8192
+   values, one 256-thread block each (thread t folds t, t+256, ... left to right, then
+   xor butterflies over the lanes and over the 8 warp totals), chunk totals reduced
+   again the same way; exact monoids give the same value in any order.  Synchronous. */
+int gg_reduce(gg_ctx* ctx, int add, const void* x, int x_dtype, int64_t n, void* out);
+
 /* ---- graph algorithms ------------------------------------------------------- */
 
 /*

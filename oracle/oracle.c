@@ -747,6 +747,206 @@ void orc_csr_spmv_plus_times_f32_rows(int64_t r0, int64_t r1, const int32_t* row
   }
 }
 
+/* ------------------------------------------------------------------------------ */
+/* SpMSpV: the operation of csc_spmspv_kernel! / gpu_spmspv! (src/spmspv.jl:1-54,   */
+/* unfinished there) over the CSR storage of A, with the per-row loop of              */
+/* src/spmv/CSR.jl:31-54 restricted to the columns that carry an entry of x.          */
+/* x: 1-based strictly increasing x_ind[0..x_nnz), values x_val of type tx.           */
+/* Rows with at least one such entry are written and listed in out_ind (1-based,      */
+/* ascending); returns ORC_ARG for bad indices (nothing written).                     */
+/* ------------------------------------------------------------------------------ */
+int orc_csr_spmspv(int64_t m, int64_t n, const int32_t* rowptr, const int32_t* colval,
+                   const void* nzval, int tv, void* y, int ty, const int32_t* x_ind,
+                   const void* x_val, int tx, int64_t x_nnz, int mul, int add, int accum,
+                   int32_t* out_ind, int64_t* out_nnz) {
+  int tc;
+  int rc = check_semiring(tv, tx, ty, mul, add, accum, &tc);
+  if (rc) return rc;
+  for (int64_t t = 0; t < x_nnz; ++t)
+    if (x_ind[t] < 1 || x_ind[t] > n || (t > 0 && x_ind[t - 1] >= x_ind[t])) return ORC_ARG;
+  int64_t* pos = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+  for (int64_t j = 0; j < n; ++j) pos[j] = -1;
+  for (int64_t t = 0; t < x_nnz; ++t) pos[x_ind[t] - 1] = t;
+  val neutral, absorb;
+  neutral_of(add, tc, &neutral);
+  int has_absorb = absorb_of(add, tc, &absorb);
+  int64_t cnt = 0;
+  for (int64_t r = 1; r <= m; ++r) {
+    val acc = neutral;
+    int hit = 0;
+    for (int64_t i = rowptr[r - 1]; i <= rowptr[r] - 1; ++i) {
+      int64_t col = colval[i - 1];
+      int64_t t = pos[col - 1];
+      if (t < 0) continue;
+      hit = 1;
+      val b = load(x_val, tx, t);
+      val a = cvt(load(nzval, tv, i - 1), tc);
+      val mres = apply(mul, tc, a, cvt(b, tc), b, r, col, col, 1);
+      acc = apply(add, tc, acc, mres, mres, r, col, col, 1);
+      if (has_absorb && veq(acc, absorb)) break;
+    }
+    if (!hit) continue;
+    val yo = load(y, ty, r - 1);
+    val a2 = cvt(acc, ty);
+    store(y, ty, r - 1, apply(accum, ty, yo, a2, a2, r, 1, r, 1));
+    if (out_ind) out_ind[cnt] = (int32_t)r;
+    ++cnt;
+  }
+  free(pos);
+  if (out_nnz) *out_nnz = cnt;
+  return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------------ */
+/* SpMV of listed rows: sparse_masked_csr_spmv_kernel! (src/spmv/CSR.jl:90-115),    */
+/* whose mask holds 1-based row ids.  ORC_ARG for a row outside 1:m (other rows are  */
+/* still written, in list order).                                                    */
+/* ------------------------------------------------------------------------------ */
+int orc_csr_spmv_rows(int64_t m, const int32_t* rowptr, const int32_t* colval,
+                      const void* nzval, int tv, void* y, int ty, const void* x, int tx,
+                      const int32_t* rows, int64_t nrows, int mul, int add, int accum) {
+  int tc;
+  int rc = check_semiring(tv, tx, ty, mul, add, accum, &tc);
+  if (rc) return rc;
+  val neutral, absorb;
+  neutral_of(add, tc, &neutral);
+  int has_absorb = absorb_of(add, tc, &absorb);
+  int bad = 0;
+  for (int64_t e = 0; e < nrows; ++e) {
+    int64_t r = rows[e];
+    if (r < 1 || r > m) {
+      bad = 1;
+      continue;
+    }
+    val acc = neutral;
+    for (int64_t i = rowptr[r - 1]; i <= rowptr[r] - 1; ++i) {
+      int64_t col = colval[i - 1];
+      val b = load(x, tx, col - 1);
+      val a = cvt(load(nzval, tv, i - 1), tc);
+      val mres = apply(mul, tc, a, cvt(b, tc), b, r, col, col, 1);
+      acc = apply(add, tc, acc, mres, mres, r, col, col, 1);
+      if (has_absorb && veq(acc, absorb)) break;
+    }
+    val yo = load(y, ty, r - 1);
+    val a2 = cvt(acc, ty);
+    store(y, ty, r - 1, apply(accum, ty, yo, a2, a2, r, 1, r, 1));
+  }
+  return bad ? ORC_ARG : ORC_OK;
+}
+
+/* ------------------------------------------------------------------------------ */
+/* Element-wise / apply / reduce with the operators of src/algebra.jl (the          */
+/* reference's e_wise_ops.jl and map_and_reduce.jl are empty; its algorithms use    */
+/* broadcasts, bfs.jl:60-70, shortest_path.jl:72-79).                               */
+/* ------------------------------------------------------------------------------ */
+static int ewise_type(int op, int ta, int tb, int tz, int* tc_out) {
+  int tc = compute_type(ta, tb, op);
+  int tp = ta > tb ? ta : tb;
+  if (tz < tc || tz < tp) return ORC_TYPE;
+  if (!is_index_op(op) && !op_defined(op, tc)) return ORC_UNSUPPORTED;
+  *tc_out = tc;
+  return ORC_OK;
+}
+
+/* z[i] = op(x[i], y[i], i, 1, i, 1) where mask[i] != 0 (or everywhere) */
+int orc_ewise(int op, void* z, int tz, const void* x, int tx, const void* y, int ty, int64_t n,
+              const void* mask, int tmask) {
+  int tc;
+  int rc = ewise_type(op, tx, ty, tz, &tc);
+  if (rc) return rc;
+  for (int64_t i = 0; i < n; ++i) {
+    if (mask && is_zero(load(mask, tmask, i))) continue;
+    val a = load(x, tx, i), b = load(y, ty, i);
+    val v = apply(op, tc, cvt(a, tc), cvt(b, tc), b, i + 1, 1, i + 1, 1);
+    store(z, tz, i, cvt(v, tz));
+  }
+  return ORC_OK;
+}
+
+/* z[i] = op(x[i], s) or op(s, x[i]); s is one value of type ts */
+int orc_apply(int op, void* z, int tz, const void* x, int tx, const void* s, int ts,
+              int s_first, int64_t n, const void* mask, int tmask) {
+  int tc;
+  int rc = s_first ? ewise_type(op, ts, tx, tz, &tc) : ewise_type(op, tx, ts, tz, &tc);
+  if (rc) return rc;
+  val sv = load(s, ts, 0);
+  for (int64_t i = 0; i < n; ++i) {
+    if (mask && is_zero(load(mask, tmask, i))) continue;
+    val a = load(x, tx, i);
+    val v = s_first ? apply(op, tc, cvt(sv, tc), cvt(a, tc), a, i + 1, 1, i + 1, 1)
+                    : apply(op, tc, cvt(a, tc), cvt(sv, tc), sv, i + 1, 1, i + 1, 1);
+    store(z, tz, i, cvt(v, tz));
+  }
+  return ORC_OK;
+}
+
+/* One chunk of up to 8192 values in the library's order: 256 threads fold values t,
+   t + 256, ... left to right; each warp's 32 lanes combine by xor butterfly (lane l
+   takes add(v[l], v[l ^ o]), o = 16, 8, 4, 2, 1); lane 0 of warp 0 then combines the 8
+   warp totals (lanes 8..31 neutral) the same way. */
+static val reduce_chunk(int add, int t, const void* x, int tx, int64_t c0, int64_t n, val neutral) {
+  val th[256], w[32], tot[8];
+  for (int k = 0; k < 256; ++k) {
+    val acc = neutral;
+    for (int u = 0; u < 32; ++u) {
+      int64_t i = c0 + k + (int64_t)u * 256;
+      if (i < n) {
+        val v = cvt(load(x, tx, i), t);
+        acc = apply(add, t, acc, v, v, 0, 0, 0, 0);
+      }
+    }
+    th[k] = acc;
+  }
+  for (int wid = 0; wid < 8; ++wid) {
+    for (int l = 0; l < 32; ++l) w[l] = th[wid * 32 + l];
+    for (int o = 16; o > 0; o >>= 1) {
+      val nw[32];
+      for (int l = 0; l < 32; ++l) nw[l] = apply(add, t, w[l], w[l ^ o], w[l ^ o], 0, 0, 0, 0);
+      memcpy(w, nw, sizeof(w));
+    }
+    tot[wid] = w[0];
+  }
+  for (int l = 0; l < 32; ++l) w[l] = l < 8 ? tot[l] : neutral;
+  for (int o = 16; o > 0; o >>= 1) {
+    val nw[32];
+    for (int l = 0; l < 32; ++l) nw[l] = apply(add, t, w[l], w[l ^ o], w[l ^ o], 0, 0, 0, 0);
+    memcpy(w, nw, sizeof(w));
+  }
+  return w[0];
+}
+
+/* *out = add over x[0..n) from the neutral element, in the library's fixed order:
+   chunks of 8192, chunk totals reduced again until one value is left. */
+int orc_reduce(int add, const void* x, int tx, int64_t n, void* out) {
+  int tc;
+  int rc = check_semiring(tx, tx, tx, OP_FIRST, add, OP_SECOND, &tc);
+  if (rc) return rc;
+  val neutral;
+  neutral_of(add, tx, &neutral);
+  if (n == 0) {
+    store(out, tx, 0, neutral);
+    return ORC_OK;
+  }
+  size_t esz = (tx == T_BOOL) ? 1 : (tx == T_I32 || tx == T_F32) ? 4 : 8;
+  int64_t cnt = n;
+  const void* in = x;
+  void* buf = NULL;
+  for (;;) {
+    int64_t chunks = (cnt + 8191) / 8192;
+    void* nb = malloc((size_t)chunks * esz);
+    for (int64_t c = 0; c < chunks; ++c)
+      store(nb, tx, c, reduce_chunk(add, tx, in, tx, c * 8192, cnt, neutral));
+    free(buf);
+    buf = nb;
+    in = buf;
+    cnt = chunks;
+    if (cnt == 1) break;
+  }
+  store(out, tx, 0, load(buf, tx, 0));
+  free(buf);
+  return ORC_OK;
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -54,6 +54,12 @@ def lib():
             "orc_gen_grid": [I64, I64, U64, I32, P, P, P],
             "orc_gen_uniform_f32": [I64, U64, P],
             "orc_coo_to_csr": [I64, I64, P, P, P, I32, I32, I32, P, P, P, P],
+            "orc_csr_spmspv": [I64, I64, P, P, P, I32, P, I32, P, P, I32, I64, I32, I32, I32, P,
+                               P],
+            "orc_csr_spmv_rows": [I64, P, P, P, I32, P, I32, P, I32, P, I64, I32, I32, I32],
+            "orc_ewise": [I32, P, I32, P, I32, P, I32, I64, P, I32],
+            "orc_apply": [I32, P, I32, P, I32, P, I32, I32, I64, P, I32],
+            "orc_reduce": [I32, P, I32, I64, P],
             "orc_num_threads": [],
             "orc_set_num_threads": [I32],
         }
@@ -206,6 +212,56 @@ def sssp(n, rowptr, colval, nzval, sources, max_rounds=0):
     rounds = lib().orc_sssp(n, _p(rowptr), _p(colval), _p(nzval), tcode(nzval), _p(src), len(src),
                             _p(dist), td, max_rounds)
     return dist, rounds
+
+
+def csr_spmspv(m, n, rowptr, colval, nzval, y, x_ind, x_val, mul=MUL, add=ADD, accum=SECOND):
+    """SpMSpV (src/spmspv.jl:1-54 over CSR): y updated in place on the rows reached;
+    returns (status, 1-based rows written ascending)."""
+    rowptr, colval, nzval = _c(rowptr, np.int32), _c(colval, np.int32), _c(nzval)
+    x_ind, x_val = _c(x_ind, np.int32), _c(x_val)
+    assert y.flags.c_contiguous
+    out = np.zeros(max(m, 1), dtype=np.int32)
+    cnt = ctypes.c_int64(0)
+    rc = lib().orc_csr_spmspv(m, n, _p(rowptr), _p(colval), _p(nzval), tcode(nzval), _p(y),
+                              tcode(y), _p(x_ind), _p(x_val), tcode(x_val), len(x_ind), mul,
+                              add, accum, _p(out), ctypes.byref(cnt))
+    return rc, out[:cnt.value].copy()
+
+
+def csr_spmv_rows(m, rowptr, colval, nzval, y, x, rows, mul=MUL, add=ADD, accum=SECOND):
+    """sparse_masked_csr_spmv_kernel! (src/spmv/CSR.jl:90-115): the listed 1-based rows."""
+    rowptr, colval, nzval, x = _c(rowptr, np.int32), _c(colval, np.int32), _c(nzval), _c(x)
+    rows = _c(rows, np.int32)
+    assert y.flags.c_contiguous
+    return lib().orc_csr_spmv_rows(m, _p(rowptr), _p(colval), _p(nzval), tcode(nzval), _p(y),
+                                   tcode(y), _p(x), tcode(x), _p(rows), len(rows), mul, add,
+                                   accum)
+
+
+def ewise(op, z, x, y, mask=None):
+    """z[i] = op(x[i], y[i]) where mask[i] != 0; z updated in place; returns the status."""
+    x, y = _c(x), _c(y)
+    mask = None if mask is None else _c(mask)
+    assert z.flags.c_contiguous
+    return lib().orc_ewise(op, _p(z), tcode(z), _p(x), tcode(x), _p(y), tcode(y), len(x), _p(mask),
+                           0 if mask is None else tcode(mask))
+
+
+def apply_scalar(op, z, x, s, s_first=False, mask=None):
+    """z[i] = op(x[i], s) or op(s, x[i]); s a numpy scalar; returns the status."""
+    x = _c(x)
+    sv = np.array([s], dtype=np.asarray(s).dtype)
+    mask = None if mask is None else _c(mask)
+    return lib().orc_apply(op, _p(z), tcode(z), _p(x), tcode(x), _p(sv), tcode(sv),
+                           1 if s_first else 0, len(x), _p(mask), 0 if mask is None else tcode(mask))
+
+
+def reduce(add, x):
+    """(status, add over x in the library's fixed chunk / butterfly order)."""
+    x = _c(x)
+    out = np.zeros(1, dtype=x.dtype)
+    rc = lib().orc_reduce(add, _p(x), tcode(x), len(x), _p(out))
+    return rc, out[0]
 
 
 def spmv_plus_times_f32(rowptr, colval, nzval, x, y, rows=None):
