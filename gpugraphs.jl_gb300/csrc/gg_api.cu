@@ -157,13 +157,8 @@ __global__ void k_invert_perm(int64_t m, const int32_t* perm, int32_t* iperm) {
 }
 
 static void free_mat_storage(gg_mat* A);
-static void free_mat_storage(gg_mat* A) {
-  cudaFree(A->rowptr);
-  cudaFree(A->colval);
-  cudaFree(A->nzval);
-  cudaFree(A->slice_ptr);
-  cudaFree(A->perm);
-  cudaFree(A->iperm);
+// everything built from the handle's arrays on first use (plans, copies, analyses)
+static void free_derived(gg_mat* A) {
   if (A->blocks) {
     RowBlocks* rb = A->blocks;
     cudaFree(rb->blocks);
@@ -180,6 +175,11 @@ static void free_mat_storage(gg_mat* A) {
     free_mat_storage(A->sell_copy);
     delete A->sell_copy;
     A->sell_copy = nullptr;
+  }
+  if (A->tr_copy) {
+    free_mat_storage(A->tr_copy);
+    delete A->tr_copy;
+    A->tr_copy = nullptr;
   }
   if (A->colperm) {
     cudaFree(A->colperm->colval_r);
@@ -216,6 +216,16 @@ static void free_mat_storage(gg_mat* A) {
     delete A->sellplan;
     A->sellplan = nullptr;
   }
+}
+
+static void free_mat_storage(gg_mat* A) {
+  cudaFree(A->rowptr);
+  cudaFree(A->colval);
+  cudaFree(A->nzval);
+  cudaFree(A->slice_ptr);
+  cudaFree(A->perm);
+  cudaFree(A->iperm);
+  free_derived(A);
 }
 
 static int blocks_for(gg_ctx* ctx, int64_t work) {
@@ -478,6 +488,14 @@ int gg_mat_destroy(gg_mat* A) {
   cudaSetDevice(A->device);
   free_mat_storage(A);
   delete A;
+  return GG_OK;
+}
+
+int gg_mat_values_changed(gg_ctx* ctx, gg_mat* A) {
+  if (!ctx || !A) return set_error(GG_ERR_ARGUMENT, "ctx / A is NULL");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  free_derived(A);
   return GG_OK;
 }
 

@@ -514,6 +514,7 @@ struct gg_mat {
   gg::WinPlan* winplan = nullptr;
   gg::SpvPlan* spv = nullptr;
   gg_mat* sell_copy = nullptr;  // CSR handles: SELL-32 copy (rows sorted by length) for plus-times
+  gg_mat* tr_copy = nullptr;    // CSR handles: CSR storage of the transpose (gg_spmv_t)
   int64_t max_row_len = -1;
   // tuned choices (gg_tune): plus-times SpMV kernel (0 = built-in rule, 1 = CSR row
   // blocks, 2 = the SELL copy, 3 = column-window tiles), rows per row block, SpMM

@@ -18,14 +18,14 @@ from .errors import (ArgumentError, BoundsError, DimensionMismatch, GPUGraphsErr
                      SpmmAssertionError, UnsupportedError)
 from .ewise import gpu_apply_, gpu_ewise_, gpu_reduce
 from .ops import gpu_spmm_, gpu_spmspv, gpu_spmspv_, gpu_spmv_, gpu_spmv_rows_, synchronize
-from .storage import (AbstractSparseGPUMatrix, SparseGPUMatrixCSR, SparseGPUMatrixSELL,
-                      sprand_gpu)
+from .storage import (AbstractSparseGPUMatrix, SparseGPUMatrixCSC, SparseGPUMatrixCSR,
+                      SparseGPUMatrixSELL, sprand_gpu)
 from .tuning import autotune, spmv_layout
 from .vectors import SparseGPUVector
 
 __all__ = [
     "AbstractSparseGPUMatrix", "SparseGPUMatrixCSR", "SparseGPUMatrixSELL", "gpu_spmv_",
-    "gpu_spmm_", "SparseGPUVector", "gpu_spmspv_", "gpu_spmspv", "gpu_spmv_rows_",
+    "gpu_spmm_", "SparseGPUMatrixCSC", "SparseGPUVector", "gpu_spmspv_", "gpu_spmspv", "gpu_spmv_rows_",
     "gpu_ewise_", "gpu_apply_", "gpu_reduce", "sprand_gpu", "autotune", "spmv_layout", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
     "bfs_parents_", "shortest_path", "shortest_path_", "monoid_neutral", "monoid_absorb", "synchronize",
     "GPUGraphs_add", "GPUGraphs_safe_add", "GPUGraphs_mul", "GPUGraphs_second",

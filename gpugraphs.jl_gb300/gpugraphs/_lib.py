@@ -35,6 +35,8 @@ SIGNATURES = {
     "gg_mat_arrays": [P, PP, PP, PP, PP],
     "gg_spmv": [P, P, I, I, I, P, I, I64, P, I, I64, P, I, I64, I64, I64],
     "gg_spmm": [P, P, I, I, I, P, I, I64, I64, P, I, I64, I64, I64, I, P, I, I64, I64, I64],
+    "gg_mat_values_changed": [P, P],
+    "gg_spmv_t": [P, P, I, I, I, P, I, I64, P, I, I64, P, I, I64, I64, I64],
     "gg_spmspv": [P, P, I, I, I, P, I, I64, P, P, I, I64, I64, P, PI64],
     "gg_spmv_rows": [P, P, I, I, I, P, I, I64, P, I, I64, P, I64],
     "gg_ewise": [P, I, P, I, P, I, P, I, I64, P, I],

@@ -17,7 +17,7 @@ import torch
 from . import core
 from .algebra import GPUGraphs_add, GPUGraphs_mul, GPUGraphs_second, op_code
 from .errors import ArgumentError, DimensionMismatch, SpmmAssertionError, check
-from .storage import AbstractSparseGPUMatrix, SparseGPUMatrixCSR
+from .storage import AbstractSparseGPUMatrix, SparseGPUMatrixCSC, SparseGPUMatrixCSR
 from .vectors import SparseGPUVector
 
 
@@ -39,7 +39,7 @@ def gpu_spmv_(C, A, B, mul=GPUGraphs_mul, add=GPUGraphs_add, accum=GPUGraphs_sec
               range=None, mask=None):
     """In-place semiring SpMV, the drop-in of gpu_spmv! (src/spmv/CSR.jl:2-29)."""
     if not isinstance(A, AbstractSparseGPUMatrix):
-        raise ArgumentError("A must be a SparseGPUMatrixCSR or SparseGPUMatrixSELL")
+        raise ArgumentError("A must be a SparseGPUMatrixCSR, SparseGPUMatrixCSC or SparseGPUMatrixSELL")
     if not isinstance(B, torch.Tensor) or not isinstance(C, torch.Tensor):
         raise ArgumentError("All inputs must be on the same backend")
     if A.size(2) != B.numel():
@@ -65,10 +65,12 @@ def gpu_spmv_(C, A, B, mul=GPUGraphs_mul, add=GPUGraphs_add, accum=GPUGraphs_sec
         mcode, mlen, mp = core.dtype_code(mask), mask.numel(), core.ptr(mask)
     lo, hi = _range_bounds(range)
     L = core.lib()
+    # a CSC matrix is the CSR storage of its transpose: its product is the transposed SpMV
+    fn = L.gg_spmv_t if isinstance(A, SparseGPUMatrixCSC) else L.gg_spmv
     with torch.cuda.device(A.device):
         c = core.ctx(A.device)
-        check(L.gg_spmv(c, A.handle, op_code(mul), op_code(add), op_code(accum), core.ptr(C), ty,
-                        C.numel(), core.ptr(B), tx, B.numel(), mp, mcode, mlen, lo, hi), L)
+        check(fn(c, A.handle, op_code(mul), op_code(add), op_code(accum), core.ptr(C), ty,
+                 C.numel(), core.ptr(B), tx, B.numel(), mp, mcode, mlen, lo, hi), L)
     return None
 
 
@@ -93,7 +95,7 @@ def gpu_spmm_(C, A, B, mul=GPUGraphs_mul, add=GPUGraphs_add, accum=GPUGraphs_sec
     B and C may be column-major (Julia's layout, e.g. ``t.T.contiguous().T``) or
     row-major; both must use the same layout.  Shape violations raise
     SpmmAssertionError like the reference's @assert."""
-    if not isinstance(A, AbstractSparseGPUMatrix):
+    if not isinstance(A, AbstractSparseGPUMatrix) or isinstance(A, SparseGPUMatrixCSC):
         raise ArgumentError("A must be a SparseGPUMatrixCSR or SparseGPUMatrixSELL")
     if B.dim() != 2 or C.dim() != 2:
         raise SpmmAssertionError("B and C must be matrices")

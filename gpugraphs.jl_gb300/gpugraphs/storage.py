@@ -186,9 +186,65 @@ class SparseGPUMatrixCSR(AbstractSparseGPUMatrix):
         if len(hit) == 0:
             raise ArgumentError("Index (%d, %d) is not in the matrix. Adding new values is not supported yet." % (i, j))
         self.nzval[lo - 1 + int(hit[0])] = v
+        self.values_changed()
+
+    def values_changed(self):
+        """Drop the copies and analyses the library derived from the old values (call
+        after writing to ``nzval`` directly)."""
+        L = core.lib()
+        with torch.cuda.device(self.device):
+            check(L.gg_mat_values_changed(core.ctx(self.device), self._h), L)
 
     def __repr__(self):
         return "SparseGPUMatrixCSR{%s}(%d, %d) - %d explicit elements" % (
+            core.CODE2NP[self.dtype_code], self.m, self.n, self._nnz)
+
+
+class SparseGPUMatrixCSC(AbstractSparseGPUMatrix):
+    """Compressed Sparse Column matrix on the device (src/storage/CSC.jl, marked "not
+    properly supported yet" in the reference).  ``SparseGPUMatrixCSC(m, n, colptr,
+    rowval, nzval)`` follows Julia's SparseMatrixCSC convention (colptr of length
+    n + 1, 1-based rows in 1:m; the reference's constructor compares colptr with m + 1,
+    the same thing for square matrices).  The arrays are held as the CSR storage of the
+    transpose (same colptr / rowval / nzval), and gpu_spmv_ on this type runs the
+    transposed SpMV of that handle, so ``C = A * B`` in the semiring."""
+
+    def __init__(self, m, n, colptr, rowval, nzval, device=None):
+        super().__init__()
+        if len(colptr) != n + 1:
+            raise ArgumentError("length(colptr) must be equal to n + 1")
+        if len(rowval) != len(nzval):
+            raise ArgumentError("length(rowval) must be equal to length(nzval)")
+        try:
+            self._t = SparseGPUMatrixCSR(n, m, colptr, rowval, nzval, device=device)
+        except ArgumentError as e:
+            msg = str(e).replace("rowptr", "colptr").replace("colval", "rowval")
+            raise ArgumentError(msg.replace("m + 1", "n + 1")) from None
+        self.m, self.n, self._nnz = int(m), int(n), self._t.nnz()
+        self.dtype_code = self._t.dtype_code
+        self.device = self._t.device
+        self.colptr, self.rowval, self.nzval = self._t.rowptr, self._t.colval, self._t.nzval
+
+    @property
+    def handle(self):
+        """The CSR handle of the transpose (the library's view of this matrix)."""
+        return self._t.handle
+
+    @classmethod
+    def from_scipy(cls, A, dtype=None, device=None):
+        """SparseGPUMatrixCSC(A::SparseMatrixCSC, backend): the CSC of A, rows sorted."""
+        import scipy.sparse as sp
+
+        A = sp.csc_matrix(A)
+        A.sort_indices()
+        data = A.data if dtype is None else A.data.astype(dtype)
+        return cls(A.shape[0], A.shape[1], A.indptr + 1, A.indices + 1, data, device=device)
+
+    def values_changed(self):
+        self._t.values_changed()
+
+    def __repr__(self):
+        return "SparseGPUMatrixCSC{%s}(%d, %d) - %d explicit elements" % (
             core.CODE2NP[self.dtype_code], self.m, self.n, self._nnz)
 
 

@@ -168,6 +168,14 @@ int gg_mat_info(const gg_mat* A, int* format, int64_t* m, int64_t* n, int64_t* n
  */
 int gg_mat_arrays(const gg_mat* A, void** ptr, void** colval, void** nzval, void** perm);
 
+/*
+ * Drops everything the library derived from the handle's values on first use (the
+ * SELL-32 and transposed copies, graph analyses, plans); call it after writing to the
+ * arrays gg_mat_arrays returns (setindex!, src/storage/CSR.jl:166-180).  Waits for the
+ * context's stream first.
+ */
+int gg_mat_values_changed(gg_ctx* ctx, gg_mat* A);
+
 /* ---- semiring kernels -------------------------------------------------------- */
 
 /*
@@ -219,6 +227,23 @@ int gg_spmm(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* C, 
 int gg_spmspv(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* y, int y_dtype,
               int64_t y_len, const int32_t* x_ind, const void* x_val, int x_dtype,
               int64_t x_nnz, int64_t x_len, int32_t* y_ind, int64_t* y_nnz);
+
+/*
+ * Semiring SpMV with the transpose of a CSR handle: y = A' x.  Replaces the CSC method of
+ * gpu_spmv! (src/spmv/CSC.jl:2-61, which adds with an atomic += whatever the semiring):
+ * a CSC matrix B is the CSR storage of B' (same colptr / rowval / nzval), so B x is this
+ * call on the handle made from B's arrays.  For every row j of A' selected by mask
+ * (length n) and range (1-based rows of A'),
+ *     y[j] = accum(y[j], add over the rows i of A holding column j, ascending, of
+ *                        mul(A[i, j], x[i], j, i, i, 1))
+ * with the absorb early exit, i.e. gg_spmv over the CSR storage of A', which the first
+ * call builds on the handle (stable radix sort of the column ids).  x_len must be m,
+ * y_len n; errors as gg_spmv; GG_ERR_UNSUPPORTED for a SELL handle.  Asynchronous
+ * after the first call.
+ */
+int gg_spmv_t(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* y, int y_dtype,
+              int64_t y_len, const void* x, int x_dtype, int64_t x_len, const void* mask,
+              int mask_dtype, int64_t mask_len, int64_t range_lo, int64_t range_hi);
 
 /*
  * SpMV of the listed rows only: replaces sparse_masked_csr_spmv_kernel!
