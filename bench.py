@@ -216,6 +216,7 @@ def secondary_rmat22(device, A, x):
     out["spmm_rmat22_k32"] = {"gbs_algorithmic": round(b / ms / 1e6, 1), "ms": round(ms, 3),
                               "layout": "row-major"}
     del X, Y
+    out.update(secondary_sparse_vector(device, A))
     P = rmat(22, gen.W_PATTERN, device)
     src = sources_for(P, 256, 7)
     d = G.bfs_distances(P, int(src[0]))
@@ -243,6 +244,43 @@ def secondary_rmat22(device, A, x):
     res["tune_s"] = round(time.time() - t0, 1)
     res["spmv_gbs"] = round(spmv_bytes(n, nnz) / res["spmv_ms"] / 1e6, 1)
     out["autotune_rmat22"] = res
+    return out
+
+
+def secondary_sparse_vector(device, A):
+    """SpMSpV over 1% of the vertices of R-MAT s22 (plus-times Float32; the matrix is
+    symmetric, so the column lists pushed have the row lengths), and the element-wise /
+    reduce entry points over 2^28 Float32 values (HBM-bound)."""
+    import numpy as np
+    import torch
+    import gpugraphs as G
+    out = {}
+    n = A.n
+    deg = np.diff(A.rowptr.cpu().numpy().astype(np.int64))
+    rng = np.random.default_rng(5)
+    ind = np.sort(rng.choice(n, n // 100, replace=False)).astype(np.int32) + 1
+    xv = G.SparseGPUVector(n, ind, rng.random(len(ind)).astype(np.float32))
+    y = torch.zeros(n, dtype=torch.float32, device=device)
+    rows = G.gpu_spmspv_(y, A, xv)
+    reached = rows.long().cpu().numpy() - 1
+    pushed, pulled = int(deg[ind - 1].sum()), int(deg[reached].sum())
+    ts = time_host(lambda i: G.gpu_spmspv_(y, A, xv), 10)
+    t = statistics.median(ts)
+    b = 4 * pushed + 8 * pulled + 8 * len(reached) + 8 * len(ind)
+    out["spmspv_rmat22_1pct"] = {"ms": round(t * 1e3, 3), "x_nnz": len(ind), "rows_reached": len(reached),
+                                 "entries_pushed": pushed, "entries_pulled": pulled,
+                                 "gbs_algorithmic": round(b / t / 1e9, 1),
+                                 "note": "synchronous call incl. validation sync and result count"}
+    N = 1 << 28
+    a = torch.rand(N, device=device)
+    b2 = torch.rand(N, device=device)
+    z = torch.empty(N, device=device)
+    ms = time_steps(lambda: G.gpu_ewise_(z, a, b2, G.GPUGraphs_min), 10)
+    out["ewise_min_f32_2p28"] = {"ms": round(ms, 3), "gbs": round(12 * N / ms / 1e6, 1)}
+    ts = time_host(lambda i: G.gpu_reduce(a, G.GPUGraphs_add), 10)
+    t = statistics.median(ts)
+    out["reduce_add_f32_2p28"] = {"ms": round(t * 1e3, 3), "gbs": round(4 * N / t / 1e9, 1)}
+    del a, b2, z
     return out
 
 

@@ -284,6 +284,37 @@ int gg_apply(gg_ctx* ctx, int op, void* z, int z_dtype, const void* x, int x_dty
    again the same way; exact monoids give the same value in any order.  Synchronous. */
 int gg_reduce(gg_ctx* ctx, int add, const void* x, int x_dtype, int64_t n, void* out);
 
+/* ---- graph files (host) --------------------------------------------------------- */
+/*
+ * Reads an assembled Rutherford-Boeing (or Harwell-Boeing) matrix file: the files the
+ * reference's benchmark loads with RutherfordBoeingData (benchmark/benchmarks.jl:262-266).
+ * Returns the m x n matrix as CSC: 1-based Int32 colptr (n+1) / rowval (nnz, rows
+ * ascending in each column) and Float64 values (1.0 for pattern files), all allocated
+ * by the library on the host (release each with gg_host_free).  expand_symmetric != 0
+ * mirrors the stored triangle of symmetric / skew-symmetric / Hermitian files.  kind
+ * (may be NULL): bit 0 pattern, bit 1 integer, bit 2 symmetric, bit 3 skew, bit 4
+ * Hermitian.  Fields are read by the widths of the file's Fortran formats.  Repeated
+ * entries keep the first.  GG_ERR_ARGUMENT for unreadable or malformed files,
+ * GG_ERR_UNSUPPORTED for complex or elemental files.
+ */
+int gg_read_rb(const char* path, int expand_symmetric, int64_t* m, int64_t* n, int64_t* nnz,
+               int32_t** colptr, int32_t** rowval, double** values, int* kind);
+
+/*
+ * Reads an edge list (GraphIO.EdgeList, benchmark/benchmarks.jl:12-14): one edge
+ * "u v [w]" per line (spaces, tabs or commas), '#' / '%' comment lines, vertex ids
+ * starting at `base` (0 or 1).  Returns the adjacency A (A[u, v] for the edge u -> v)
+ * of nv = largest id + 1 - base vertices as CSC, which is the CSR storage of A_T, the
+ * form the graph calls take: colptr (nv+1), rowval, values (w, or 1.0 without a third
+ * column; *weighted says which), host memory released with gg_host_free.  A repeated
+ * edge keeps its first weight.
+ */
+int gg_read_edgelist(const char* path, int base, int64_t* nv, int64_t* nnz, int32_t** colptr,
+                     int32_t** rowval, double** values, int* weighted);
+
+/* Releases host memory returned by gg_read_rb / gg_read_edgelist. */
+int gg_host_free(void* p);
+
 /* ---- graph algorithms ------------------------------------------------------- */
 
 /*
