@@ -23,7 +23,9 @@ export AbstractSparseGPUMatrix, SparseGPUMatrixCSR, SparseGPUMatrixSELL, gpu_spm
        sprand_gpu, monoid_neutral, monoid_absorb, bfs_distances, bfs_distances!, bfs_parents,
        bfs_parents!, shortest_path, shortest_path!, GPUGraphs_add, GPUGraphs_safe_add,
        GPUGraphs_mul, GPUGraphs_second, GPUGraphs_band, GPUGraphs_bor, GPUGraphs_any,
-       GPUGraphs_secondi, GPUGraphs_max, GPUGraphs_min
+       GPUGraphs_secondi, GPUGraphs_max, GPUGraphs_min, SparseGPUVector, SparseGPUMatrixCSC,
+       gpu_spmspv!, gpu_spmspv, gpu_spmv_rows!, gpu_ewise!, gpu_apply!, gpu_reduce, read_rb,
+       read_edgelist
 
 # ---------------------------------------------------------------------------------
 # algebra (src/algebra.jl): same functions, plus their operator codes in the C ABI
@@ -348,5 +350,169 @@ shortest_path!(A_T::AbstractSparseGPUMatrix, source::Integer, dist, next, update
                diff = nothing) = _sssp!(A_T, Int64[source], dist, next)
 shortest_path!(A_T::AbstractSparseGPUMatrix, sources::AbstractVector{<:Integer}, dist, next,
                updated = nothing, diff = nothing) = _sssp!(A_T, Vector{Int64}(sources), dist, next)
+
+# ---------------------------------------------------------------------------------
+# sparse vectors (src/GPUGraphsVector.jl), SpMSpV (src/spmspv.jl), the sparse-mask
+# kernel (src/spmv/CSR.jl:90-115), CSC SpMV (src/spmv/CSC.jl) and the e-wise /
+# map-reduce steps the reference leaves to broadcasts
+# ---------------------------------------------------------------------------------
+mutable struct SparseGPUVector{Tv,Ti<:Integer}
+    n::Int
+    nzind::CuVector{Ti}
+    nzval::CuVector{Tv}
+end
+
+function SparseGPUVector(n::Integer, nzind::AbstractVector, nzval::AbstractVector{Tv},
+                         backend = nothing) where {Tv}
+    length(nzind) != length(nzval) &&
+        throw(ArgumentError("length(nzind) must be equal to length(nzval)"))
+    return SparseGPUVector{Tv,Int32}(Int(n), CuVector{Int32}(nzind), CuVector{Tv}(nzval))
+end
+SparseGPUVector(v::SparseVector{Tv}, backend = nothing) where {Tv} =
+    SparseGPUVector(length(v), v.nzind, v.nzval)
+function SparseGPUVector(v::Vector{Tv}, backend = nothing) where {Tv}
+    nzind = findall(!iszero, v)
+    return SparseGPUVector(length(v), nzind, v[nzind])
+end
+
+"""
+    gpu_spmspv!(C, A, B::SparseGPUVector; mul, add, accum) -> rows
+
+For every row i of A holding an entry whose column carries an entry of B,
+C[i] = accum(C[i], add over those entries of mul(A[i, j], B[j], i, j, j, 1)) in storage
+order; returns the 1-based rows written, ascending.
+"""
+function gpu_spmspv!(C::CuVector{Tr}, A::SparseGPUMatrixCSR{Tv}, B::SparseGPUVector{Tx};
+                     mul::Function = GPUGraphs_mul, add::Function = GPUGraphs_add,
+                     accum::Function = GPUGraphs_second) where {Tr,Tv,Tx}
+    size(A, 2) != B.n && throw(DimensionMismatch("Matrix dimensions must agree"))
+    size(C, 1) != size(A, 1) && throw(DimensionMismatch("Matrix dimensions must agree"))
+    rows = CuVector{Int32}(undef, max(size(A, 1), 1))
+    cnt = Ref{Int64}(0)
+    check(ccall((:gg_spmspv, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cint, CuPtr{Cvoid}, Cint, Int64, CuPtr{Int32},
+                 CuPtr{Cvoid}, Cint, Int64, Int64, CuPtr{Int32}, Ptr{Int64}),
+                ctx(), A.handle, opcode(mul), opcode(add), opcode(accum), pointer(C), dtcode(Tr),
+                length(C), pointer(B.nzind), pointer(B.nzval), dtcode(Tx), length(B.nzind), B.n,
+                pointer(rows), cnt))
+    return rows[1:cnt[]]
+end
+
+function gpu_spmspv(A::SparseGPUMatrixCSR{Tv}, B::SparseGPUVector{Tx};
+                    mul::Function = GPUGraphs_mul, add::Function = GPUGraphs_add) where {Tv,Tx}
+    C = CUDA.zeros(promote_type(Tv, Tx), size(A, 1))
+    rows = gpu_spmspv!(C, A, B; mul = mul, add = add, accum = GPUGraphs_second)
+    return SparseGPUVector{eltype(C),Int32}(size(A, 1), rows, C[rows])
+end
+
+function gpu_spmv_rows!(C::CuVector{Tr}, A::SparseGPUMatrixCSR{Tv}, B::CuVector{Tx},
+                        rows::CuVector{Int32}; mul::Function = GPUGraphs_mul,
+                        add::Function = GPUGraphs_add,
+                        accum::Function = GPUGraphs_second) where {Tr,Tv,Tx}
+    check(ccall((:gg_spmv_rows, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cint, CuPtr{Cvoid}, Cint, Int64, CuPtr{Cvoid},
+                 Cint, Int64, CuPtr{Int32}, Int64),
+                ctx(), A.handle, opcode(mul), opcode(add), opcode(accum), pointer(C), dtcode(Tr),
+                length(C), pointer(B), dtcode(Tx), length(B), pointer(rows), length(rows)))
+    return nothing
+end
+
+# CSC: held as the CSR storage of the transpose (same colptr / rowval / nzval)
+mutable struct SparseGPUMatrixCSC{Tv,Ti<:Integer} <: AbstractSparseGPUMatrix{Tv,Ti}
+    t::SparseGPUMatrixCSR{Tv,Ti}
+    m::Int
+    n::Int
+    colptr::CuVector{Ti}
+    rowval::CuVector{Ti}
+    nzval::CuVector{Tv}
+end
+
+function SparseGPUMatrixCSC(m::Int, n::Int, colptr::AbstractVector, rowval::AbstractVector,
+                            nzval::AbstractVector{Tv}, backend = nothing) where {Tv}
+    t = SparseGPUMatrixCSR(n, m, colptr, rowval, nzval)
+    return SparseGPUMatrixCSC{Tv,Int32}(t, m, n, t.rowptr, t.colval, t.nzval)
+end
+SparseGPUMatrixCSC(A::SparseMatrixCSC{Tv}, backend = nothing) where {Tv} =
+    SparseGPUMatrixCSC(size(A, 1), size(A, 2), A.colptr, A.rowval, A.nzval)
+
+function gpu_spmv!(C::CuVector{Tr}, A::SparseGPUMatrixCSC{Tv}, B::CuVector{Tx};
+                   mul::Function = GPUGraphs_mul, add::Function = GPUGraphs_add,
+                   accum::Function = GPUGraphs_second,
+                   range::Union{Nothing,UnitRange} = nothing,
+                   mask::Union{Nothing,AbstractVector} = nothing) where {Tr,Tv,Tx}
+    size(A, 2) != length(B) && throw(DimensionMismatch("Matrix dimensions must agree"))
+    size(C, 1) != size(A, 1) && throw(DimensionMismatch("Matrix dimensions must agree"))
+    mp, mt, ml = mask === nothing ? (C_NULL, Cint(0), Int64(0)) :
+                 (pointer(mask), dtcode(eltype(mask)), Int64(length(mask)))
+    lo, hi = range === nothing ? (0, 0) : (first(range), last(range))
+    check(ccall((:gg_spmv_t, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cint, CuPtr{Cvoid}, Cint, Int64, CuPtr{Cvoid},
+                 Cint, Int64, CuPtr{Cvoid}, Cint, Int64, Int64, Int64),
+                ctx(), A.t.handle, opcode(mul), opcode(add), opcode(accum), pointer(C), dtcode(Tr),
+                length(C), pointer(B), dtcode(Tx), length(B), mp, mt, ml, lo, hi))
+    return nothing
+end
+
+function gpu_ewise!(z::CuVector{Tz}, x::CuVector{Tx}, y::CuVector{Ty}, op::Function;
+                    mask::Union{Nothing,CuVector} = nothing) where {Tz,Tx,Ty}
+    check(ccall((:gg_ewise, LIB), Cint,
+                (Ptr{Cvoid}, Cint, CuPtr{Cvoid}, Cint, CuPtr{Cvoid}, Cint, CuPtr{Cvoid}, Cint, Int64,
+                 CuPtr{Cvoid}, Cint),
+                ctx(), opcode(op), pointer(z), dtcode(Tz), pointer(x), dtcode(Tx), pointer(y),
+                dtcode(Ty), length(z), mask === nothing ? CU_NULL : pointer(mask),
+                mask === nothing ? Cint(0) : dtcode(eltype(mask))))
+    return z
+end
+
+function gpu_apply!(z::CuVector{Tz}, x::CuVector{Tx}, s::Ts, op::Function;
+                    bind_first::Bool = false, mask::Union{Nothing,CuVector} = nothing) where {Tz,Tx,Ts}
+    sr = Ref{Ts}(s)
+    check(ccall((:gg_apply, LIB), Cint,
+                (Ptr{Cvoid}, Cint, CuPtr{Cvoid}, Cint, CuPtr{Cvoid}, Cint, Ptr{Cvoid}, Cint, Cint,
+                 Int64, CuPtr{Cvoid}, Cint),
+                ctx(), opcode(op), pointer(z), dtcode(Tz), pointer(x), dtcode(Tx), sr, dtcode(Ts),
+                Cint(bind_first), length(z), mask === nothing ? CU_NULL : pointer(mask),
+                mask === nothing ? Cint(0) : dtcode(eltype(mask))))
+    return z
+end
+
+function gpu_reduce(x::CuVector{T}, add::Function) where {T}
+    out = Ref{T}()
+    check(ccall((:gg_reduce, LIB), Cint, (Ptr{Cvoid}, Cint, CuPtr{Cvoid}, Cint, Int64, Ptr{Cvoid}),
+                ctx(), opcode(add), pointer(x), dtcode(T), length(x), out))
+    return out[]
+end
+
+# graph files (host): Rutherford-Boeing / Harwell-Boeing matrices and edge lists
+function _take_host(cp, rv, vv, ncol, nnz)
+    colptr = copy(unsafe_wrap(Array, Ptr{Int32}(cp[]), ncol + 1))
+    rowval = copy(unsafe_wrap(Array, Ptr{Int32}(rv[]), nnz))
+    vals = copy(unsafe_wrap(Array, Ptr{Float64}(vv[]), nnz))
+    for p in (cp[], rv[], vv[])
+        ccall((:gg_host_free, LIB), Cint, (Ptr{Cvoid},), p)
+    end
+    return colptr, rowval, vals
+end
+
+function read_rb(path::AbstractString; expand_symmetric::Bool = true)
+    m = Ref{Int64}(); n = Ref{Int64}(); nnz = Ref{Int64}(); kind = Ref{Cint}()
+    cp = Ref{Ptr{Cvoid}}(); rv = Ref{Ptr{Cvoid}}(); vv = Ref{Ptr{Cvoid}}()
+    check(ccall((:gg_read_rb, LIB), Cint,
+                (Cstring, Cint, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}},
+                 Ptr{Ptr{Cvoid}}, Ptr{Cint}), path, Cint(expand_symmetric), m, n, nnz, cp, rv, vv, kind))
+    colptr, rowval, vals = _take_host(cp, rv, vv, n[], nnz[])
+    return SparseMatrixCSC{Float64,Int32}(m[], n[], colptr, rowval, vals)
+end
+
+# adjacency A (A[u, v] for the edge u -> v) of an edge-list file
+function read_edgelist(path::AbstractString; base::Integer = 1)
+    nv = Ref{Int64}(); nnz = Ref{Int64}(); w = Ref{Cint}()
+    cp = Ref{Ptr{Cvoid}}(); rv = Ref{Ptr{Cvoid}}(); vv = Ref{Ptr{Cvoid}}()
+    check(ccall((:gg_read_edgelist, LIB), Cint,
+                (Cstring, Cint, Ptr{Int64}, Ptr{Int64}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}},
+                 Ptr{Ptr{Cvoid}}, Ptr{Cint}), path, Cint(base), nv, nnz, cp, rv, vv, w))
+    colptr, rowval, vals = _take_host(cp, rv, vv, nv[], nnz[])
+    return SparseMatrixCSC{Float64,Int32}(nv[], nv[], colptr, rowval, vals)
+end
 
 end # module
