@@ -35,14 +35,57 @@ static int ew_grid(gg_ctx* ctx, int64_t n) {
 template <int TC>
 __global__ void k_ewise(int op, void* z, int tz, const void* __restrict__ x, int tx,
                         const void* __restrict__ y, int ty, int64_t n, const void* __restrict__ mask,
-                        int tmask) {
+                        int tmask, int64_t ibase) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     if (mask && raw_is_zero(load_raw(mask, tmask, i), tmask)) continue;
     const Raw a = load_raw(x, tx, i), b = load_raw(y, ty, i);
+    const int64_t r1 = ibase + i + 1;  // the entry's 1-based index for index operators
     const typename CType<TC>::T v =
-        apply_op<TC>(op, raw_to<TC>(a, tx), raw_to<TC>(b, ty), b, ty, i + 1, 1, i + 1, 1);
+        apply_op<TC>(op, raw_to<TC>(a, tx), raw_to<TC>(b, ty), b, ty, r1, 1, r1, 1);
     store_as<TC>(z, tz, i, v);
+  }
+}
+
+// same (non-Bool) element type everywhere, no mask, 16-byte aligned: 16 bytes of each
+// operand per load (kV values), two vectors per thread in flight; the tail [nv * kV, n)
+// is left to k_ewise
+template <int TC>
+__global__ void k_ewise_vec(int op, void* z, const void* __restrict__ x,
+                            const void* __restrict__ y, int64_t nv) {
+  typedef typename CType<TC>::T T;
+  const int kV = 16 / sizeof(T);
+  const uint4* xv = static_cast<const uint4*>(x);
+  const uint4* yv = static_cast<const uint4*>(y);
+  uint4* zv = static_cast<uint4*>(z);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += 2 * stride) {
+    const bool two = v + stride < nv;
+    uint4 a0 = __ldcs(xv + v), b0 = __ldcs(yv + v), a1 = a0, b1 = b0;
+    if (two) {
+      a1 = __ldcs(xv + v + stride);
+      b1 = __ldcs(yv + v + stride);
+    }
+    const T* pa0 = reinterpret_cast<const T*>(&a0);
+    const T* pb0 = reinterpret_cast<const T*>(&b0);
+    const T* pa1 = reinterpret_cast<const T*>(&a1);
+    const T* pb1 = reinterpret_cast<const T*>(&b1);
+    uint4 r0, r1;
+    T* q0 = reinterpret_cast<T*>(&r0);
+    T* q1 = reinterpret_cast<T*>(&r1);
+#pragma unroll
+    for (int e = 0; e < kV; ++e) {
+      const int64_t i0 = v * kV + e, i1 = (v + stride) * kV + e;
+      Raw b;
+      b.d = 0;
+      b.i = 0;
+      if (dtype_is_float(TC)) b.d = static_cast<double>(pb0[e]); else b.i = static_cast<int64_t>(pb0[e]);
+      q0[e] = apply_op<TC>(op, pa0[e], pb0[e], b, TC, i0 + 1, 1, i0 + 1, 1);
+      if (dtype_is_float(TC)) b.d = static_cast<double>(pb1[e]); else b.i = static_cast<int64_t>(pb1[e]);
+      q1[e] = apply_op<TC>(op, pa1[e], pb1[e], b, TC, i1 + 1, 1, i1 + 1, 1);
+    }
+    __stcs(zv + v, r0);
+    if (two) __stcs(zv + v + stride, r1);
   }
 }
 
@@ -109,7 +152,27 @@ __global__ void __launch_bounds__(kRedThreads)
 template <int TC>
 static int ewise_t(gg_ctx* ctx, int op, void* z, int tz, const void* x, int tx, const void* y,
                    int ty, int64_t n, const void* mask, int tmask) {
-  k_ewise<TC><<<ew_grid(ctx, n), 256, 0, ctx->stream>>>(op, z, tz, x, tx, y, ty, n, mask, tmask);
+  typedef typename CType<TC>::T T;
+  const int kV = 16 / (int)sizeof(T);
+  const bool aligned = ((reinterpret_cast<uintptr_t>(z) | reinterpret_cast<uintptr_t>(x) |
+                         reinterpret_cast<uintptr_t>(y)) & 15u) == 0;
+  if (TC != GG_BOOL && !mask && tx == TC && ty == TC && tz == TC && aligned && n >= kV) {
+    const int64_t nv = n / kV;
+    k_ewise_vec<TC><<<ew_grid(ctx, nv), 256, 0, ctx->stream>>>(op, z, x, y, nv);
+    GG_CUDA(cudaGetLastError());
+    trace_count(ctx, 1);
+    const int64_t done = nv * kV;
+    if (done == n) return GG_OK;
+    // the last n - done values, shifted so that entry i keeps its index
+    T* zt = static_cast<T*>(z) + done;
+    k_ewise<TC><<<1, 256, 0, ctx->stream>>>(op, zt, tz, static_cast<const T*>(x) + done, tx,
+                                            static_cast<const T*>(y) + done, ty, n - done,
+                                            nullptr, 0, done);
+    GG_CUDA(cudaGetLastError());
+    trace_count(ctx, 1);
+    return GG_OK;
+  }
+  k_ewise<TC><<<ew_grid(ctx, n), 256, 0, ctx->stream>>>(op, z, tz, x, tx, y, ty, n, mask, tmask, 0);
   GG_CUDA(cudaGetLastError());
   trace_count(ctx, 1);
   return GG_OK;

@@ -24,12 +24,16 @@
 //
 // Both bitmaps are all zero between calls: each call clears the bits it set (the
 // reached rows while writing the ordered result pattern, or from the reached list).
+#include <vector>
+
 #include "gg_semiring.cuh"
 
 namespace gg {
 
 static const int kSpvShort = 32;  // longer rows are folded by a warp
 static const int kEmitWords = 1024;  // bitmap words per block of the ordered pattern
+static const int kSpvPiece = 2048;   // entries of a long-row piece
+static const int kPushLong = 4096;   // longer columns are pushed in pieces by all warps
 
 // column index of a CSR matrix plus the SpMSpV workspace (built on first use)
 struct SpvPlan {
@@ -42,8 +46,15 @@ struct SpvPlan {
   int32_t* tlist = nullptr;   // [m] rows reached, in arrival order
   int32_t* llist = nullptr;   // [m] listed rows longer than kSpvShort
   int32_t* bsum = nullptr;    // [blocks + 1] offsets of the ordered pattern
-  unsigned* ctr = nullptr;    // [4] reached rows, long rows, bad input, spare
+  unsigned* ctr = nullptr;    // [4] reached rows, long rows, bad input, long columns
   unsigned* h_ctr = nullptr;  // pinned copy of ctr
+  // rows longer than kSpvShort cut into pieces of kSpvPiece entries (index build)
+  int4* pieces = nullptr;       // [npieces] (row, first entry, end entry, 0), 0-based
+  int64_t npieces = 0;
+  int32_t* first_piece = nullptr;  // [m] first piece of each long row
+  int32_t* pcnt = nullptr;         // [npieces] present entries of a piece (this call)
+  void* prod = nullptr;            // [nnz] products of present entries, compacted per piece
+  int32_t* lcol = nullptr;         // [n] columns of x too long for one warp's push (this call)
 };
 
 void free_spv_plan(gg_mat* A) {
@@ -59,6 +70,11 @@ void free_spv_plan(gg_mat* A) {
   cudaFree(p->bsum);
   cudaFree(p->ctr);
   cudaFreeHost(p->h_ctr);
+  cudaFree(p->pieces);
+  cudaFree(p->first_piece);
+  cudaFree(p->pcnt);
+  cudaFree(p->prod);
+  cudaFree(p->lcol);
   delete p;
   A->spv = nullptr;
 }
@@ -126,12 +142,16 @@ __global__ void k_spv_unscatter(const int32_t* __restrict__ ind, int64_t nx, int
 // warp per entry j of x: mark the rows of column j, listing each newly reached row
 __global__ void k_spv_push(const int32_t* __restrict__ ind, int64_t nx,
                            const int32_t* __restrict__ colptr, const int32_t* __restrict__ rows,
-                           unsigned* tbits, int32_t* tlist, unsigned* ctr) {
+                           unsigned* tbits, int32_t* tlist, unsigned* ctr, int32_t* lcol) {
   const int lane = threadIdx.x & 31;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nx; t += nw) {
     const int32_t j = ind[t] - 1;
     const int32_t e0 = colptr[j], e1 = colptr[j + 1];
+    if (e1 - e0 > kPushLong) {  // a hub column: k_spv_push_long spreads it over the grid
+      if (lane == 0) lcol[atomicAdd(ctr + 3, 1u)] = j;
+      continue;
+    }
     for (int32_t b = e0; b < e1; b += 32) {
       const int32_t e = b + lane;
       bool fresh = false;
@@ -149,6 +169,46 @@ __global__ void k_spv_push(const int32_t* __restrict__ ind, int64_t nx,
         if (fresh) tlist[base + __popc(fm & ((1u << lane) - 1u))] = i;
       }
     }
+  }
+}
+
+// the columns k_spv_push deferred, cut into pieces of kPushLong entries numbered across
+// all of them; warp w takes pieces w, w + nw, ... (every warp walks the short list of
+// deferred columns to find its pieces, so no warp waits for another)
+__global__ void k_spv_push_long(const int32_t* __restrict__ lcol, const int32_t* __restrict__ colptr,
+                                const int32_t* __restrict__ rows, unsigned* tbits,
+                                int32_t* tlist, unsigned* ctr) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const unsigned ncols = ctr[3];
+  int64_t qbase = 0;  // global number of this column's first piece
+  for (unsigned c = 0; c < ncols; ++c) {
+    const int32_t j = lcol[c];
+    const int32_t e0 = colptr[j], e1 = colptr[j + 1];
+    const int64_t np = (e1 - e0 + kPushLong - 1) / kPushLong;
+    for (int64_t pi = ((w - qbase) % nw + nw) % nw; pi < np; pi += nw) {
+      const int32_t pe0 = e0 + (int32_t)pi * kPushLong;
+      const int32_t pe1 = e1 - pe0 < kPushLong ? e1 : pe0 + kPushLong;
+      for (int32_t b = pe0; b < pe1; b += 32) {
+        const int32_t e = b + lane;
+        bool fresh = false;
+        int32_t i = 0;
+        if (e < pe1) {
+          i = rows[e];
+          const unsigned bit = 1u << (i & 31);
+          fresh = (atomicOr(tbits + (i >> 5), bit) & bit) == 0u;
+        }
+        const unsigned fm = __ballot_sync(0xffffffffu, fresh);
+        if (fm) {
+          unsigned base = 0;
+          if (lane == 0) base = atomicAdd(ctr, (unsigned)__popc(fm));
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if (fresh) tlist[base + __popc(fm & ((1u << lane) - 1u))] = i;
+        }
+      }
+    }
+    qbase += np;
   }
 }
 
@@ -170,10 +230,20 @@ __global__ void k_spv_pull(SRGen<TC> sr, const int32_t* __restrict__ rowptr,
       continue;
     }
     const int32_t k0 = rowptr[r] - 1, k1 = rowptr[r + 1] - 1;
-    if (k1 - k0 > kSpvShort) {
-      llist[atomicAdd(ctr + 1, 1u)] = (int32_t)r;
-      continue;
+    const bool is_long = k1 - k0 > kSpvShort;
+    {
+      // one atomic per warp for the long rows of this pass
+      const unsigned am = __activemask();
+      const unsigned lm = __ballot_sync(am, is_long);
+      if (lm) {
+        const int lane = threadIdx.x & 31, leader = __ffs(am) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(ctr + 1, (unsigned)__popc(lm));
+        base = __shfl_sync(am, base, leader);
+        if (is_long) llist[base + __popc(lm & ((1u << lane) - 1u))] = (int32_t)r;
+      }
     }
+    if (is_long) continue;
     T acc = sr.neutral();
     for (int32_t k = k0; k < k1; ++k) {
       const int32_t c1 = colval[k];
@@ -219,6 +289,90 @@ __global__ void k_spv_pull_long(SRGen<TC> sr, const int32_t* __restrict__ rowptr
         if (sr.is_absorb(acc)) {
           done = true;
           break;
+        }
+      }
+    }
+    if (lane == 0) sr.write(r, acc);
+  }
+}
+
+// Long rows of SpMSpV, pass 1: a warp per piece of a reached long row tests 128 entries
+// per step (4 per lane, loads issued together), multiplies the present ones and writes
+// their products compacted in storage order at the start of the piece's own range of
+// prod; pcnt[p] = how many.  Pieces of rows not reached cost one bitmap test.
+template <int TC>
+__global__ void k_spv_compact(SRGen<TC> sr, const int4* __restrict__ pieces, int64_t npieces,
+                              const int32_t* __restrict__ colval, const unsigned* __restrict__ tbits,
+                              const unsigned* __restrict__ xbits, int32_t* pcnt,
+                              typename SRGen<TC>::T* prod) {
+  typedef typename SRGen<TC>::T T;
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < npieces; p += nw) {
+    const int4 d = pieces[p];
+    if (!bit_set(tbits, d.x)) continue;
+    int32_t cnt = 0;
+    for (int32_t base = d.y; base < d.z; base += 128) {
+      int32_t c[4];
+      bool on[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int32_t k = base + 32 * u + lane;
+        c[u] = k < d.z ? __ldg(colval + k) : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) on[u] = c[u] > 0 && bit_set(xbits, c[u] - 1);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int32_t k = base + 32 * u + lane;
+        const unsigned m = __ballot_sync(0xffffffffu, on[u]);
+        if (on[u])
+          prod[d.y + cnt + __popc(m & ((1u << lane) - 1u))] = sr.mulk(k, c[u], (int64_t)d.x + 1);
+        cnt += __popc(m);
+      }
+    }
+    if (lane == 0) pcnt[p] = cnt;
+  }
+}
+
+// Long rows of SpMSpV, pass 2: a warp per reached long row walks its pieces 32 counts at
+// a time and adds the compacted products in order (every lane holds the same sum; the
+// warp leaves at the first absorbing value), then writes the row.
+template <int TC>
+__global__ void k_spv_fold_long(SRGen<TC> sr, const int32_t* __restrict__ rowptr,
+                                const int32_t* __restrict__ llist, const unsigned* __restrict__ ctr,
+                                const int32_t* __restrict__ first_piece,
+                                const int32_t* __restrict__ pcnt,
+                                const typename SRGen<TC>::T* __restrict__ prod) {
+  typedef typename SRGen<TC>::T T;
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t cnt_rows = ctr[1];
+  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < cnt_rows; t += nw) {
+    const int32_t r = llist[t];
+    const int32_t k0 = rowptr[r] - 1, k1 = rowptr[r + 1] - 1;
+    const int32_t p0 = first_piece[r];
+    const int32_t np = (k1 - k0 + kSpvPiece - 1) / kSpvPiece;
+    T acc = sr.neutral();
+    bool done = false;
+    for (int32_t pb = 0; pb < np && !done; pb += 32) {
+      const int32_t cl = pb + lane < np ? pcnt[p0 + pb + lane] : 0;
+      unsigned nzm = __ballot_sync(0xffffffffu, cl > 0);
+      while (nzm && !done) {
+        const int src = __ffs(nzm) - 1;
+        nzm &= nzm - 1u;
+        const int32_t cnt = __shfl_sync(0xffffffffu, cl, src);
+        const int64_t start = (int64_t)k0 + (int64_t)(pb + src) * kSpvPiece;
+        for (int32_t q = 0; q < cnt && !done; q += 32) {
+          const T v = q + lane < cnt ? prod[start + q + lane] : sr.neutral();
+          const int n = cnt - q < 32 ? cnt - q : 32;
+          for (int i = 0; i < n; ++i) {
+            acc = sr.addv(acc, shfl_from<T>(v, i));
+            if (sr.is_absorb(acc)) {
+              done = true;
+              break;
+            }
+          }
         }
       }
     }
@@ -331,6 +485,7 @@ static int ensure_spv(gg_ctx* ctx, gg_mat* A, bool index) {
     if (e == cudaSuccess) e = cudaMalloc((void**)&p->llist, (m > 0 ? m : 1) * sizeof(int32_t));
     if (e == cudaSuccess)
       e = cudaMalloc((void**)&p->bsum, (mw / kEmitWords + 2) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&p->lcol, (n > 0 ? n : 1) * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMalloc((void**)&p->ctr, 4 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&p->h_ctr, 4 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemsetAsync(p->xbits, 0, nwd * sizeof(unsigned), ctx->stream);
@@ -363,8 +518,31 @@ static int ensure_spv(gg_ctx* ctx, gg_mat* A, bool index) {
     if (e != cudaSuccess) rc = cuda_error(e, "column index");
   }
   cudaFree(cnt);
-  if (rc == GG_OK) p->indexed = true;
-  return rc;
+  if (rc != GG_OK) return rc;
+  // pieces of the long rows (host table from the row pointers) and the product buffer
+  std::vector<int32_t> rp((size_t)m + 1);
+  GG_CUDA(cudaMemcpy(rp.data(), A->rowptr, (m + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  std::vector<int4> pcs;
+  std::vector<int32_t> first((size_t)(m > 0 ? m : 1), -1);
+  for (int64_t r = 0; r < m; ++r) {
+    const int32_t k0 = rp[(size_t)r] - 1, k1 = rp[(size_t)r + 1] - 1;
+    if (k1 - k0 <= kSpvShort) continue;
+    first[(size_t)r] = (int32_t)pcs.size();
+    for (int32_t k = k0; k < k1; k += kSpvPiece)
+      pcs.push_back(make_int4((int32_t)r, k, k1 - k < kSpvPiece ? k1 : k + kSpvPiece, 0));
+  }
+  p->npieces = (int64_t)pcs.size();
+  const size_t np = pcs.size() > 0 ? pcs.size() : 1;
+  GG_CUDA(cudaMalloc((void**)&p->pieces, np * sizeof(int4)));
+  GG_CUDA(cudaMalloc((void**)&p->pcnt, np * sizeof(int32_t)));
+  GG_CUDA(cudaMalloc((void**)&p->first_piece, first.size() * sizeof(int32_t)));
+  GG_CUDA(cudaMalloc(&p->prod, (size_t)(nnz > 0 ? nnz : 1) * 8));
+  if (!pcs.empty())
+    GG_CUDA(cudaMemcpy(p->pieces, pcs.data(), pcs.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  GG_CUDA(cudaMemcpy(p->first_piece, first.data(), first.size() * sizeof(int32_t),
+                     cudaMemcpyHostToDevice));
+  p->indexed = true;
+  return GG_OK;
 }
 
 template <int TC>
@@ -401,6 +579,22 @@ static int spv_pull(gg_ctx* ctx, gg_mat* A, const SRGen<TC>& sr, const int32_t* 
         sr, A->rowptr, A->colval, rows ? rows : p->tlist, rows ? nullptr : p->ctr, nrows,
         rows ? 1 : 0, m, p->xbits, p->llist, p->ctr);
     GG_CUDA(cudaGetLastError());
+    if (kSparse) {
+      // long rows: present products compacted per piece by many warps, then folded in
+      // order by a warp per row (a hub is not walked by one warp entry by entry)
+      typedef typename SRGen<TC>::T T;
+      if (p->npieces > 0) {
+        k_spv_compact<TC><<<spv_grid(ctx, p->npieces * 32), 256, 0, ctx->stream>>>(
+            sr, p->pieces, p->npieces, A->colval, p->tbits, p->xbits, p->pcnt,
+            static_cast<T*>(p->prod));
+        GG_CUDA(cudaGetLastError());
+        k_spv_fold_long<TC><<<spv_grid(ctx, bound * 32), 256, 0, ctx->stream>>>(
+            sr, A->rowptr, p->llist, p->ctr, p->first_piece, p->pcnt, static_cast<const T*>(p->prod));
+        GG_CUDA(cudaGetLastError());
+      }
+      trace_count(ctx, 3);
+      return GG_OK;
+    }
     k_spv_pull_long<TC, kSparse><<<spv_grid(ctx, bound * 32), 256, 0, ctx->stream>>>(
         sr, A->rowptr, A->colval, p->llist, p->ctr, p->xbits);
     GG_CUDA(cudaGetLastError());
@@ -433,9 +627,12 @@ static int spmspv_t(gg_ctx* ctx, gg_mat* A, int mul, int add, int accum, void* y
     const int tr = trace_main_begin(ctx);
     k_spv_push<<<spv_grid(ctx, x_nnz * 32), 256, 0, ctx->stream>>>(x_ind, x_nnz, p->colptr,
                                                                    p->rows, p->tbits, p->tlist,
-                                                                   p->ctr);
+                                                                   p->ctr, p->lcol);
     GG_CUDA(cudaGetLastError());
-    trace_count(ctx, 2);
+    k_spv_push_long<<<spv_grid(ctx, (int64_t)ctx->num_sms * 2048), 256, 0, ctx->stream>>>(
+        p->lcol, p->colptr, p->rows, p->tbits, p->tlist, p->ctr);
+    GG_CUDA(cudaGetLastError());
+    trace_count(ctx, 3);
     GG_CHECK((spv_pull<TC, true>(ctx, A, spv_semiring<TC>(A, mul, add, accum, y, ty, p->xs, tx),
                                  nullptr, 0)));
     trace_main_end(ctx, tr);

@@ -179,7 +179,8 @@ def test_spmv_rows_matches_oracle(dtype, mul, add):
 EW = [(O.ADD, np.float32), (O.MUL, np.float32), (O.MIN, np.float32), (O.MAX, np.float64),
       (O.MINUS, np.float32), (O.RMINUS, np.int32), (O.ADD, np.int32), (O.MIN, np.int64),
       (O.SAFE_ADD, np.int32), (O.LOR, np.bool_), (O.LAND, np.bool_), (O.ANY, np.int32),
-      (O.PAIR, np.float32), (O.SECOND, np.float32)]
+      (O.PAIR, np.float32), (O.SECOND, np.float32), (O.SECONDI, np.int64), (O.FIRSTI, np.int64),
+      (O.MIN, np.float64)]
 
 
 def ew_input(dtype, n, seed):
@@ -274,3 +275,44 @@ def test_reduce_multi_pass_order():
     rc, want = O.reduce(O.ADD, x)
     assert rc == 0 and got == want
     assert abs(float(got) - x.astype(np.float64).sum()) <= 1e-5 * x.astype(np.float64).sum()
+
+
+@pytest.mark.parametrize("mul,add", [(O.MUL, O.ADD), (O.ADD, O.MIN)])
+def test_spmspv_hub_rows_span_several_pieces(mul, add):
+    # rows of 20000 and 5000 entries (pieces of 2048), an absorbing +Inf inside a hub
+    m, n = 300, 20000
+    rng = np.random.default_rng(50)
+    D = sp.random(m, n, density=0.002, format="lil", random_state=rng, dtype=np.float64)
+    D[5, :] = rng.random(n) + 0.1
+    D[7, rng.choice(n, 5000, replace=False)] = 1.0
+    A = sp.csr_matrix(D).astype(np.float32)
+    A.sort_indices()
+    rp, cv, nz = (A.indptr + 1).astype(np.int32), (A.indices + 1).astype(np.int32), A.data.copy()
+    for density, special in ((0.3, False), (0.05, True), (1.0, False)):
+        ind, val = sparse_x(n, int(density * n), 51, np.float32)
+        if special:
+            val[len(val) // 2] = np.inf
+            val[len(val) // 2 + 3] = np.nan
+        y0 = np.zeros(m, np.float32)
+        got, rows, want_y, want_rows, _ = run_spmspv(m, n, rp, cv, nz, ind, val, y0, mul, add, O.SECOND)
+        assert np.array_equal(rows, want_rows)
+        assert same(got, want_y)
+
+
+def test_spmspv_hub_columns_pushed_by_the_grid():
+    # columns of 10000 and 6000 entries (longer than one warp's push share)
+    m, n = 10000, 500
+    rng = np.random.default_rng(60)
+    D = sp.random(m, n, density=0.004, format="lil", random_state=rng, dtype=np.float64)
+    D[:, 3] = rng.random((m, 1)) + 0.1
+    D[rng.choice(m, 6000, replace=False), 11] = 2.0
+    A = sp.csr_matrix(D).astype(np.float32)
+    A.sort_indices()
+    rp, cv, nz = (A.indptr + 1).astype(np.int32), (A.indices + 1).astype(np.int32), A.data.copy()
+    ind = np.array([3, 4, 11, 12, 100, 499], np.int32) + 1
+    val = (rng.random(len(ind)) + 0.5).astype(np.float32)
+    for mul, add in ((O.MUL, O.ADD), (O.ADD, O.MIN)):
+        got, rows, want_y, want_rows, _ = run_spmspv(m, n, rp, cv, nz, ind, val, np.zeros(m, np.float32),
+                                                     mul, add, O.SECOND)
+        assert np.array_equal(rows, want_rows)
+        assert same(got, want_y)
