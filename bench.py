@@ -696,6 +696,38 @@ def run_spmm(args):
         print(json.dumps(out), flush=True)
 
 
+def run_sparse_vector(args):
+    """SpMSpV over 1% of the vertices of R-MAT scale 22 (plus-times Float32), e-wise min
+    and reduce over 2^28 Float32 values: the sparse-vector, e-wise and reduce entry
+    points on their own.  The line's value is the SpMSpV's algorithmic GB/s."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    from gpugraphs import generators as gen
+    A = rmat(22, gen.W_U01_F32, device)
+    clk = ClockSampler(local)
+    clk.start()
+    sec = secondary_sparse_vector(device, A)
+    clocks = clk.stop()
+    sv = sec["spmspv_rmat22_1pct"]
+    peak, peak_kind = peak_hbm()
+    out = {
+        "metric": "SpMSpV GB/s (plus-times Float32, x on 1% of R-MAT scale 22's vertices)",
+        "value": sv["gbs_algorithmic"], "unit": "GB/s", "n_gpus": ws, "steps": 10, "warmup": 1,
+        "ms_per_step": sv["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded R-MAT generator on the device)",
+        "config": {"workload": "sparse_vector_rmat22", "n": A.n, "nnz": A.nnz(),
+                   "x_nnz": sv["x_nnz"]},
+        "roofline": {"bound": "hbm", "achieved": sv["gbs_algorithmic"], "peak": peak, "unit": "GB/s",
+                     "frac": round(sv["gbs_algorithmic"] / peak, 4), "traffic": None,
+                     "peak_kind": peak_kind},
+        "e2e": None, "clocks": clocks, "secondary": sec,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 # ---------------------------------------------------------------------------------
 # serving: Poisson arrivals over 16 resident graphs, continuous batching
 # ---------------------------------------------------------------------------------
@@ -1008,6 +1040,8 @@ def main():
         run_batch(args)
     elif args.workload == "spmm_rmat22":
         run_spmm(args)
+    elif args.workload == "sparse_vector_rmat22":
+        run_sparse_vector(args)
     elif args.workload == "serve":
         run_serve(args)
     elif args.workload == "multigraph":

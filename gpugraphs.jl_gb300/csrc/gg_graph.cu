@@ -477,26 +477,63 @@ __global__ void __launch_bounds__(256)
 }
 
 // pieces of the deferred frontier hubs: piece p of hub h has the global index
-// off_h + p (off_h = pieces of the hubs before it) and goes to warp (off_h + p) mod nw
-__device__ __forceinline__ int64_t first_piece(int64_t gw, int64_t nw, int64_t off) {
-  int64_t f = (gw - off) % nw;
-  return f < 0 ? f + nw : f;
+// hoff[h] + p (hoff = exclusive prefix sums of the hubs' piece counts, hoff[nh] = total);
+// warp w takes global pieces w, w + nw, ...
+__global__ void __launch_bounds__(1024)
+    k_hub_offsets(const int32_t* __restrict__ prow, const int32_t* __restrict__ hq,
+                  const Counters* hctr, int32_t* hoff) {
+  __shared__ int32_t wsum[32];
+  __shared__ int32_t carry;
+  const int64_t nh = (int64_t)*((volatile const unsigned long long*)&hctr->nh);
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t b0 = 0; b0 < nh; b0 += 1024) {
+    const int64_t i = b0 + threadIdx.x;
+    int32_t np = 0;
+    if (i < nh) {
+      const int32_t u = hq[i];
+      np = (prow[u + 1] - prow[u] + kPushPiece - 1) / kPushPiece;
+    }
+    const int32_t incl = block_incl_scan(np, wsum);
+    const int32_t c = carry;
+    if (i < nh) hoff[i] = c + incl - np;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = c + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) hoff[nh] = carry;
+}
+
+// the hub holding global piece q, searching forward from hub h (q only grows)
+__device__ __forceinline__ int64_t hub_of(const int32_t* __restrict__ hoff, int64_t nh, int64_t q,
+                                          int64_t h) {
+  if (__ldg(hoff + h + 1) > q) return h;
+  int64_t lo = h + 1, hi = nh - 1;  // last index with hoff[idx] <= q
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (__ldg(hoff + mid) <= q) lo = mid; else hi = mid - 1;
+  }
+  return lo;
 }
 
 __global__ void __launch_bounds__(256)
     k_bfs_push_hub(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
                    const int32_t* __restrict__ hq, int32_t level, unsigned* visited,
-                   int32_t* dist, int32_t* qn, Counters* ctr, const Counters* hctr) {
+                   int32_t* dist, int32_t* qn, Counters* ctr, const Counters* hctr,
+                   const int32_t* __restrict__ hoff) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t nh = (int64_t)*((volatile const unsigned long long*)&hctr->nh);
-  int64_t off = 0;
-  for (int64_t h = 0; h < nh; ++h) {
-    const int32_t u = hq[h];
-    const int32_t k0 = prow[u], k1 = prow[u + 1];
-    const int64_t np = (k1 - k0 + kPushPiece - 1) / kPushPiece;
-    for (int64_t p = first_piece(gw, nw, off); p < np; p += nw) {
+  if (nh == 0) return;
+  const int64_t npieces = hoff[nh];
+  int64_t h = 0;
+  for (int64_t q = gw; q < npieces; q += nw) {
+    h = hub_of(hoff, nh, q, h);
+    {
+      const int32_t u = hq[h];
+      const int32_t k0 = prow[u], k1 = prow[u + 1];
+      const int64_t p = q - hoff[h];
       const int32_t kb = k0 + (int32_t)p * kPushPiece;
       const int32_t ke = kb + kPushPiece < k1 ? kb + kPushPiece : k1;
       for (int32_t base = kb; base < ke; base += 32) {
@@ -515,7 +552,6 @@ __global__ void __launch_bounds__(256)
         warp_append(claim, w, deg, qn, ctr);
       }
     }
-    off += np;
   }
 }
 
@@ -1031,6 +1067,7 @@ struct BfsScratch {
   int32_t* hq;  // deferred frontier hubs (the first far list of near-far searches)
   int32_t* q2;  // the second far list
   int32_t* q3;  // the third far list
+  int32_t* hoff;  // piece offsets of the deferred hubs (k_hub_offsets)
   Counters* ctr;
   CoopCtl* cc;
 };
@@ -1039,7 +1076,7 @@ static int bfs_scratch(gg_ctx* ctx, int64_t n, BfsScratch* s) {
   const int64_t nw = (n + 31) / 32 + 1;
   const size_t bm = ((nw * sizeof(unsigned)) + 255) & ~(size_t)255;
   const size_t qb = (((n + 1) * sizeof(int32_t)) + 255) & ~(size_t)255;
-  GG_CHECK(ensure_scratch(ctx, 3 * bm + 5 * qb + 512));
+  GG_CHECK(ensure_scratch(ctx, 3 * bm + 6 * qb + 512));
   char* p = static_cast<char*>(ctx->scratch);
   s->visited = (unsigned*)p;
   s->fb[0] = (unsigned*)(p + bm);
@@ -1049,8 +1086,9 @@ static int bfs_scratch(gg_ctx* ctx, int64_t n, BfsScratch* s) {
   s->hq = (int32_t*)(p + 3 * bm + 2 * qb);
   s->q2 = (int32_t*)(p + 3 * bm + 3 * qb);
   s->q3 = (int32_t*)(p + 3 * bm + 4 * qb);
-  s->ctr = (Counters*)(p + 3 * bm + 5 * qb);
-  s->cc = (CoopCtl*)(p + 3 * bm + 5 * qb + 256);
+  s->hoff = (int32_t*)(p + 3 * bm + 5 * qb);
+  s->ctr = (Counters*)(p + 3 * bm + 6 * qb);
+  s->cc = (CoopCtl*)(p + 3 * bm + 6 * qb + 256);
   GG_CUDA(cudaMemsetAsync(p, 0, 3 * bm, ctx->stream));
   return GG_OK;
 }
@@ -1198,10 +1236,12 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
       k_bfs_push<<<gridsz(ctx, nf * 32), 256, 0, ctx->stream>>>(
           P.rowptr, P.colval, sc.q[cur], nf, (int32_t)level, sc.visited, dist, sc.q[cur ^ 1], sc.ctr,
           hubs ? sc.hq : nullptr);
-      if (hubs)
+      if (hubs) {
+        k_hub_offsets<<<1, 1024, 0, ctx->stream>>>(P.rowptr, sc.hq, sc.ctr, sc.hoff);
         k_bfs_push_hub<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(
             P.rowptr, P.colval, sc.hq, (int32_t)level, sc.visited, dist, sc.q[cur ^ 1], sc.ctr,
-            sc.ctr);
+            sc.ctr, sc.hoff);
+      }
       frontier_is_bitmap = false;
     }
     GG_CUDA(cudaGetLastError());
@@ -1328,21 +1368,22 @@ template <typename T>
 __global__ void __launch_bounds__(256)
     k_sssp_push_hub(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
                     const T* __restrict__ pw, const int32_t* __restrict__ hq, T* dist,
-                    unsigned* inq_next, int32_t* qn, Counters* ctr, const Counters* hctr) {
+                    unsigned* inq_next, int32_t* qn, Counters* ctr, const Counters* hctr,
+                    const int32_t* __restrict__ hoff) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t nh = (int64_t)*((volatile const unsigned long long*)&hctr->nh);
-  int64_t off = 0;
-  for (int64_t h = 0; h < nh; ++h) {
+  if (nh == 0) return;
+  const int64_t npieces = hoff[nh];
+  int64_t h = 0;
+  for (int64_t q = gw; q < npieces; q += nw) {
+    h = hub_of(hoff, nh, q, h);
     const int32_t u = hq[h];
     const int32_t k0 = prow[u], k1 = prow[u + 1];
-    const int64_t np = (k1 - k0 + kPushPiece - 1) / kPushPiece;
-    const int64_t p0 = first_piece(gw, nw, off);
-    off += np;
-    if (p0 >= np) continue;
     const T du = ld_cg(dist + u);
-    for (int64_t p = p0; p < np; p += nw) {
+    {
+      const int64_t p = q - hoff[h];
       const int32_t kb = k0 + (int32_t)p * kPushPiece;
       const int32_t ke = kb + kPushPiece < k1 ? kb + kPushPiece : k1;
       for (int32_t base = kb; base < ke; base += 32) {
@@ -1877,9 +1918,18 @@ __global__ void __launch_bounds__(256)
     const int cnt = nmid - g0 < 32 ? (int)(nmid - g0) : 32;
     T mine = Lim<T>::max();
     int32_t myv = -1;
+    // the group's row ids and row bounds, loaded by the lanes at once (row j in lane j),
+    // so each row's scan starts without waiting on its own id and row pointers
+    int32_t vj = -1;
+    int64_t k0j = 0, k1j = 0;
+    if (lane < cnt) {
+      vj = mid[g0 + lane];
+      k0j = (int64_t)rp[vj] - 1;
+      k1j = (int64_t)rp[vj + 1] - 1;
+    }
     for (int j = 0; j < cnt; ++j) {
-      const int32_t v = mid[g0 + j];
-      const int64_t k0 = (int64_t)rp[v] - 1, k1 = (int64_t)rp[v + 1] - 1;
+      const int32_t v = __shfl_sync(0xffffffffu, vj, j);
+      const int64_t k0 = __shfl_sync(0xffffffffu, k0j, j), k1 = __shfl_sync(0xffffffffu, k1j, j);
       T b = Lim<T>::max();
       for (int64_t kb = k0; kb < k1; kb += 128) {
         int32_t u[4];
@@ -2099,10 +2149,12 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
     k_sssp_push<T><<<gridsz(ctx, nf * 32), 256, 0, ctx->stream>>>(
         P.rowptr, P.colval, static_cast<const T*>(P.w), sc.q[cur], nf, d, sc.fb[cur],
         sc.fb[cur ^ 1], sc.q[cur ^ 1], sc.ctr, hubs ? sc.hq : nullptr);
-    if (hubs)
+    if (hubs) {
+      k_hub_offsets<<<1, 1024, 0, ctx->stream>>>(P.rowptr, sc.hq, sc.ctr, sc.hoff);
       k_sssp_push_hub<T><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(
           P.rowptr, P.colval, static_cast<const T*>(P.w), sc.hq, d, sc.fb[cur ^ 1], sc.q[cur ^ 1],
-          sc.ctr, sc.ctr);
+          sc.ctr, sc.ctr, sc.hoff);
+    }
     GG_CUDA(cudaGetLastError());
     GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
     GG_CUDA(cudaStreamSynchronize(ctx->stream));
