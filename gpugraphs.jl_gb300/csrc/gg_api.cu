@@ -195,6 +195,8 @@ static void free_derived(gg_mat* A) {
     cudaFree(A->hubplan->pieces);
     cudaFree(A->hubplan->acc);
     cudaFree(A->hubplan->mid);
+    cudaFree(A->hubplan->order);
+    cudaFree(A->hubplan->d_norder);
     delete A->hubplan;
     A->hubplan = nullptr;
   }

@@ -58,10 +58,15 @@ int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n) {
                    [](const int4& a, const int4& b) { return (a.z - a.y) > (b.z - b.y); });
   std::stable_sort(mid.begin(), mid.end(),
                    [&](int32_t a, int32_t b) { return rp[a + 1] - rp[a] > rp[b + 1] - rp[b]; });
+  std::vector<int32_t> order(mid);
+  for (int64_t v = 0; v < n; ++v)
+    if (rp[v + 1] - rp[v] <= 32) order.push_back((int32_t)v);
+  const unsigned long long norder = (unsigned long long)order.size();
   HubPlan* P = new HubPlan();
   P->nhub = (int64_t)hubs.size();
   P->npiece = (int64_t)pieces.size();
   P->nmid = (int64_t)mid.size();
+  P->norder = (int64_t)norder;
   cudaError_t e = cudaSuccess;
   auto up = [&](void** dst, const void* src, size_t bytes) {
     if (e != cudaSuccess) return;
@@ -72,6 +77,8 @@ int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n) {
   up((void**)&P->hubs, hubs.data(), hubs.size() * sizeof(int32_t));
   up((void**)&P->pieces, pieces.data(), pieces.size() * sizeof(int4));
   up((void**)&P->mid, mid.data(), mid.size() * sizeof(int32_t));
+  up((void**)&P->order, order.data(), order.size() * sizeof(int32_t));
+  up((void**)&P->d_norder, &norder, sizeof(norder));
   if (e == cudaSuccess) e = cudaMalloc(&P->acc, (P->nhub + 1) * kMaxW * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
@@ -79,6 +86,8 @@ int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n) {
     cudaFree(P->pieces);
     cudaFree(P->acc);
     cudaFree(P->mid);
+    cudaFree(P->order);
+    cudaFree(P->d_norder);
     delete P;
     return cuda_error(e, "hub analysis");
   }
@@ -280,8 +289,9 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
     k_ms_round<T><<<(int)gcap, 256, 0, R.st>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr,
                                                w.vlist, w.ctr + 3, w.cq[cur ^ 1], ncq_nxt);
   } else {
+    // every non-hub vertex, in the plan's order: the long rows first, spread over the warps
     k_ms_round<T><<<(int)gb, 256, 0, R.st>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr,
-                                             nullptr, nullptr, w.cq[cur ^ 1], ncq_nxt);
+                                             hp->order, hp->d_norder, w.cq[cur ^ 1], ncq_nxt);
   }
   GG_CUDA(cudaGetLastError());
   if (hp->npiece > 0) {

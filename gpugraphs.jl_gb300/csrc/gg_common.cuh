@@ -381,6 +381,11 @@ struct HubPlan {
   // rows of 33..kHubDegB entries (0-based), longest first: a warp each in pull rounds
   int32_t* mid = nullptr;
   int64_t nmid = 0;
+  // every non-hub row, the mid rows first (longest first), then the others ascending:
+  // the visiting order of full batched rounds (round-robin over warps balances them)
+  int32_t* order = nullptr;
+  unsigned long long* d_norder = nullptr;  // device copy of the order's length
+  int64_t norder = 0;
 };
 static const int kHubDegB = 2048;
 static const int kHubPieceB = 2048;

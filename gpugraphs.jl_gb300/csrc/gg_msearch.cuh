@@ -331,24 +331,50 @@ __global__ void __launch_bounds__(256)
   const int lane = threadIdx.x & 31;
   unsigned dropped_cols = 0;
   const int64_t total = vlist ? (int64_t)*((volatile const unsigned long long*)nlist) : n;
-  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < total;
-       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const int64_t v = vlist ? (int64_t)vlist[i] : i;
-    const int64_t k0 = (int64_t)g.rowptr[v] - 1, k1 = (int64_t)g.rowptr[v + 1] - 1;
-    if (k1 - k0 > kHubDegB) continue;
-    T best = Lim<T>::max();
-    const bool any = bs_pull<T>(g, D, chg, k0, k1, lane, best);
-    bool dropped = false;
-    if (any) {
-      T* dv = D + v * 32 + lane;
-      if (best < *dv) {
-        *dv = best;
-        dropped = true;
-      }
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  // the warp's vertices gw, gw + nw, ... taken 32 at a time: vertex j of a batch has its
+  // id and row bounds loaded by lane j up front, and the batch's changed vertices are
+  // counted and queued with one atomic each
+  for (int64_t i0 = gw; i0 < total; i0 += 32 * nw) {
+    const int64_t ij = i0 + (int64_t)lane * nw;
+    int64_t vj = -1, k0j = 0, k1j = 0;
+    if (ij < total) {
+      vj = vlist ? (int64_t)vlist[ij] : ij;
+      k0j = (int64_t)g.rowptr[vj] - 1;
+      k1j = (int64_t)g.rowptr[vj + 1] - 1;
     }
-    const unsigned b = __ballot_sync(kFullB, dropped);
-    dropped_cols |= b;
-    if (lane == 0 && b) ms_changed(v, b, chg_next, count, cq, ncq);
+    const unsigned live = __ballot_sync(kFullB, vj >= 0);
+    unsigned my_cols = 0;  // lane j: the columns that dropped for vertex j
+    for (int j = 0; j < 32 && ((live >> j) & 1u); ++j) {
+      const int64_t v = __shfl_sync(kFullB, vj, j);
+      const int64_t k0 = __shfl_sync(kFullB, k0j, j), k1 = __shfl_sync(kFullB, k1j, j);
+      if (k1 - k0 > kHubDegB) continue;
+      T best = Lim<T>::max();
+      const bool any = bs_pull<T>(g, D, chg, k0, k1, lane, best);
+      bool dropped = false;
+      if (any) {
+        T* dv = D + v * 32 + lane;
+        if (best < *dv) {
+          *dv = best;
+          dropped = true;
+        }
+      }
+      const unsigned b = __ballot_sync(kFullB, dropped);
+      dropped_cols |= b;
+      if (lane == j) my_cols = b;
+    }
+    if (my_cols) atomicOr(chg_next + vj, my_cols);
+    const unsigned cm = __ballot_sync(kFullB, my_cols != 0);
+    if (cm) {
+      unsigned long long qb = 0;
+      if (lane == 0) {
+        atomicAdd(count, (unsigned long long)__popc(cm));
+        if (cq) qb = atomicAdd(ncq, (unsigned long long)__popc(cm));
+      }
+      qb = __shfl_sync(kFullB, qb, 0);
+      if (cq && my_cols) cq[qb + __popc(cm & ((1u << lane) - 1u))] = (int32_t)vj;
+    }
   }
   if (drop && lane == 0 && dropped_cols) atomicOr(drop, dropped_cols);
 }

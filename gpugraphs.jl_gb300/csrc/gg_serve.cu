@@ -464,8 +464,10 @@ static void ss_round(gg_server* S, Executor& E, const SrvGraph& sg, const HubPla
     k_ms_round<T><<<grid_s(S, n * 32), 256, 0, st>>>(n, sg.g, D, E.c0, E.c1, E.d_cnt, E.d_amask,
                                                       E.vlist, E.d_cnt + 3, E.cq[cur ^ 1], ncq_nxt);
   } else {
+    // every non-hub vertex in the plan's order (long rows first, spread over the warps)
     k_ms_round<T><<<grid_s(S, n * 32), 256, 0, st>>>(n, sg.g, D, E.c0, E.c1, E.d_cnt, E.d_amask,
-                                                      nullptr, nullptr, E.cq[cur ^ 1], ncq_nxt);
+                                                      hp->order, hp->d_norder, E.cq[cur ^ 1],
+                                                      ncq_nxt);
   }
   if (hp->npiece > 0)
     k_ms_round_hub<T><<<grid_s(S, hp->npiece * 32), 256, 0, st>>>(
