@@ -1927,7 +1927,48 @@ __global__ void __launch_bounds__(256)
       k0j = (int64_t)rp[vj] - 1;
       k1j = (int64_t)rp[vj + 1] - 1;
     }
-    for (int j = 0; j < cnt; ++j) {
+    // groups whose longest row (the first: the list is sorted) has at most 128 entries:
+    // 8 lanes per row, 4 rows at once, 32 entries per step
+    const int64_t len0 = __shfl_sync(0xffffffffu, k1j - k0j, 0);
+    if (len0 <= 128) {
+      const int sub = lane >> 3, sl = lane & 7;
+      for (int j0 = 0; j0 < cnt; j0 += 4) {
+        const int r = j0 + sub;  // this sub-warp's row of the group
+        const int64_t k0 = __shfl_sync(0xffffffffu, k0j, r & 31);
+        const int64_t k1s = __shfl_sync(0xffffffffu, k1j, r & 31);
+        const int64_t k1 = r < cnt ? k1s : k0;
+        T b = Lim<T>::max();
+        for (int64_t kb = k0; kb < k1; kb += 32) {
+          int32_t u[4];
+          bool on[4];
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const int64_t k = kb + t * 8 + sl;
+            u[t] = k < k1 ? __ldg(cv + k) - 1 : -1;
+          }
+#pragma unroll
+          for (int t = 0; t < 4; ++t) on[t] = u[t] >= 0 && bit_of(chg, u[t]);
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const T c = on[t] ? relax_add(view_weight<T>(nz, tv, kb + t * 8 + sl), ld_cg(dist + u[t]))
+                              : Lim<T>::max();
+            b = c < b ? c : b;
+          }
+        }
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+          const T t = __shfl_xor_sync(0xffffffffu, b, o);
+          b = t < b ? t : b;
+        }
+        // lane j0 + q takes the minimum of sub-warp q (rows j0 .. j0 + 3)
+        const T got = __shfl_sync(0xffffffffu, b, ((lane - j0) & 3) * 8);
+        if (lane >= j0 && lane < j0 + 4 && lane < cnt) {
+          mine = got;
+          myv = vj;
+        }
+      }
+    }
+    for (int j = 0; j < cnt && len0 > 128; ++j) {
       const int32_t v = __shfl_sync(0xffffffffu, vj, j);
       const int64_t k0 = __shfl_sync(0xffffffffu, k0j, j), k1 = __shfl_sync(0xffffffffu, k1j, j);
       T b = Lim<T>::max();
