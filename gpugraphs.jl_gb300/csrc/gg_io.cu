@@ -4,6 +4,8 @@
 // the layout) and whitespace-separated edge lists (GraphIO.EdgeList,
 // benchmark/benchmarks.jl:12-14).
 //
+// Matrix Market coordinate files are read too (gg_read_mtx).
+//
 // Rutherford-Boeing, assembled matrices:
 //   line 1  title (columns 1-72) and key
 //   line 2  card counts (total, pointer, index, value[, right-hand side])
@@ -340,6 +342,97 @@ static int read_edgelist(const char* path, int base, HostMatrix* H, int* weighte
   return GG_OK;
 }
 
+// Matrix Market coordinate files (the other format SuiteSparse matrices are published
+// in): "%%MatrixMarket matrix coordinate <real|integer|pattern> <general|symmetric|
+// skew-symmetric>", '%' comment lines, a size line "m n nnz", then nnz lines "i j [v]"
+// with 1-based indices.  Symmetric / skew files store one triangle, expanded like the
+// Rutherford-Boeing ones when expand != 0.
+static int read_mtx(const char* path, int expand, HostMatrix* H, int* kind_out) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_error(GG_ERR_ARGUMENT, "cannot open %s", path);
+  LineReader R{f, {}};
+  int rc = GG_OK;
+  do {
+    if (!R.next()) { rc = set_error(GG_ERR_ARGUMENT, "%s: empty file", path); break; }
+    std::string banner = R.line;
+    for (auto& ch : banner) ch = (char)std::tolower((unsigned char)ch);
+    if (banner.compare(0, 14, "%%matrixmarket") != 0) {
+      rc = set_error(GG_ERR_ARGUMENT, "%s: no %%%%MatrixMarket banner", path);
+      break;
+    }
+    if (banner.find("coordinate") == std::string::npos) {
+      rc = set_error(GG_ERR_UNSUPPORTED, "%s: only coordinate (sparse) files are read", path);
+      break;
+    }
+    if (banner.find("complex") != std::string::npos) {
+      rc = set_error(GG_ERR_UNSUPPORTED, "%s: complex values", path);
+      break;
+    }
+    const bool pattern = banner.find("pattern") != std::string::npos;
+    const bool integer = banner.find("integer") != std::string::npos;
+    const bool skew = banner.find("skew-symmetric") != std::string::npos;
+    const bool herm = banner.find("hermitian") != std::string::npos;
+    const bool sym = !skew && !herm && banner.find("symmetric") != std::string::npos;
+    long long m = -1, n = -1, nnz = -1;
+    while (R.next()) {
+      const char* s = R.line.c_str();
+      while (*s == ' ' || *s == '\t') ++s;
+      if (!*s || *s == '%') continue;
+      if (std::sscanf(s, "%lld %lld %lld", &m, &n, &nnz) != 3) m = -1;
+      break;
+    }
+    if (m < 0 || n < 0 || nnz < 0) { rc = set_error(GG_ERR_ARGUMENT, "%s: bad size line", path); break; }
+    if (m >= (1LL << 31) || n >= (1LL << 31) || nnz >= (1LL << 31)) {
+      rc = set_error(GG_ERR_ARGUMENT, "%s: sizes do not fit Int32 indices", path);
+      break;
+    }
+    std::vector<int64_t> col, row;
+    std::vector<double> val;
+    const size_t cap = (size_t)nnz * ((expand && (sym || skew || herm)) ? 2 : 1);
+    col.reserve(cap);
+    row.reserve(cap);
+    val.reserve(cap);
+    long long got = 0;
+    while (got < nnz && R.next()) {
+      const char* s = R.line.c_str();
+      while (*s == ' ' || *s == '\t') ++s;
+      if (!*s || *s == '%') continue;
+      char* e = nullptr;
+      const long long i = std::strtoll(s, &e, 10);
+      const char* s2 = e;
+      const long long j = std::strtoll(s2, &e, 10);
+      if (e == s2) { rc = set_error(GG_ERR_ARGUMENT, "%s: bad entry line", path); break; }
+      double v = 1.0;
+      if (!pattern) {
+        const char* s3 = e;
+        v = std::strtod(s3, &e);
+        if (e == s3) { rc = set_error(GG_ERR_ARGUMENT, "%s: entry without a value", path); break; }
+      }
+      if (i < 1 || i > m || j < 1 || j > n) {
+        rc = set_error(GG_ERR_ARGUMENT, "%s: entry (%lld, %lld) outside %lldx%lld", path, i, j, m, n);
+        break;
+      }
+      col.push_back(j - 1);
+      row.push_back(i - 1);
+      val.push_back(v);
+      if (expand && (sym || skew || herm) && i != j) {
+        col.push_back(i - 1);
+        row.push_back(j - 1);
+        val.push_back(skew ? -v : v);
+      }
+      ++got;
+    }
+    if (rc != GG_OK) break;
+    if (got < nnz) { rc = set_error(GG_ERR_ARGUMENT, "%s: %lld of %lld entries", path, got, nnz); break; }
+    H->m = m;
+    H->n = n;
+    finish_csc(m, n, col, row, val, &H->ptr, &H->idx, &H->val);
+    *kind_out = (pattern ? 1 : 0) | (integer ? 2 : 0) | (sym ? 4 : 0) | (skew ? 8 : 0) | (herm ? 16 : 0);
+  } while (0);
+  std::fclose(f);
+  return rc;
+}
+
 static int export_matrix(HostMatrix& H, int64_t* m, int64_t* n, int64_t* nnz, int32_t** colptr,
                          int32_t** rowval, double** values) {
   const size_t nz = H.idx.size();
@@ -378,6 +471,17 @@ int gg_read_rb(const char* path, int expand_symmetric, int64_t* m, int64_t* n, i
   HostMatrix H;
   int k = 0;
   GG_CHECK(read_rb(path, expand_symmetric, &H, &k));
+  if (kind) *kind = k;
+  return export_matrix(H, m, n, nnz, colptr, rowval, values);
+}
+
+int gg_read_mtx(const char* path, int expand_symmetric, int64_t* m, int64_t* n, int64_t* nnz,
+                int32_t** colptr, int32_t** rowval, double** values, int* kind) {
+  if (!path || !m || !n || !nnz || !colptr || !rowval || !values)
+    return set_error(GG_ERR_ARGUMENT, "NULL argument");
+  HostMatrix H;
+  int k = 0;
+  GG_CHECK(read_mtx(path, expand_symmetric, &H, &k));
   if (kind) *kind = k;
   return export_matrix(H, m, n, nnz, colptr, rowval, values);
 }

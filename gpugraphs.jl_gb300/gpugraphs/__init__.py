@@ -17,7 +17,7 @@ from .algorithms import (bfs_distances, bfs_distances_, bfs_distances_batch, bfs
 from .errors import (ArgumentError, BoundsError, DimensionMismatch, GPUGraphsError,
                      SpmmAssertionError, UnsupportedError)
 from .ewise import gpu_apply_, gpu_ewise_, gpu_reduce
-from .fileio import RBData, read_edgelist, read_rb
+from .fileio import RBData, read_edgelist, read_mtx, read_rb
 from .ops import gpu_spmm_, gpu_spmspv, gpu_spmspv_, gpu_spmv_, gpu_spmv_rows_, synchronize
 from .storage import (AbstractSparseGPUMatrix, SparseGPUMatrixCSC, SparseGPUMatrixCSR,
                       SparseGPUMatrixSELL, sprand_gpu)
@@ -27,7 +27,7 @@ from .vectors import SparseGPUVector
 __all__ = [
     "AbstractSparseGPUMatrix", "SparseGPUMatrixCSR", "SparseGPUMatrixSELL", "gpu_spmv_",
     "gpu_spmm_", "SparseGPUMatrixCSC", "SparseGPUVector", "gpu_spmspv_", "gpu_spmspv", "gpu_spmv_rows_",
-    "gpu_ewise_", "gpu_apply_", "gpu_reduce", "RBData", "read_rb", "read_edgelist", "sprand_gpu", "autotune", "spmv_layout", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
+    "gpu_ewise_", "gpu_apply_", "gpu_reduce", "RBData", "read_rb", "read_mtx", "read_edgelist", "sprand_gpu", "autotune", "spmv_layout", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
     "bfs_parents_", "shortest_path", "shortest_path_", "monoid_neutral", "monoid_absorb", "synchronize",
     "GPUGraphs_add", "GPUGraphs_safe_add", "GPUGraphs_mul", "GPUGraphs_second",
     "GPUGraphs_band", "GPUGraphs_bor", "GPUGraphs_any", "GPUGraphs_secondi", "GPUGraphs_max",

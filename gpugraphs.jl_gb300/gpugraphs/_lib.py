@@ -37,6 +37,7 @@ SIGNATURES = {
     "gg_spmm": [P, P, I, I, I, P, I, I64, I64, P, I, I64, I64, I64, I, P, I, I64, I64, I64],
     "gg_mat_values_changed": [P, P],
     "gg_read_rb": [ctypes.c_char_p, I, PI64, PI64, PI64, PP, PP, PP, PI],
+    "gg_read_mtx": [ctypes.c_char_p, I, PI64, PI64, PI64, PP, PP, PP, PI],
     "gg_read_edgelist": [ctypes.c_char_p, I, PI64, PI64, PP, PP, PP, PI],
     "gg_host_free": [P],
     "gg_spmv_t": [P, P, I, I, I, P, I, I64, P, I, I64, P, I, I64, I64, I64],

@@ -1,6 +1,6 @@
-"""Graph files: Rutherford-Boeing matrices and edge lists, read by the library on the
-host (gg_read_rb / gg_read_edgelist), as the reference's benchmark loads its inputs
-(benchmark/benchmarks.jl:12-14, 262-266)."""
+"""Graph files: Rutherford-Boeing and Matrix Market matrices and edge lists, read by the
+library on the host (gg_read_rb / gg_read_mtx / gg_read_edgelist), as the reference's
+benchmark loads its inputs (benchmark/benchmarks.jl:12-14, 262-266)."""
 import ctypes
 import os
 
@@ -53,6 +53,22 @@ class RBData:
 def read_rb(path, expand_symmetric=True):
     """The matrix of a Rutherford-Boeing / Harwell-Boeing file as a scipy CSC matrix."""
     return RBData(path, expand_symmetric).data
+
+
+def read_mtx(path, expand_symmetric=True):
+    """The matrix of a Matrix Market coordinate file as a scipy CSC matrix (Float64
+    values, ones for pattern files); symmetric storage expanded unless told not to."""
+    import scipy.sparse as sp
+
+    L = core.lib()
+    m, n, nnz = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    cp, rv, vv = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    kind = ctypes.c_int()
+    check(L.gg_read_mtx(os.fsencode(path), 1 if expand_symmetric else 0, ctypes.byref(m),
+                        ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(cp), ctypes.byref(rv),
+                        ctypes.byref(vv), ctypes.byref(kind)), L)
+    colptr, rowval, values = _take(L, cp, rv, vv, n.value, nnz.value)
+    return sp.csc_matrix((values, rowval - 1, colptr - 1), shape=(m.value, n.value))
 
 
 def read_edgelist(path, base=1):

@@ -25,7 +25,7 @@ export AbstractSparseGPUMatrix, SparseGPUMatrixCSR, SparseGPUMatrixSELL, gpu_spm
        GPUGraphs_mul, GPUGraphs_second, GPUGraphs_band, GPUGraphs_bor, GPUGraphs_any,
        GPUGraphs_secondi, GPUGraphs_max, GPUGraphs_min, SparseGPUVector, SparseGPUMatrixCSC,
        gpu_spmspv!, gpu_spmspv, gpu_spmv_rows!, gpu_ewise!, gpu_apply!, gpu_reduce, read_rb,
-       read_edgelist
+       read_mtx, read_edgelist
 
 # ---------------------------------------------------------------------------------
 # algebra (src/algebra.jl): same functions, plus their operator codes in the C ABI
@@ -498,6 +498,16 @@ function read_rb(path::AbstractString; expand_symmetric::Bool = true)
     m = Ref{Int64}(); n = Ref{Int64}(); nnz = Ref{Int64}(); kind = Ref{Cint}()
     cp = Ref{Ptr{Cvoid}}(); rv = Ref{Ptr{Cvoid}}(); vv = Ref{Ptr{Cvoid}}()
     check(ccall((:gg_read_rb, LIB), Cint,
+                (Cstring, Cint, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}},
+                 Ptr{Ptr{Cvoid}}, Ptr{Cint}), path, Cint(expand_symmetric), m, n, nnz, cp, rv, vv, kind))
+    colptr, rowval, vals = _take_host(cp, rv, vv, n[], nnz[])
+    return SparseMatrixCSC{Float64,Int32}(m[], n[], colptr, rowval, vals)
+end
+
+function read_mtx(path::AbstractString; expand_symmetric::Bool = true)
+    m = Ref{Int64}(); n = Ref{Int64}(); nnz = Ref{Int64}(); kind = Ref{Cint}()
+    cp = Ref{Ptr{Cvoid}}(); rv = Ref{Ptr{Cvoid}}(); vv = Ref{Ptr{Cvoid}}()
+    check(ccall((:gg_read_mtx, LIB), Cint,
                 (Cstring, Cint, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}},
                  Ptr{Ptr{Cvoid}}, Ptr{Cint}), path, Cint(expand_symmetric), m, n, nnz, cp, rv, vv, kind))
     colptr, rowval, vals = _take_host(cp, rv, vv, n[], nnz[])

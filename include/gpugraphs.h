@@ -301,6 +301,15 @@ int gg_read_rb(const char* path, int expand_symmetric, int64_t* m, int64_t* n, i
                int32_t** colptr, int32_t** rowval, double** values, int* kind);
 
 /*
+ * Reads a Matrix Market coordinate file (real / integer / pattern; general / symmetric /
+ * skew-symmetric / Hermitian), the other format SuiteSparse matrices are published in.
+ * Same result, ownership, expansion and kind flags as gg_read_rb; GG_ERR_UNSUPPORTED for
+ * array (dense) or complex files.
+ */
+int gg_read_mtx(const char* path, int expand_symmetric, int64_t* m, int64_t* n, int64_t* nnz,
+                int32_t** colptr, int32_t** rowval, double** values, int* kind);
+
+/*
  * Reads an edge list (GraphIO.EdgeList, benchmark/benchmarks.jl:12-14): one edge
  * "u v [w]" per line (spaces, tabs or commas), '#' / '%' comment lines, vertex ids
  * starting at `base` (0 or 1).  Returns the adjacency A (A[u, v] for the edge u -> v)

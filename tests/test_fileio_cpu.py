@@ -123,3 +123,49 @@ def test_edgelist_to_transposed_adjacency(tmp_path):
     (tmp_path / "x.txt").write_text("1 x\n")
     with pytest.raises(G.ArgumentError):
         fileio.read_edgelist(str(tmp_path / "x.txt"))
+
+
+def test_mtx_matches_scipy_writer(tmp_path):
+    rng = np.random.default_rng(7)
+    A = sp.random(40, 33, density=0.1, format="coo", random_state=rng)
+    A.data = A.data * 100 - 30
+    path = tmp_path / "a.mtx"
+    scipy.io.mmwrite(str(path), A, precision=17)
+    B = fileio.read_mtx(str(path))
+    assert B.shape == A.shape
+    assert np.array_equal(B.toarray(), A.toarray())
+    # symmetric integer storage: the lower triangle written, both read back
+    S = sp.random(25, 25, density=0.2, format="csr", random_state=rng)
+    S = (S + S.T).tocoo()
+    S.data = np.round(S.data * 10) + 1
+    p2 = tmp_path / "s.mtx"
+    scipy.io.mmwrite(str(p2), S.astype(np.int64), symmetry="symmetric")
+    D = fileio.read_mtx(str(p2)).toarray()
+    assert np.array_equal(D, S.toarray())
+    tri = fileio.read_mtx(str(p2), expand_symmetric=False).toarray()
+    assert np.array_equal(tri, np.tril(S.toarray()))
+
+
+def test_mtx_pattern_skew_and_errors(tmp_path):
+    txt = ("%%MatrixMarket matrix coordinate pattern general\n"
+           "% comment\n"
+           "3 4 3\n"
+           "1 2\n3 4\n2 1\n")
+    (tmp_path / "p.mtx").write_text(txt)
+    D = fileio.read_mtx(str(tmp_path / "p.mtx")).toarray()
+    want = np.zeros((3, 4)); want[0, 1] = want[2, 3] = want[1, 0] = 1
+    assert np.array_equal(D, want)
+    skew = ("%%MatrixMarket matrix coordinate real skew-symmetric\n"
+            "3 3 2\n2 1 1.5\n3 1 -4e-1\n")
+    (tmp_path / "z.mtx").write_text(skew)
+    Z = fileio.read_mtx(str(tmp_path / "z.mtx")).toarray()
+    assert np.array_equal(Z, np.array([[0, -1.5, 0.4], [1.5, 0, 0], [-0.4, 0, 0]]))
+    (tmp_path / "d.mtx").write_text("%%MatrixMarket matrix array real general\n2 2\n1\n2\n3\n4\n")
+    with pytest.raises(G.UnsupportedError):
+        fileio.read_mtx(str(tmp_path / "d.mtx"))
+    (tmp_path / "b.mtx").write_text("%%MatrixMarket matrix coordinate real general\n2 2 1\n3 1 1.0\n")
+    with pytest.raises(G.ArgumentError):
+        fileio.read_mtx(str(tmp_path / "b.mtx"))
+    (tmp_path / "t.mtx").write_text("%%MatrixMarket matrix coordinate real general\n2 2 2\n1 1 1.0\n")
+    with pytest.raises(G.ArgumentError):
+        fileio.read_mtx(str(tmp_path / "t.mtx"))
