@@ -219,7 +219,8 @@ int gg_spmm(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* C, 
  * with the absorb early exit of src/spmv/CSR.jl:31-54; other rows of the dense y are
  * not written.  y_ind (device, capacity m, may be NULL) receives the 1-based rows
  * written, ascending; *y_nnz (may be NULL) their count.  The first call builds a column
- * index of A (kept on the handle).  Errors: GG_ERR_DIMENSION as gpu_spmspv! (n != x_len,
+ * index of A and its workspace, kept on the handle: 4(n+1) + 12 nnz bytes for the index
+ * and the long-row products, about 12n + 13m bytes of bitmaps, staging and lists.  Errors: GG_ERR_DIMENSION as gpu_spmspv! (n != x_len,
  * m != y_len), GG_ERR_TYPE / GG_ERR_UNSUPPORTED as gg_spmv, GG_ERR_ARGUMENT for indices
  * that are not increasing or outside 1:n (nothing written), GG_ERR_UNSUPPORTED for a
  * SELL handle.  Synchronous.
