@@ -122,6 +122,23 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(value, device=None):
+    """The largest of a per-rank float over the process group (timings: the job is as
+    slow as its slowest rank); the value itself without a group of more than one rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_gbs(ws, bytes_per_rank, ms):
+    """Whole-job GB/s: every rank moved bytes_per_rank in ms (the max over ranks)."""
+    return ws * bytes_per_rank / (ms * 1e-3) / 1e9
+
+
 def spmv_bytes(n, nnz):
     return 4 * (n + 1) + 8 * nnz + 4 * n + 4 * n
 
@@ -339,13 +356,10 @@ def run_spmv_rmat(args, scale=22):
             step()
         torch.cuda.synchronize()
     clocks = clk.stop()
-    if ws > 1:
-        t = torch.tensor([ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, device)
     per_step_ms = ms / args.steps
     B = spmv_bytes(n, nnz)
-    value = ws * B / (per_step_ms * 1e-3) / 1e9
+    value = aggregate_gbs(ws, B, per_step_ms)
 
     # roofline of the dominant kernel: the same K steps again under the library's
     # launch tracer, which brackets the matrix-streaming kernel of every call with
@@ -403,10 +417,7 @@ def run_spmv_rmat(args, scale=22):
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.steps
     assert bool(torch.equal(yd[(args.steps - 1) & 1].cpu(), yh[(args.steps - 1) & 1]))
-    e2e_t = torch.tensor([e2e_ms], device=device)
-    if ws > 1:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_val = ws * B / (float(e2e_t.item()) * 1e-3) / 1e9
+    e2e_val = aggregate_gbs(ws, B, max_over_ranks(e2e_ms, device))
 
     ok = spot_check(A, x, y)
     layout = G.spmv_layout(A)
