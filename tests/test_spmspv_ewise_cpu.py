@@ -161,3 +161,46 @@ def test_reduce_exact_monoids_and_float_sum():
     assert O.reduce(O.LOR, xb)[1] and not O.reduce(O.LAND, xb)[1]
     assert O.reduce(O.BOR, xb)[0] == 0
     assert O.reduce(O.ADD, xb)[0] == O.UNSUPPORTED
+
+
+def _reduce_order_py(x):
+    """The library's reduction order restated with numpy Float32 scalars: chunks of 8192,
+    thread t of 256 folds t, t+256, ... left to right, xor butterflies over each warp's 32
+    lanes (lane l takes v[l] + v[l ^ o]) and over the 8 warp totals, chunk totals again."""
+    vals = [np.float32(v) for v in x]
+    while len(vals) > 1 or not vals:
+        if not vals:
+            return np.float32(0)
+        out = []
+        for c0 in range(0, len(vals), 8192):
+            th = []
+            for t in range(256):
+                acc = np.float32(0)
+                for u in range(32):
+                    i = c0 + t + 256 * u
+                    if i < len(vals):
+                        acc = np.float32(acc + vals[i])
+                th.append(acc)
+            tot = []
+            for w in range(8):
+                v = th[32 * w:32 * w + 32]
+                for o in (16, 8, 4, 2, 1):
+                    v = [np.float32(v[l] + v[l ^ o]) for l in range(32)]
+                tot.append(v[0])
+            v = tot + [np.float32(0)] * 24
+            for o in (16, 8, 4, 2, 1):
+                v = [np.float32(v[l] + v[l ^ o]) for l in range(32)]
+            out.append(v[0])
+        vals = out
+        if len(vals) == 1:
+            break
+    return vals[0]
+
+
+def test_reduce_order_pinned_by_an_independent_restatement():
+    rng = np.random.default_rng(21)
+    for n in (1, 255, 8192, 8193, 20000):
+        x = (rng.random(n) * 2 - 0.5).astype(np.float32)
+        rc, got = O.reduce(O.ADD, x)
+        assert rc == 0
+        assert np.float32(got).tobytes() == _reduce_order_py(x).tobytes(), n
