@@ -90,3 +90,28 @@ def test_operator_scalars_match_algebra():
     assert G.monoid_absorb(np.float32, G.GPUGraphs_any) is None
     with pytest.raises(G.ArgumentError):
         G.monoid_neutral(np.float32, G.GPUGraphs_lor)
+
+
+def test_null_handles_are_argument_errors(libpath):
+    """Every entry point checks its handles before touching a device: NULL context or
+    matrix returns GG_ERR_ARGUMENT with a message (no GPU needed, no crash)."""
+    from gpugraphs import _lib
+    L = _lib.load()
+    ARG = header_enums()["GG_ERR_ARGUMENT"]
+    n64 = ctypes.c_int64(0)
+    cases = [
+        L.gg_spmv(None, None, 9, 5, 2, None, 4, 0, None, 4, 0, None, 0, 0, 0, 0),
+        L.gg_spmv_t(None, None, 9, 5, 2, None, 4, 0, None, 4, 0, None, 0, 0, 0, 0),
+        L.gg_spmspv(None, None, 9, 5, 2, None, 4, 0, None, None, 4, 0, 0, None, ctypes.byref(n64)),
+        L.gg_spmv_rows(None, None, 9, 5, 2, None, 4, 0, None, 4, 0, None, 0),
+        L.gg_ewise(None, 5, None, 4, None, 4, None, 4, 0, None, 0),
+        L.gg_apply(None, 5, None, 4, None, 4, None, 4, 0, 0, None, 0),
+        L.gg_reduce(None, 5, None, 4, 0, None),
+        L.gg_read_rb(None, 1, None, None, None, None, None, None, None),
+        L.gg_read_mtx(None, 1, None, None, None, None, None, None, None),
+        L.gg_read_edgelist(None, 1, None, None, None, None, None, None),
+        L.gg_mat_values_changed(None, None),
+    ]
+    for rc in cases:
+        assert rc == ARG
+        assert L.gg_last_error()
