@@ -43,10 +43,55 @@ template <typename T>
 __device__ __forceinline__ T shfl_xor_m(unsigned mask, T v, int off, int width) {
   return __shfl_xor_sync(mask, v, off, width);
 }
+template <typename T>
+__device__ __forceinline__ T shfl_idx_m(unsigned mask, T v, int src) {
+  return __shfl_sync(mask, v, src);
+}
+template <>
+__device__ __forceinline__ uint8_t shfl_idx_m<uint8_t>(unsigned mask, uint8_t v, int src) {
+  return static_cast<uint8_t>(__shfl_sync(mask, static_cast<int>(v), src));
+}
 template <>
 __device__ __forceinline__ uint8_t shfl_xor_m<uint8_t>(unsigned mask, uint8_t v, int off,
                                                        int width) {
   return static_cast<uint8_t>(__shfl_xor_sync(mask, static_cast<int>(v), off, width));
+}
+
+// ---------------------------------------------------------------------------------
+// storage-order refold with the reference's early exit (csr_spmv_kernel!,
+// src/spmv/CSR.jl:47-52) for rows reduced in parallel
+//
+// A parallel (tree-ordered) fold of a floating-point row differs from the sequential
+// fold with its stop at the absorbing value only through NaN: a NaN or -Inf term
+// after the sum reached +Inf (GPUGraphs_add), or a NaN after -Inf / +Inf (min /
+// max).  Without the stop those give NaN; any other non-finite or finite result is
+// the same.  So a row whose parallel result is NaN is folded again, by the whole
+// warp: lanes compute 32 products at once (coalesced loads) and the sum is taken in
+// storage order through shuffles, stopping where the reference stops.  Integer and
+// Bool accumulators never compare unequal to themselves, so they skip this.
+// ---------------------------------------------------------------------------------
+template <class SR>
+__device__ __forceinline__ typename SR::T warp_refold_row(const SR& sr, const int32_t* __restrict__ rowptr,
+                                                          const int32_t* __restrict__ colval,
+                                                          int64_t row0, int lane) {
+  typedef typename SR::T T;
+  const int32_t kb = __ldg(rowptr + row0) - 1, ke = __ldg(rowptr + row0 + 1) - 1;
+  T acc = sr.neutral();
+  bool done = false;
+  for (int32_t base = kb; base < ke && !done; base += 32) {
+    const int32_t k = base + lane;
+    T p = sr.neutral();
+    if (k < ke) p = sr.mulk(k, __ldg(colval + k), row0 + 1);
+    const int cnt = ke - base < 32 ? ke - base : 32;
+    for (int j = 0; j < cnt; ++j) {
+      acc = sr.addv(acc, shfl_idx_m<T>(kFull, p, j));
+      if (sr.is_absorb(acc)) {
+        done = true;
+        break;
+      }
+    }
+  }
+  return acc;
 }
 
 // ---------------------------------------------------------------------------------
@@ -140,6 +185,7 @@ __global__ void __launch_bounds__(kRBWarps * 32)
       for (int off = 16; off > 0; off >>= 1) acc = sr.addv(acc, shfl_xor_m<T>(kFull, acc, off, 32));
       const int32_t f0 = long_first_seg[sg.w], f1 = long_first_seg[sg.w + 1];
       if (f1 - f0 == 1) {  // the whole row in one segment
+        if (acc != acc) acc = warp_refold_row(sr, rowptr, colval, row, lane);
         if (lane == 0) sr.write(row, acc);
         continue;
       }
@@ -152,12 +198,14 @@ __global__ void __launch_bounds__(kRBWarps * 32)
       prev = __shfl_sync(kFull, prev, 0);
       if (prev == (unsigned)(f1 - f0 - 1)) {  // this warp completed the row
         __threadfence();
+        T tot = sr.neutral();
         if (lane == 0) {
-          T tot = sr.neutral();
           for (int32_t q = f0; q < f1; ++q) tot = sr.addv(tot, __ldcg(partials + q));
-          sr.write(long_rows[sg.w], tot);
           long_count[sg.w] = 0;  // ready for the next launch
         }
+        tot = shfl_idx_m<T>(kFull, tot, 0);
+        if (tot != tot) tot = warp_refold_row(sr, rowptr, colval, row, lane);
+        if (lane == 0) sr.write(row, tot);
       }
     }
   }
@@ -314,6 +362,7 @@ __global__ void __launch_bounds__(kPipeWarps * 32)
     for (int off = 16; off > 0; off >>= 1) acc = sr.addv(acc, shfl_xor_m<T>(kFull, acc, off, 32));
     const int32_t f0 = long_first_seg[sg.w], f1 = long_first_seg[sg.w + 1];
     if (f1 - f0 == 1) {  // the whole row in one segment
+      if (acc != acc) acc = warp_refold_row(sr, rowptr, colval, row, lane);
       if (lane == 0) sr.write(row, acc);
       continue;
     }
@@ -326,12 +375,14 @@ __global__ void __launch_bounds__(kPipeWarps * 32)
     prev = __shfl_sync(kFull, prev, 0);
     if (prev == (unsigned)(f1 - f0 - 1)) {
       __threadfence();
+      T tot = sr.neutral();
       if (lane == 0) {
-        T tot = sr.neutral();
         for (int32_t q = f0; q < f1; ++q) tot = sr.addv(tot, __ldcg(partials + q));
-        sr.write(long_rows[sg.w], tot);
         long_count[sg.w] = 0;
       }
+      tot = __shfl_sync(kFull, tot, 0);
+      if (tot != tot) tot = warp_refold_row(sr, rowptr, colval, row, lane);
+      if (lane == 0) sr.write(row, tot);
     }
   }
 }
@@ -1141,6 +1192,48 @@ int launch_pipe_f32(gg_ctx* ctx, gg_mat* A, const float* nz, const float* x, flo
   return GG_OK;
 }
 
+// ---------------------------------------------------------------------------------
+// A CSR handle whose plus-times product ran on its SELL-32 copy or its column-window
+// tiles: those kernels fold without the stop at +Inf (the SELL reference kernel has
+// none), so every row whose result is NaN is folded again over the handle's own CSR
+// in storage order with the stop (csr_spmv_kernel!, src/spmv/CSR.jl:47-52).  One warp
+// per 32 rows reads their results (one coalesced load) and refolds its NaN rows
+// together (warp_refold_row).  Inputs without NaN / -Inf cost one read of y.
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_refold_nan_rows(SRPlusTimesF32 sr, const int32_t* __restrict__ rowptr,
+                      const int32_t* __restrict__ colval, int64_t m) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < m; w += nw) {
+    const int64_t r = w * 32 + lane;
+    const float v = r < m ? __ldcs(sr.y + r) : 0.0f;
+    unsigned bad = __ballot_sync(kFull, v != v);
+    while (bad) {
+      const int b = __ffs(bad) - 1;
+      bad &= bad - 1;
+      const int64_t row = w * 32 + b;
+      const float acc = warp_refold_row(sr, rowptr, colval, row, lane);
+      if (lane == 0) sr.y[row] = acc;
+    }
+  }
+}
+
+static int launch_refold_nan_rows(gg_ctx* ctx, const gg_mat* A, const float* x, float* y) {
+  SRPlusTimesF32 sr;
+  sr.nz = static_cast<const float*>(A->nzval);
+  sr.x = x;
+  sr.y = y;
+  const int64_t warps = (A->m + 31) / 32;
+  int64_t grid = (warps + 7) / 8;
+  const int64_t cap = (int64_t)ctx->num_sms * 8;
+  if (grid > cap) grid = cap;
+  k_refold_nan_rows<<<(int)grid, 256, 0, ctx->stream>>>(sr, A->rowptr, A->colval, A->m);
+  trace_count(ctx, 1);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
 // dispatch of gg_spmv after validation (gg_api.cu); tc = accumulator type
 int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, void* y, int ty,
                   const void* x, int tx, const void* mask, int tmask, int64_t lo, int64_t hi) {
@@ -1158,7 +1251,8 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
       GG_CHECK(build_win_plan(ctx, A));
       if (A->winplan->enabled) {
         A->last_layout = 3;
-        return launch_spmv_win(ctx, A, sr.x, sr.y);
+        GG_CHECK(launch_spmv_win(ctx, A, sr.x, sr.y));
+        return launch_refold_nan_rows(ctx, A, sr.x, sr.y);
       }
     }
     const bool use_copy = A->tuned_spmv == 2 || ((A->tuned_spmv == 0 || A->tuned_spmv == 3) &&
@@ -1173,7 +1267,9 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
         A->sell_copy->hot_cols = A->hot_cols;
       }
       A->last_layout = 2;
-      return spmv_dispatch(ctx, A->sell_copy, tc, mul, add, accum, y, ty, x, tx, mask, tmask, lo, hi);
+      GG_CHECK(spmv_dispatch(ctx, A->sell_copy, tc, mul, add, accum, y, ty, x, tx, mask, tmask,
+                             lo, hi));
+      return launch_refold_nan_rows(ctx, A, sr.x, sr.y);
     }
     GG_CHECK(build_colperm(ctx, A));
     const int32_t* colval = A->colval;

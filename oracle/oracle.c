@@ -711,6 +711,315 @@ int64_t orc_sssp(int64_t n, const int32_t* rowptr, const int32_t* colval, const 
 }
 
 /* ------------------------------------------------------------------------------ */
+/* Cross-checks for full-size graphs.  The restatements above follow the           */
+/* reference's level-synchronous BFS and Jacobi Bellman-Ford loops, which cost      */
+/* O(levels x nnz) and O(rounds x nnz) -- hours on a 4096 x 4096 grid.  The         */
+/* functions below reach the same results by other algorithms (frontier BFS,        */
+/* Dijkstra) in O(nnz) / O(nnz log n); tests/test_oracle_cpu.py checks them against */
+/* the restatements on graphs of every kind the tests use.                          */
+/* ------------------------------------------------------------------------------ */
+
+/* Out-edges of A_T (row v of A_T lists the in-neighbours u of v): for every column
+   u the rows v of its entries, with the entry's value widened to the distance type
+   when weights != 0.  pattern = 1 takes every stored entry, 0 only those with an
+   odd (true) stored value, the edges bfs_distances! follows (edge_odd).  Rows of one
+   column come in no particular order.  sym = 1 (with pattern = 1) states that A_T is
+   symmetric with mirrored values: its rows are then its own out-edge lists. */
+typedef struct {
+  int64_t* ptr;  /* n + 1 */
+  int32_t* row;  /* 0-based v */
+  int32_t* wi;   /* integer weights (or NULL) */
+  float* wf;     /* Float32 weights (or NULL) */
+} outedges;
+
+static void outedges_free(outedges* T) {
+  free(T->ptr);
+  free(T->row);
+  free(T->wi);
+  free(T->wf);
+}
+
+static int outedges_build(int64_t n, const int32_t* rowptr, const int32_t* colval,
+                          const void* nzval, int tv, int pattern, int weights, int sym,
+                          outedges* T) {
+  memset(T, 0, sizeof(*T));
+  int64_t nnz = rowptr[n] - 1;
+  if (sym && pattern) {
+    /* A_T == A (the caller says so): row u of A_T lists the out-neighbours of u */
+    T->ptr = (int64_t*)malloc(((size_t)n + 1) * sizeof(int64_t));
+    T->row = (int32_t*)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(int32_t));
+    if (weights && tv == T_F32) T->wf = (float*)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(float));
+    if (weights && tv != T_F32) T->wi = (int32_t*)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(int32_t));
+    if (!T->ptr || !T->row || (weights && !T->wf && !T->wi)) { outedges_free(T); return ORC_ARG; }
+    for (int64_t u = 0; u <= n; ++u) T->ptr[u] = rowptr[u] - 1;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < nnz; ++i) {
+      T->row[i] = colval[i] - 1;
+      if (T->wf) T->wf[i] = ((const float*)nzval)[i];
+      if (T->wi) T->wi[i] = (int32_t)load(nzval, tv, i).i;
+    }
+    return ORC_OK;
+  }
+  T->ptr = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
+  int64_t* fill = (int64_t*)malloc(((size_t)n + 1) * sizeof(int64_t));
+  if (!T->ptr || !fill) { free(fill); outedges_free(T); return ORC_ARG; }
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t v = 0; v < n; ++v)
+    for (int64_t i = rowptr[v] - 1; i < rowptr[v + 1] - 1; ++i)
+      if (pattern || edge_odd(nzval, tv, i)) __atomic_fetch_add(&T->ptr[colval[i]], 1, __ATOMIC_RELAXED);
+  for (int64_t u = 0; u < n; ++u) T->ptr[u + 1] += T->ptr[u];
+  int64_t ne = T->ptr[n];
+  memcpy(fill, T->ptr, ((size_t)n + 1) * sizeof(int64_t));
+  T->row = (int32_t*)malloc((size_t)(ne > 0 ? ne : 1) * sizeof(int32_t));
+  if (weights && tv == T_F32) T->wf = (float*)malloc((size_t)(ne > 0 ? ne : 1) * sizeof(float));
+  if (weights && tv != T_F32) T->wi = (int32_t*)malloc((size_t)(ne > 0 ? ne : 1) * sizeof(int32_t));
+  if (!T->row || (weights && !T->wf && !T->wi)) { free(fill); outedges_free(T); return ORC_ARG; }
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t v = 0; v < n; ++v)
+    for (int64_t i = rowptr[v] - 1; i < rowptr[v + 1] - 1; ++i) {
+      if (!pattern && !edge_odd(nzval, tv, i)) continue;
+      int64_t at = __atomic_fetch_add(&fill[colval[i] - 1], 1, __ATOMIC_RELAXED);
+      T->row[at] = (int32_t)v;
+      if (T->wf) T->wf[at] = ((const float*)nzval)[i];
+      if (T->wi) T->wi[at] = (int32_t)load(nzval, tv, i).i;
+    }
+  free(fill);
+  (void)nnz;
+  return ORC_OK;
+}
+
+/* Hop distances from the source along out-edges, one frontier at a time; a vertex
+   is claimed by the first thread that moves its distance off typemax (every
+   claimant writes the same level).  Equals bfs_distances(A_T, source) of
+   src/algorithms/bfs.jl:1-73: a row joins level L exactly when an in-neighbour of
+   level L-1 reaches it over an active entry. */
+static int64_t frontier_bfs(int64_t n, const outedges* T, int64_t source, int32_t* dist) {
+  int32_t* F = (int32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int32_t));
+  int32_t* N = (int32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int32_t));
+  if (!F || !N) { free(F); free(N); return -1; }
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < n; ++v) dist[v] = INT32_MAX;
+  dist[source - 1] = 0;
+  F[0] = (int32_t)(source - 1);
+  int64_t nf = 1, level = 0;
+  while (nf > 0) {
+    int64_t nn = 0;
+    const int32_t L = (int32_t)level + 1;
+#pragma omp parallel
+    {
+      int32_t buf[256];
+      int nb = 0;
+#pragma omp for schedule(dynamic, 64)
+      for (int64_t i = 0; i < nf; ++i) {
+        const int32_t u = F[i];
+        for (int64_t e = T->ptr[u]; e < T->ptr[u + 1]; ++e) {
+          int32_t v = T->row[e];
+          int32_t expect = INT32_MAX;
+          if (__atomic_load_n(&dist[v], __ATOMIC_RELAXED) == INT32_MAX &&
+              __atomic_compare_exchange_n(&dist[v], &expect, L, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+            buf[nb++] = v;
+            if (nb == 256) {
+              int64_t at = __atomic_fetch_add(&nn, nb, __ATOMIC_RELAXED);
+              memcpy(N + at, buf, (size_t)nb * sizeof(int32_t));
+              nb = 0;
+            }
+          }
+        }
+      }
+      if (nb > 0) {
+        int64_t at = __atomic_fetch_add(&nn, nb, __ATOMIC_RELAXED);
+        memcpy(N + at, buf, (size_t)nb * sizeof(int32_t));
+      }
+    }
+    int32_t* t = F;
+    F = N;
+    N = t;
+    nf = nn;
+    if (nf > 0) ++level;
+  }
+  free(F);
+  free(N);
+  return level;
+}
+
+/* bfs_distances(A_T, source) by frontier BFS; returns the largest level, or -1. */
+int64_t orc_bfs_levels_fast(int64_t n, const int32_t* rowptr, const int32_t* colval,
+                            const void* nzval, int tv, int64_t source, int32_t* dist, int sym) {
+  outedges T;
+  if (outedges_build(n, rowptr, colval, nzval, tv, nzval == NULL, 0, sym, &T) != ORC_OK) return -1;
+  int64_t lv = frontier_bfs(n, &T, source, dist);
+  outedges_free(&T);
+  return lv;
+}
+
+/* bfs_parents(A_T, source) of src/algorithms/bfs.jl:113-183 from the pattern's hop
+   distances: the frontier of the level that reaches row v is every vertex at
+   distance dist[v] - 1, so v's parent is its first (rule 1, CSR) or largest (rule 2,
+   SELL) in-neighbour column at that distance.  dist: hop distances over every
+   stored entry (bfs_parents ignores stored values). */
+void orc_bfs_parents_from_levels(int64_t n, const int32_t* rowptr, const int32_t* colval,
+                                 const int32_t* dist, int64_t source, int rule,
+                                 int32_t* parents) {
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t v = 0; v < n; ++v) {
+    if (v == source - 1) { parents[v] = 0; continue; }
+    if (dist[v] == INT32_MAX) { parents[v] = INT32_MAX; continue; }
+    const int32_t want = dist[v] - 1;
+    int32_t p = 0;
+    for (int64_t i = rowptr[v] - 1; i < rowptr[v + 1] - 1; ++i) {
+      int32_t c = colval[i];
+      if (dist[c - 1] == want) {
+        if (rule == 1) { p = c; break; }
+        if (c > p) p = c;
+      }
+    }
+    parents[v] = p;
+  }
+}
+
+/* Hop distances of S sources over every stored entry -- shortest_path(A_T,
+   sources) with a Bool A_T (src/algorithms/shortest_path.jl:88-161) -- kept for the
+   listed rows only: out[r + q * nrows] = distance of rows[r] (0-based) from source
+   q (1-based sources[q]).  Sources run in parallel, a serial queue BFS each. */
+int orc_bfs_levels_multi(int64_t n, const int32_t* rowptr, const int32_t* colval,
+                         const int64_t* sources, int64_t S, const int64_t* rows,
+                         int64_t nrows, int32_t* out, int sym) {
+  outedges T;
+  if (outedges_build(n, rowptr, colval, NULL, T_BOOL, 1, 0, sym, &T) != ORC_OK) return ORC_ARG;
+  int fail = 0;
+#pragma omp parallel reduction(| : fail)
+  {
+    int32_t* dist = (int32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int32_t));
+    int32_t* Q = (int32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int32_t));
+    if (!dist || !Q) fail = 1;
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t q = 0; q < S; ++q) {
+      if (!dist || !Q) continue;
+      for (int64_t v = 0; v < n; ++v) dist[v] = INT32_MAX;
+      int64_t head = 0, tail = 0;
+      dist[sources[q] - 1] = 0;
+      Q[tail++] = (int32_t)(sources[q] - 1);
+      while (head < tail) {
+        int32_t u = Q[head++];
+        int32_t du = dist[u] + 1;
+        for (int64_t e = T.ptr[u]; e < T.ptr[u + 1]; ++e) {
+          int32_t v = T.row[e];
+          if (dist[v] == INT32_MAX) { dist[v] = du; Q[tail++] = v; }
+        }
+      }
+      for (int64_t r = 0; r < nrows; ++r) out[r + q * nrows] = dist[rows[r]];
+    }
+    free(dist);
+    free(Q);
+  }
+  outedges_free(&T);
+  return fail ? ORC_ARG : ORC_OK;
+}
+
+/* binary min-heap of (key << 32 | vertex); keys are the distance's order-preserving
+   32-bit pattern (non-negative Int32, or the bits of a non-negative Float32) */
+typedef struct { uint64_t* a; int64_t n, cap; } heap64;
+static int heap_push(heap64* h, uint64_t x) {
+  if (h->n == h->cap) {
+    int64_t nc = h->cap ? h->cap * 2 : 1024;
+    uint64_t* na = (uint64_t*)realloc(h->a, (size_t)nc * sizeof(uint64_t));
+    if (!na) return 0;
+    h->a = na;
+    h->cap = nc;
+  }
+  int64_t i = h->n++;
+  while (i > 0) {
+    int64_t p = (i - 1) >> 1;
+    if (h->a[p] <= x) break;
+    h->a[i] = h->a[p];
+    i = p;
+  }
+  h->a[i] = x;
+  return 1;
+}
+static uint64_t heap_pop(heap64* h) {
+  uint64_t top = h->a[0], x = h->a[--h->n];
+  int64_t i = 0;
+  for (;;) {
+    int64_t c = 2 * i + 1;
+    if (c >= h->n) break;
+    if (c + 1 < h->n && h->a[c + 1] < h->a[c]) ++c;
+    if (x <= h->a[c]) break;
+    h->a[i] = h->a[c];
+    i = c;
+  }
+  if (h->n > 0) h->a[i] = x;
+  return top;
+}
+
+/*
+ * shortest_path(A_T, source) of src/algorithms/shortest_path.jl:12-83 by Dijkstra.
+ * The Jacobi rounds reach, for every row, the minimum over paths from the source of
+ * the left fold safe_add(w_k, ... safe_add(w_1, 0)) in the distance type (Int32 for
+ * Bool / Int32 values, Float32 for Float32 values, shortest_path.jl:18).  For
+ * non-negative weights each step x -> fl(w + x) is non-decreasing in x and never
+ * below x, so settling vertices in order of distance reaches the same minimum bit
+ * for bit (Float32 included).  Negative or NaN weights return ORC_ARG, as do Int32
+ * lengths beyond typemax (the reference would wrap).
+ */
+int orc_sssp_dijkstra(int64_t n, const int32_t* rowptr, const int32_t* colval,
+                      const void* nzval, int tv, int64_t source, void* dist, int sym) {
+  if (tv != T_BOOL && tv != T_I32 && tv != T_F32) return ORC_TYPE;
+  const int64_t nnz = rowptr[n] - 1;
+  for (int64_t i = 0; i < nnz; ++i) {
+    if (tv == T_F32) {
+      float w = ((const float*)nzval)[i];
+      if (!(w >= 0.0f)) return ORC_ARG;
+    } else if (tv == T_I32 && ((const int32_t*)nzval)[i] < 0) {
+      return ORC_ARG;
+    }
+  }
+  outedges T;
+  if (outedges_build(n, rowptr, colval, nzval, tv, 1, 1, sym, &T) != ORC_OK) return ORC_ARG;
+  float* df = tv == T_F32 ? (float*)dist : NULL;
+  int32_t* di = tv == T_F32 ? NULL : (int32_t*)dist;
+  for (int64_t v = 0; v < n; ++v) {
+    if (df) df[v] = INFINITY;
+    else di[v] = INT32_MAX;
+  }
+  heap64 h = {NULL, 0, 0};
+  int rc = ORC_OK;
+  if (df) df[source - 1] = 0.0f;
+  else di[source - 1] = 0;
+  if (!heap_push(&h, (uint64_t)(source - 1))) rc = ORC_ARG;
+  while (rc == ORC_OK && h.n > 0) {
+    uint64_t top = heap_pop(&h);
+    const int32_t u = (int32_t)(top & 0xffffffffu);
+    const uint32_t key = (uint32_t)(top >> 32);
+    uint32_t cur;
+    if (df) memcpy(&cur, &df[u], 4);
+    else cur = (uint32_t)di[u];
+    if (key != cur) continue; /* stale entry */
+    for (int64_t e = T.ptr[u]; e < T.ptr[u + 1]; ++e) {
+      const int32_t v = T.row[e];
+      uint32_t nk;
+      if (df) {
+        volatile float s = T.wf[e] + df[u]; /* safe_add: +Inf stays +Inf */
+        float nd = s;
+        if (!(nd < df[v])) continue;
+        df[v] = nd;
+        memcpy(&nk, &nd, 4);
+      } else {
+        int64_t nd = (int64_t)T.wi[e] + (int64_t)di[u];
+        if (nd >= INT32_MAX) { rc = ORC_ARG; break; }
+        if (nd >= di[v]) continue;
+        di[v] = (int32_t)nd;
+        nk = (uint32_t)nd;
+      }
+      if (!heap_push(&h, ((uint64_t)nk << 32) | (uint32_t)v)) { rc = ORC_ARG; break; }
+    }
+  }
+  free(h.a);
+  outedges_free(&T);
+  return rc;
+}
+
+/* ------------------------------------------------------------------------------ */
 /* Fast typed paths timed as the CPU baseline (same algorithms, no interpreter).     */
 /* ------------------------------------------------------------------------------ */
 

@@ -60,14 +60,20 @@ def lib():
             "orc_ewise": [I32, P, I32, P, I32, P, I32, I64, P, I32],
             "orc_apply": [I32, P, I32, P, I32, P, I32, I32, I64, P, I32],
             "orc_reduce": [I32, P, I32, I64, P],
+            "orc_bfs_levels_fast": [I64, P, P, P, I32, I64, P, I32],
+            "orc_bfs_parents_from_levels": [I64, P, P, P, I64, I32, P],
+            "orc_bfs_levels_multi": [I64, P, P, P, I64, P, I64, P, I32],
+            "orc_sssp_dijkstra": [I64, P, P, P, I32, I64, P, I32],
             "orc_num_threads": [],
             "orc_set_num_threads": [I32],
         }
         for name, args in sig.items():
             f = getattr(L, name)
             f.argtypes = args
-            f.restype = I64 if name in ("orc_bfs_levels", "orc_bfs_parents", "orc_sssp") else I32
+            f.restype = I64 if name in ("orc_bfs_levels", "orc_bfs_parents", "orc_sssp",
+                                        "orc_bfs_levels_fast") else I32
         L.orc_set_num_threads.restype = None
+        L.orc_bfs_parents_from_levels.restype = None
         L.orc_csr_spmv_plus_times_f32.restype = None
         L.orc_csr_spmv_plus_times_f32_rows.restype = None
         for g in ("orc_gen_rmat", "orc_gen_er", "orc_gen_grid", "orc_gen_uniform_f32"):
@@ -195,6 +201,61 @@ def bfs_parents(n, rowptr, colval, source, rule):
     par = np.empty(n, np.int32)
     lv = lib().orc_bfs_parents(n, _p(rowptr), _p(colval), source, rule, _p(par))
     return par, lv
+
+
+def bfs_levels_fast(n, rowptr, colval, nzval, source, symmetric=False):
+    """bfs_distances(A_T, source) by frontier BFS (O(nnz); the same levels as
+    bfs_levels).  nzval None = every stored entry is an edge; symmetric=True states
+    A_T == A (no transpose is built).  Returns (dist, largest level)."""
+    rowptr, colval = _c(rowptr, np.int32), _c(colval, np.int32)
+    nzval = None if nzval is None else _c(nzval)
+    dist = np.empty(n, np.int32)
+    lv = lib().orc_bfs_levels_fast(n, _p(rowptr), _p(colval), _p(nzval),
+                                   0 if nzval is None else tcode(nzval), source, _p(dist),
+                                   int(bool(symmetric and nzval is None)))
+    if lv < 0:
+        raise MemoryError("orc_bfs_levels_fast")
+    return dist, lv
+
+
+def bfs_parents_fast(n, rowptr, colval, source, rule, dist=None, symmetric=False):
+    """bfs_parents(A_T, source) from the pattern's hop distances (O(nnz); the same
+    parents as bfs_parents)."""
+    rowptr, colval = _c(rowptr, np.int32), _c(colval, np.int32)
+    if dist is None:
+        dist, _ = bfs_levels_fast(n, rowptr, colval, None, source, symmetric)
+    dist = _c(dist, np.int32)
+    par = np.empty(n, np.int32)
+    lib().orc_bfs_parents_from_levels(n, _p(rowptr), _p(colval), _p(dist), source, rule, _p(par))
+    return par
+
+
+def bfs_levels_multi(n, rowptr, colval, sources, rows, symmetric=False):
+    """Hop distances of every source (shortest_path(A_T, sources) with Bool A_T) on
+    the listed 0-based rows: (len(rows), S) array, column q for sources[q]."""
+    rowptr, colval = _c(rowptr, np.int32), _c(colval, np.int32)
+    src = _c(np.atleast_1d(sources), np.int64)
+    rows = _c(rows, np.int64)
+    out = np.empty((len(rows), len(src)), dtype=np.int32, order="F")
+    rc = lib().orc_bfs_levels_multi(n, _p(rowptr), _p(colval), _p(src), len(src), _p(rows),
+                                    len(rows), _p(out), int(bool(symmetric)))
+    if rc != OK:
+        raise MemoryError("orc_bfs_levels_multi")
+    return out
+
+
+def sssp_dijkstra(n, rowptr, colval, nzval, source, symmetric=False):
+    """shortest_path(A_T, source) by Dijkstra (Bool / Int32 / Float32 values, all
+    non-negative): the Jacobi fixpoint of sssp bit for bit.  Returns dist (Int32
+    for Bool / Int32, Float32 for Float32)."""
+    rowptr, colval, nzval = _c(rowptr, np.int32), _c(colval, np.int32), _c(nzval)
+    td = dist_type(tcode(nzval))
+    dist = np.empty(n, dtype=npdtype(td))
+    rc = lib().orc_sssp_dijkstra(n, _p(rowptr), _p(colval), _p(nzval), tcode(nzval), source,
+                                 _p(dist), int(bool(symmetric)))
+    if rc != OK:
+        raise ValueError("orc_sssp_dijkstra: status %d (negative / NaN weights or overflow)" % rc)
+    return dist
 
 
 def dist_type(tv):

@@ -255,3 +255,78 @@ def test_generators_and_assembly():
     assert len(gs) == 4 * 4 + 3 * 5 and gw.min() >= 1.0 and gw.max() < 10.0
     x = O.gen_uniform_f32(1000, 5)
     assert x.min() >= 0 and x.max() < 1
+
+
+# --------------------------------------------------------------------------------
+# full-size cross-checks (frontier BFS, parents from levels, multi-source BFS,
+# Dijkstra) against the restated level-synchronous / Jacobi loops
+# --------------------------------------------------------------------------------
+
+def _graphs_for_cross_checks():
+    """Directed and symmetric graphs with unreachable parts, hubs and a grid."""
+    out = []
+    s, d, w = O.gen_rmat(11, 8 * 2048, 0.57, 0.19, 0.19, 5, 2)  # Int32 1..255
+    out.append(("rmat11_sym",) + O.coo_to_csr(2048, s, d, w, True, True))
+    out.append(("rmat11_dir",) + O.coo_to_csr(2048, s, d, w, False, False))
+    s, d, w = O.gen_er(3000, 3 * 3000, 6, 1)  # sparse directed ER, Float32 [0,1)
+    out.append(("er3000_dir",) + O.coo_to_csr(3000, s, d, w, False, False))
+    s, d, w = O.gen_grid(40, 37, 7, 3)  # Float32 [1, 10)
+    out.append(("grid40x37",) + O.coo_to_csr(40 * 37, s, d, w, True, True))
+    return out
+
+
+def test_frontier_bfs_equals_level_synchronous_bfs():
+    for name, rowptr, colval, nzval in _graphs_for_cross_checks():
+        n = len(rowptr) - 1
+        pat = np.ones(len(colval), np.bool_)
+        for src in (1, n // 3 + 1, n):
+            ref, _ = O.bfs_levels(n, rowptr, colval, pat, src)
+            got, lv = O.bfs_levels_fast(n, rowptr, colval, None, src)
+            assert (got == ref).all(), name
+            assert lv == ref[ref != I32MAX].max()
+            if "dir" not in name:  # symmetric: rows are their own out-edge lists
+                got, _ = O.bfs_levels_fast(n, rowptr, colval, None, src, symmetric=True)
+                assert (got == ref).all(), name
+            if nzval.dtype == np.int32:  # only odd stored values are edges
+                ref, _ = O.bfs_levels(n, rowptr, colval, nzval, src)
+                got, _ = O.bfs_levels_fast(n, rowptr, colval, nzval, src)
+                assert (got == ref).all(), name
+            for rule in (1, 2):
+                par_ref, _ = O.bfs_parents(n, rowptr, colval, src, rule)
+                assert (O.bfs_parents_fast(n, rowptr, colval, src, rule) == par_ref).all(), name
+
+
+def test_multi_source_bfs_equals_shortest_path_on_bool():
+    for name, rowptr, colval, _ in _graphs_for_cross_checks()[:3]:
+        n = len(rowptr) - 1
+        src = np.array([1, 5, n // 2, n], np.int64)
+        rows = np.arange(0, n, 3, dtype=np.int64)
+        ref, _ = O.sssp(n, rowptr, colval, np.ones(len(colval), np.bool_), src)
+        got = O.bfs_levels_multi(n, rowptr, colval, src, rows)
+        assert (got == ref[rows]).all(), name
+        if "dir" not in name:
+            got = O.bfs_levels_multi(n, rowptr, colval, src, rows, symmetric=True)
+            assert (got == ref[rows]).all(), name
+
+
+def test_dijkstra_equals_jacobi_bellman_ford_bit_for_bit():
+    """Int32 and Float32 weights: Dijkstra's distances equal the Jacobi fixpoint of
+    shortest_path! bit for bit (Float32 sums rounded once per step in both)."""
+    for name, rowptr, colval, nzval in _graphs_for_cross_checks():
+        n = len(rowptr) - 1
+        for src in (1, n // 2):
+            ref, _ = O.sssp(n, rowptr, colval, nzval, [src])
+            got = O.sssp_dijkstra(n, rowptr, colval, nzval, src)
+            assert got.dtype == ref.dtype
+            assert np.array_equal(got.view(np.int32), ref[:, 0].view(np.int32)), name
+            if "dir" not in name:
+                got = O.sssp_dijkstra(n, rowptr, colval, nzval, src, symmetric=True)
+                assert np.array_equal(got.view(np.int32), ref[:, 0].view(np.int32)), name
+    # Bool A_T: hop counts
+    name, rowptr, colval, _ = _graphs_for_cross_checks()[1]
+    n = len(rowptr) - 1
+    pat = np.ones(len(colval), np.bool_)
+    assert (O.sssp_dijkstra(n, rowptr, colval, pat, 3) == O.sssp(n, rowptr, colval, pat, [3])[0][:, 0]).all()
+    with pytest.raises(ValueError):
+        O.sssp_dijkstra(3, np.array([1, 2, 3, 3], np.int32), np.array([2, 3], np.int32),
+                        np.array([1.0, -1.0], np.float32), 1)

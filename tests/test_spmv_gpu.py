@@ -502,6 +502,121 @@ def test_spmv_plus_times_large_csr_sorted_sell_path():
             assert (yh == first).all()
 
 
+def test_spmv_long_rows_keep_the_absorb_stop():
+    """CSR row blocks (m < 65536): rows longer than 32 entries are reduced by warp
+    segments in tree order; a row whose sum is NaN there is folded again in storage
+    order with the stop at +Inf, so every row has the oracle's NaN / +Inf / -Inf
+    pattern (plain plus-times and the generic masked kernel)."""
+    m = 6000
+    rowptr, colval, nzval, A = power_law_csr(m, 41)
+    rng = np.random.default_rng(41)
+    cc = np.bincount(colval - 1, minlength=m)
+    x = rng.random(m, dtype=np.float32)
+    order = np.argsort(-cc, kind="stable")
+    x[order[0]] = np.inf
+    x[order[5:400:9]] = np.nan
+    x[order[7:400:11]] = -np.inf
+    B = G.SparseGPUMatrixCSR(m, m, rowptr, colval, nzval)
+    deg = np.diff(rowptr)
+    mask = np.ones(m, np.float32)
+    mask[::7] = 0
+    for mk in (None, mask):
+        y0 = np.full(m, 3.0, np.float32)
+        yo = y0.copy()
+        O.csr_spmv(m, m, rowptr, colval, nzval, yo, x, mask=mk)
+        with np.errstate(invalid="ignore"):
+            ref = A.astype(np.float64) @ x.astype(np.float64)
+        stop = np.isposinf(yo) & np.isnan(ref)
+        assert (stop & (deg > 32)).any() and (stop & (deg <= 32)).any()
+        y = dev(y0)
+        if mk is None:
+            G.gpu_spmv_(y, B, dev(x))
+        else:
+            G.gpu_spmv_(y, B, dev(x), mask=dev(mk))
+        yh = host(y)
+        for f in (np.isnan, np.isposinf, np.isneginf):
+            assert np.array_equal(f(yh), f(yo)), (f.__name__, mk is None)
+        short = deg <= 32
+        np.testing.assert_array_equal(yh[short], yo[short])
+        fin = np.isfinite(yo)
+        if mk is not None:
+            fin &= mask != 0
+            np.testing.assert_array_equal(yh[mask == 0], y0[mask == 0])
+        np.testing.assert_allclose(yh[fin], ref[fin], rtol=RTOL, atol=1e-6)
+
+
+def special_x(A, seed):
+    """x in [0, 1) with +Inf on the most frequent column and on a late column, NaN on
+    a light column and -Inf on another: rows reach +Inf before or after the NaN /
+    -Inf terms in storage order, in short rows and in hub rows."""
+    n = A.n
+    colval = host(A.colval)
+    cc = np.bincount(colval - 1, minlength=n)
+    x = np.random.default_rng(seed).random(n, dtype=np.float32)
+    hub = int(np.argmax(cc))
+    late = int(np.flatnonzero(cc >= 8)[-1])  # a +Inf column near the end of most rows
+    light = [int(c) for c in np.flatnonzero(cc == 1)[:2]]
+    mid = np.flatnonzero((cc >= 4) & (cc <= 64))
+    x[hub] = np.inf
+    x[late] = np.inf
+    x[light[0]] = np.nan
+    x[light[1]] = -np.inf
+    x[mid[1::97][:24]] = np.nan
+    x[mid[50::97][:24]] = -np.inf
+    return x
+
+
+@pytest.mark.parametrize("layout", ["registers", "bulk_copy", "window_tiles", "built_in"])
+def test_spmv_large_csr_keeps_the_absorb_stop(layout):
+    """A CSR of >= 65536 rows runs plus-times on its SELL-32 copy (register or
+    bulk-copy staging) or on column-window tiles; the result still follows the
+    reference's CSR kernel, whose fold stops once the sum reaches the absorbing +Inf
+    (csr_spmv_kernel!, src/spmv/CSR.jl:47-52; monoid_absorb(GPUGraphs_add) = typemax,
+    src/algebra.jl:45).  With +Inf, NaN and -Inf in x: every row of at most 128
+    entries equals the oracle bit for bit on the SELL copy, every row has the oracle's
+    NaN / +Inf / -Inf pattern on every layout, finite rows are within rtol 1e-5 of
+    FP64; two calls give the same bits."""
+    from gpugraphs import generators as gen
+    from gpugraphs import tuning
+    A = gen.rmat(17, 16, seed=31, wkind=gen.W_U01_F32)
+    n = A.n
+    rowptr, colval, nz = host(A.rowptr), host(A.colval), host(A.nzval)
+    if layout == "window_tiles":
+        tuning.apply(A, {"spmv_kernel": "window_tiles"})
+    elif layout != "built_in":
+        tuning.apply(A, {"spmv_kernel": "sell", "slice_size": 32, "sigma": n,
+                         "sell_variant": layout})
+    x = special_x(A, 31)
+    yo = np.zeros(n, np.float32)
+    assert O.csr_spmv(n, n, rowptr, colval, nz, yo, x) == O.OK
+    # the cases the test is about are present
+    deg = np.diff(rowptr)
+    short = deg <= SELL_CHUNK
+    with np.errstate(invalid="ignore"):
+        ref = A.to_scipy().astype(np.float64) @ x.astype(np.float64)
+    stop = np.isposinf(yo) & np.isnan(ref)  # +Inf reached, then NaN or -Inf
+    assert (stop & short).sum() >= 10 and (stop & ~short).sum() >= 1
+    assert (np.isnan(yo) & short).any() and (np.isneginf(yo) & short).any()
+    first = None
+    for _ in range(2):
+        y = torch.full((n,), -7.0, dtype=torch.float32, device="cuda")
+        G.gpu_spmv_(y, A, dev(x))
+        yh = host(y)
+        if first is None:
+            first = yh
+        else:
+            assert np.array_equal(yh.view(np.int32), first.view(np.int32))
+    assert G.spmv_layout(A) == ("window_tiles" if layout == "window_tiles" else "sell")
+    for f in (np.isnan, np.isposinf, np.isneginf):
+        assert np.array_equal(f(yh), f(yo)), f.__name__
+    if layout != "window_tiles":
+        np.testing.assert_array_equal(yh[short], yo[short])
+    fin = np.isfinite(yo)
+    np.testing.assert_allclose(yh[fin], ref[fin], rtol=RTOL, atol=1e-6)
+    # the NaN rows the fast fold leaves are refolded like the oracle on long rows too
+    np.testing.assert_array_equal(yh[stop], yo[stop])
+
+
 @pytest.mark.parametrize("scale,seed", [(16, 21), (17, 14), (18, 22)])
 def test_spmv_plus_times_window_tiles(scale, seed):
     """Plus-times over column-window tiles of a large power-law CSR (rows
@@ -530,22 +645,26 @@ def test_spmv_plus_times_window_tiles(scale, seed):
             assert (yh == first).all()
     deg = np.diff(host(A.rowptr))
     assert (first[deg == 0] == 0).all()
-    # special values: one NaN column, one +Inf column (positive weights: rows through it
-    # are +Inf unless they also hold the NaN)
+    # special values: one NaN column, one +Inf column.  A CSR row follows
+    # csr_spmv_kernel!'s storage-order fold with its stop at +Inf (CSR.jl:47-52): a row
+    # holding the +Inf column before the NaN one is +Inf, after it NaN -- the oracle's
+    # pattern, not the FP64 product's
     colcount = np.bincount(host(A.colval) - 1, minlength=n)
     hub = int(np.argmax(colcount))
     light = int(np.flatnonzero(colcount == 1)[0])
     xs = x.copy()
     xs[hub] = np.inf
     xs[light] = np.nan
-    with np.errstate(invalid="ignore"):
-        ref_s = S @ xs.astype(np.float64)
+    yo = np.zeros(n, np.float32)
+    O.csr_spmv(n, n, host(A.rowptr), host(A.colval), host(A.nzval), yo, xs)
     y = torch.zeros(n, dtype=torch.float32, device="cuda")
     G.gpu_spmv_(y, A, dev(xs))
     yh = host(y)
-    assert (np.isnan(yh) == np.isnan(ref_s)).all()
-    assert (np.isposinf(yh) == np.isposinf(ref_s)).all()
-    fin = np.isfinite(ref_s)
+    assert (np.isnan(yh) == np.isnan(yo)).all()
+    assert (np.isposinf(yh) == np.isposinf(yo)).all()
+    with np.errstate(invalid="ignore"):
+        ref_s = S @ xs.astype(np.float64)
+    fin = np.isfinite(yo)
     np.testing.assert_allclose(yh[fin], ref_s[fin], rtol=RTOL, atol=1e-6)
 
 
