@@ -301,30 +301,13 @@ def secondary_sparse_vector(device, A):
     return out
 
 
-def run_spmv_rmat(args, scale=22):
+def measure_spmv(A, x, steps, warmup, device, ws, sample_clocks=True):
+    """Times `steps` plus-times SpMVs y = A x with inputs resident in HBM (CUDA events
+    on the launching stream), the main kernel alone under the library's launch tracer,
+    and the same call end to end with host buffers.  Returns a dict of the figures."""
     import torch
     import torch.distributed as dist
     import gpugraphs as G
-    from gpugraphs import generators as gen
-
-    ws, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    device = torch.device("cuda", local)
-    if ws > 1:
-        dist.init_process_group("nccl", device_id=device)
-    A = rmat(scale, gen.W_U01_F32, device)
-    x = gen.uniform_vector(A.n, seed=2, device=device)
-    if args.sell_variant or args.hot_cols or args.layout == "sell":
-        from gpugraphs import tuning
-        tuning.apply(A, {"spmv_kernel": "sell", "slice_size": 32, "sigma": A.m})
-        G.gpu_spmv_(torch.zeros(A.n, device=device), A, x)  # builds the SELL-32 copy
-        choice = {"sell_variant": args.sell_variant or "registers"}
-        if args.hot_cols:
-            choice["hot_cols"] = args.hot_cols
-        tuning.apply(A, choice)
-    if args.layout == "window_tiles":
-        from gpugraphs import tuning
-        tuning.apply(A, {"spmv_kernel": "window_tiles"})
     n, nnz = A.n, A.nnz()
     y = torch.zeros(n, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
@@ -332,47 +315,45 @@ def run_spmv_rmat(args, scale=22):
     def step():
         G.gpu_spmv_(y, A, x)
 
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         step()
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
-    clk = ClockSampler(local)
-    clk.start()
-    time.sleep(0.3)
+    clk = ClockSampler(device.index or 0) if sample_clocks else None
+    if clk:
+        clk.start()
+        time.sleep(0.3)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     ev0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         step()
     ev1.record(stream)
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
     ms = ev0.elapsed_time(ev1)
-    t_end = time.time() + 1.0  # keep the sampler on the same work a little longer
-    while time.time() < t_end:
-        for _ in range(50):
-            step()
-        torch.cuda.synchronize()
-    clocks = clk.stop()
+    clocks = None
+    if clk:
+        t_end = time.time() + 1.0  # keep the sampler on the same work a little longer
+        while time.time() < t_end:
+            for _ in range(50):
+                step()
+            torch.cuda.synchronize()
+        clocks = clk.stop()
     ms = max_over_ranks(ms, device)
-    per_step_ms = ms / args.steps
+    per_step_ms = ms / steps
     B = spmv_bytes(n, nnz)
-    value = aggregate_gbs(ws, B, per_step_ms)
 
     # roofline of the dominant kernel: the same K steps again under the library's
     # launch tracer, which brackets the matrix-streaming kernel of every call with
     # CUDA events on the launching stream and counts every kernel launch
     from gpugraphs.tracing import launch_trace
     with launch_trace(device) as tr:
-        for _ in range(args.steps):
+        for _ in range(steps):
             step()
     kernel_ms = tr.kernel_ms / max(tr.timed, 1)
-    peak, peak_kind = peak_hbm()
-    achieved = B / (kernel_ms * 1e-3) / 1e9
-    workload = "spmv_csr_rmat%d" % scale
-    traffic = traffic_from_profiles(workload)
 
     # e2e through the public API with host buffers
     # every step copies its x from pinned host memory and reads its y back; the copies
@@ -408,18 +389,52 @@ def run_spmv_rmat(args, scale=22):
         for b in range(2):
             stream.wait_event(ev_freed[b])
 
-    e2e_steps(max(args.warmup, 3))
+    e2e_steps(max(warmup, 3))
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    e2e_steps(args.steps)
+    e2e_steps(steps)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    assert bool(torch.equal(yd[(args.steps - 1) & 1].cpu(), yh[(args.steps - 1) & 1]))
-    e2e_val = aggregate_gbs(ws, B, max_over_ranks(e2e_ms, device))
+    e2e_ms = e0.elapsed_time(e1) / steps
+    assert bool(torch.equal(yd[(steps - 1) & 1].cpu(), yh[(steps - 1) & 1]))
+    peak, peak_kind = peak_hbm()
+    achieved = B / (kernel_ms * 1e-3) / 1e9
+    return {"y": y, "per_step_ms": per_step_ms, "value": aggregate_gbs(ws, B, per_step_ms),
+            "kernel_ms": kernel_ms, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+            "frac": achieved / peak, "bytes": B, "launches": tr.launches, "clocks": clocks,
+            "e2e": aggregate_gbs(ws, B, max_over_ranks(e2e_ms, device)), "e2e_ms": e2e_ms}
 
-    ok = spot_check(A, x, y)
+
+def run_spmv_rmat(args, scale=22):
+    import torch
+    import torch.distributed as dist
+    import gpugraphs as G
+    from gpugraphs import generators as gen
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=device)
+    A = rmat(scale, gen.W_U01_F32, device)
+    x = gen.uniform_vector(A.n, seed=2, device=device)
+    if args.sell_variant or args.hot_cols or args.layout == "sell":
+        from gpugraphs import tuning
+        tuning.apply(A, {"spmv_kernel": "sell", "slice_size": 32, "sigma": A.m})
+        G.gpu_spmv_(torch.zeros(A.n, device=device), A, x)  # builds the SELL-32 copy
+        choice = {"sell_variant": args.sell_variant or "registers"}
+        if args.hot_cols:
+            choice["hot_cols"] = args.hot_cols
+        tuning.apply(A, choice)
+    if args.layout == "window_tiles":
+        from gpugraphs import tuning
+        tuning.apply(A, {"spmv_kernel": "window_tiles"})
+    n, nnz = A.n, A.nnz()
+    m = measure_spmv(A, x, args.steps, args.warmup, device, ws)
+    y = m.pop("y")
+    workload = "spmv_csr_rmat%d" % scale
+    traffic = traffic_from_profiles(workload)
     layout = G.spmv_layout(A)
     if layout == "window_tiles":
         kernel_label = ("k_spmv_pipe (tail rows) + k_spmv_win (column-window tiles: rows sorted "
@@ -428,30 +443,40 @@ def run_spmv_rmat(args, scale=22):
         kernel_label = ({"registers": "k_sell_hot32", "bulk_copy": "k_sell_tma32"}[
             args.sell_variant or "registers"]
             + " (SELL-32 copy sorted by row length, relabelled columns)")
-    secondary = {} if (args.no_secondary or scale != 22) else secondary_rmat22(device, A, x)
+    # parity of this run's own output, every row, after the timed region
+    parity = {}
+    if rank == 0 and not args.no_parity:
+        parity["spmv_rmat%d" % scale] = spmv_parity(A, x, y)
+    secondary = {}
+    if not args.no_secondary and scale == 22:
+        secondary = secondary_rmat22(device, A, x)
     cpu = cpu_baseline_spmv(A, x) if (rank == 0 and not args.no_cpu) else None
+    if not args.no_secondary and scale == 22:
+        del A, x, y
+        torch.cuda.empty_cache()
+        secondary.update(secondary_large(args, device, parity, rank))
     out = {
         "metric": "SpMV GB/s (plus-times Float32, CSR, R-MAT scale %d)" % scale,
-        "value": round(value, 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": round(per_step_ms, 5),
+        "value": round(m["value"], 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(m["per_step_ms"], 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded R-MAT generator on the device)",
         "config": {"workload": workload, "n": n, "nnz": nnz, "format": "CSR",
                    "semiring": "(mul, add, second)",
                    "l2": "inputs larger than L2 (CSR %.2f GB)" % ((4 * (n + 1) + 8 * nnz) / 1e9),
                    "parallelism": "replicas" if ws > 1 else "single"},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "peak_kind": peak_kind, "algorithmic_bytes": B,
-                     "kernel_ms": round(kernel_ms, 5),
+        "roofline": {"bound": "hbm", "achieved": round(m["achieved"], 2), "peak": m["peak"],
+                     "unit": "GB/s", "frac": round(m["frac"], 4), "traffic": traffic,
+                     "peak_kind": m["peak_kind"], "algorithmic_bytes": m["bytes"],
+                     "kernel_ms": round(m["kernel_ms"], 5),
                      "kernel": kernel_label},
-        "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * n,
+        "e2e": {"value": round(m["e2e"], 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * n,
                 "schedule": "x of step i+1 copied in and y of step i-1 copied out on two side "
                             "streams while step i's SpMV runs (double buffers)"},
-        "gpu_launches": tr.launches,
-        "clocks": clocks,
-        "parity_spot_check": ok,
+        "gpu_launches": m["launches"],
+        "clocks": m["clocks"],
+        "parity": parity,
         "secondary": secondary,
     }
     if cpu is not None:
@@ -462,21 +487,26 @@ def run_spmv_rmat(args, scale=22):
         dist.destroy_process_group()
 
 
-def spot_check(A, x, y, nrows=2048):
-    """FP64 check of this run's output on seeded rows (rel err vs FP64 <= 1e-5)."""
+def spmv_parity(A, x, y):
+    """Every row of this run's SpMV output against an FP64 product (rel err <= 1e-5)
+    and against the oracle's storage-order fold (csr_spmv_kernel!), bit for bit on
+    the rows of <= 128 entries (the SELL-32 copy folds those in storage order)."""
     import numpy as np
-    import torch
-    rp = A.rowptr.to(torch.int64)
-    rows = torch.from_numpy(np.random.default_rng(3).integers(0, A.n, nrows)).to(x.device)
-    worst = 0.0
-    xs = x.double()
-    for i in rows.tolist():
-        lo, hi = int(rp[i]) - 1, int(rp[i + 1]) - 1
-        ref = float((A.nzval[lo:hi].double() * xs[A.colval[lo:hi].long() - 1]).sum()) if hi > lo else 0.0
-        got = float(y[i])
-        err = abs(got - ref) / abs(ref) if ref != 0 else abs(got)
-        worst = max(worst, err)
-    return {"rows": nrows, "max_rel_err_vs_fp64": worst, "ok": worst <= 1e-5}
+    import scipy.sparse as sp
+    from oracle import oracle as O
+    rp, cv, nz = A.rowptr.cpu().numpy(), A.colval.cpu().numpy(), A.nzval.cpu().numpy()
+    xh, yh = x.cpu().numpy(), y.cpu().numpy()
+    M = sp.csr_matrix((nz.astype(np.float64), cv - 1, rp - 1), shape=(A.m, A.n))
+    ref = M @ xh.astype(np.float64)
+    d = np.abs(yh.astype(np.float64) - ref)
+    err = float(np.max(np.where(ref != 0, d / np.where(ref != 0, np.abs(ref), 1.0), d)))
+    yo = np.empty(A.m, np.float32)
+    O.spmv_plus_times_f32(rp, cv, nz, xh, yo)
+    short = np.diff(rp) <= 128
+    exact = int(np.count_nonzero(yh[short] == yo[short]))
+    return {"rows": int(A.m), "max_rel_err_vs_fp64": err, "rows_le_128_entries": int(short.sum()),
+            "rows_le_128_bit_exact_vs_oracle": exact,
+            "ok": bool(err <= 1e-5 and exact == int(short.sum()))}
 
 
 def cpu_baseline_spmv(A, x, budget_s=8.0):
@@ -504,15 +534,10 @@ def cpu_baseline_spmv(A, x, budget_s=8.0):
 # BFS / SSSP workloads (R-MAT scale 24, 4096 x 4096 grid)
 # ---------------------------------------------------------------------------------
 
-def run_search(args, kind, graph):
-    import numpy as np
-    import torch
-    import gpugraphs as G
+def search_graph(kind, graph, device):
+    """The configured search graphs: R-MAT (Bool pattern for BFS, Int32 weights 1..255
+    for shortest paths) or the 4096 x 4096 grid (pattern / Float32 weights [1, 10))."""
     from gpugraphs import generators as gen
-
-    ws, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    device = torch.device("cuda", local)
     if graph.startswith("rmat"):
         sc = int(graph[4:])
         A = rmat(sc, gen.W_PATTERN if kind == "bfs" else gen.W_INT_1_255, device)
@@ -523,6 +548,54 @@ def run_search(args, kind, graph):
                      device=device)
         cfg = "4096x4096 4-neighbour grid" + (", Bool pattern" if kind == "bfs" else
                                                ", Float32 weights [1,10)")
+    return A, cfg
+
+
+def hop_levels(A, s, device):
+    """BFS level count from s on A's pattern (a search's hop eccentricity + 1)."""
+    import torch
+    import gpugraphs as G
+    P = A if A.dtype == torch.bool else G.SparseGPUMatrixCSR(
+        A.m, A.n, A.rowptr, A.colval, torch.ones(A.nnz(), dtype=torch.bool, device=device))
+    lv = G.bfs_distances(P, int(s))
+    return int(lv[lv != I32MAX].max().item()) + 1
+
+
+def search_parity(A, kind, s, d):
+    """One search's result against the oracle's full-size cross-checks: BFS levels
+    and CSR parents by frontier BFS, shortest paths by Dijkstra (bit for bit; both
+    pinned against the restated reference loops in the CPU tests)."""
+    import numpy as np
+    import gpugraphs as G
+    from oracle import oracle as O
+    rp, cv = A.rowptr.cpu().numpy(), A.colval.cpu().numpy()
+    t0 = time.perf_counter()
+    if kind == "bfs":
+        ref, _ = O.bfs_levels_fast(A.n, rp, cv, None, s, symmetric=True)
+        lev_ok = bool(np.array_equal(d.cpu().numpy(), ref))
+        par = G.bfs_parents(A, s).cpu().numpy()
+        par_ok = bool(np.array_equal(par, O.bfs_parents_fast(A.n, rp, cv, s, 1, dist=ref)))
+        out = {"source": int(s), "levels_equal": lev_ok, "parents_equal": par_ok,
+               "ok": lev_ok and par_ok, "oracle": "frontier BFS; parents from levels (CSR rule)"}
+    else:
+        ref = O.sssp_dijkstra(A.n, rp, cv, A.nzval.cpu().numpy(), s, symmetric=True)
+        got = d.cpu().numpy()
+        ok = bool(np.array_equal(got.view(np.int32), ref.view(np.int32)))
+        out = {"source": int(s), "distances_equal": ok, "ok": ok,
+               "oracle": "Dijkstra in the distance type (%s)" % got.dtype}
+    out["check_s"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
+def run_search(args, kind, graph):
+    import numpy as np
+    import torch
+    import gpugraphs as G
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    A, cfg = search_graph(kind, graph, device)
     n, nnz = A.n, A.nnz()
     src = sources_for(A, 64, 11)
     run = (lambda i: G.bfs_distances(A, int(src[i % len(src)]))) if kind == "bfs" else \
@@ -579,17 +652,60 @@ def run_search(args, kind, graph):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu:
-        if kind != "bfs":  # level count of the same search on the Bool pattern
-            P = G.SparseGPUMatrixCSR(A.m, A.n, A.rowptr, A.colval,
-                                     torch.ones(A.nnz(), dtype=torch.bool, device=device))
-            lv = G.bfs_distances(P, int(src[0]))
-            del P
-        else:
-            lv = d0
-        levels_full = int(lv[lv != I32MAX].max().item()) + 1
-        out["cpu_baseline"] = cpu_baseline_search(A, kind, int(src[0]), mcc, levels_full)
+        out["cpu_baseline"] = cpu_baseline_search(A, kind, int(src[0]), mcc,
+                                                  hop_levels(A, src[0], device))
+    if rank == 0 and not args.no_parity:
+        out["parity"] = search_parity(A, kind, int(src[0]), d0)
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def secondary_large(args, device, parity, rank):
+    """The configurations beyond the scale-22 graph, each measured briefly: plus-times
+    SpMV on R-MAT scale 24 (the 70%-of-HBM target configuration), BFS and shortest
+    paths on R-MAT scale 24 and on the 4096 x 4096 grid, and a summary of the serving
+    loop.  One search of each large graph is checked against the oracle."""
+    import torch
+    import gpugraphs as G
+    from gpugraphs import generators as gen
+    out = {}
+    t0 = time.time()
+    A = rmat(24, gen.W_U01_F32, device)
+    x = gen.uniform_vector(A.n, seed=2, device=device)
+    m = measure_spmv(A, x, 10, 3, device, 1, sample_clocks=False)
+    out["spmv_csr_rmat24"] = {
+        "n": A.n, "nnz": A.nnz(), "ms": round(m["per_step_ms"], 4), "gbs": round(m["value"], 1),
+        "kernel_ms": round(m["kernel_ms"], 4), "kernel_gbs": round(m["achieved"], 1),
+        "frac": round(m["frac"], 4), "peak": m["peak"], "e2e_gbs": round(m["e2e"], 1),
+        "layout": G.spmv_layout(A)}
+    del A, x, m
+    torch.cuda.empty_cache()
+    for kind, graph, reps, budget in (("bfs", "rmat24", 8, 40), ("sssp", "rmat24", 4, 4),
+                                      ("bfs", "grid4096", 4, 40), ("sssp", "grid4096", 3, 6)):
+        A, cfg = search_graph(kind, graph, device)
+        src = sources_for(A, 64, 11)
+        run = (lambda i: G.bfs_distances(A, int(src[i % len(src)]))) if kind == "bfs" else \
+            (lambda i: G.shortest_path(A, int(src[i % len(src)])))
+        d0 = run(0)
+        unreached = torch.isinf(d0) if d0.is_floating_point() else (d0 == I32MAX)
+        mcc = reached_edges(A, torch.where(unreached, I32MAX, 0).to(torch.int32))
+        ts = time_host(run, reps, warmup=2)
+        t = sum(ts) / len(ts)
+        lv = hop_levels(A, src[0], device)
+        B = (bfs_bytes if kind == "bfs" else sssp_bytes)(A.n, A.nnz())
+        rec = {"gteps": round(mcc / t / 1e9, 3), "ms": round(t * 1e3, 3), "searches": reps,
+               "levels_from_first_source": lv, "n": A.n, "nnz": A.nnz(), "m_cc": mcc,
+               "gbs_algorithmic": round(B / t / 1e9, 1), "graph": cfg}
+        if rank == 0 and not args.no_cpu:
+            rec["cpu_baseline"] = cpu_baseline_search(A, kind, int(src[0]), mcc, lv, budget=budget)
+        if rank == 0 and not args.no_parity and (kind, graph) in (("bfs", "rmat24"), ("sssp", "grid4096")):
+            parity["%s_%s" % (kind, graph)] = search_parity(A, kind, int(src[0]), d0)
+        out["%s_%s" % (kind, graph)] = rec
+        del A, d0, run
+        torch.cuda.empty_cache()
+    out["serve_summary"] = serve_summary(device)
+    out["large_configs_s"] = round(time.time() - t0, 1)
+    return out
 
 
 def cpu_baseline_search(A, kind, s, mcc, levels_full, budget=40):
@@ -743,67 +859,60 @@ def run_sparse_vector(args):
 # serving: Poisson arrivals over 16 resident graphs, continuous batching
 # ---------------------------------------------------------------------------------
 
-def run_serve(args):
+class ServeMix:
     """16 resident R-MAT graphs (scales 16..23, one Int32- and one Float32-weighted per
     scale); requests: 1/3 BFS (Int32 graphs), 1/3 shortest paths (any graph), 1/3
-    20-step plus-times SpMV iterations (Float32 graphs); graph and source seeded.
-    For each Poisson rate the host submits open-loop for a bounded number of requests
-    and the server's own submit->result latencies give p50 / p99; the plain path runs
-    the same kind of mix one query at a time through the single-query functions."""
-    import numpy as np
-    import torch
-    import gpugraphs as G
-    from gpugraphs import generators as gen
-    from gpugraphs.serving import Server
+    20-step plus-times SpMV iterations (Float32 graphs); graph and source seeded."""
 
-    ws, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    device = torch.device("cuda", local)
-    graphs = []
-    for sc in range(16, 24):
-        graphs.append(rmat(sc, gen.W_INT_1_255, device))
-        graphs.append(rmat(sc, gen.W_U01_F32, device))
-    ints = [i for i in range(16) if i % 2 == 0]
-    flts = [i for i in range(16) if i % 2 == 1]
-    xs = {g: gen.uniform_vector(graphs[g].n, seed=100 + g, device=device) for g in flts}
-    rng = np.random.default_rng(9)
+    def __init__(self, device):
+        import numpy as np
+        from gpugraphs import generators as gen
+        self.graphs = []
+        for sc in range(16, 24):
+            self.graphs.append(rmat(sc, gen.W_INT_1_255, device))
+            self.graphs.append(rmat(sc, gen.W_U01_F32, device))
+        self.ints = [i for i in range(16) if i % 2 == 0]
+        self.flts = [i for i in range(16) if i % 2 == 1]
+        self.xs = {g: gen.uniform_vector(self.graphs[g].n, seed=100 + g, device=device)
+                   for g in self.flts}
+        self.rng = np.random.default_rng(9)
 
-    def draw():
+    def draw(self):
+        rng = self.rng
         kind = int(rng.integers(0, 3))
         if kind == 0:
-            g = int(rng.choice(ints))
+            g = int(rng.choice(self.ints))
         elif kind == 1:
             g = int(rng.integers(0, 16))
         else:
-            g = int(rng.choice(flts))
-        return kind, g, int(rng.integers(1, graphs[g].n + 1))
+            g = int(rng.choice(self.flts))
+        return kind, g, int(rng.integers(1, self.graphs[g].n + 1))
 
-    # plain path: one query at a time, every graph's per-matrix analysis built first
-    # (each kind runs once per graph before the timed queries)
-    plain_lat = []
-    nplain = max(30, args.steps)
-    for g in range(16):
-        for kind in ((0, 1) if g in ints else (1, 2)):
-            _single(G, graphs, xs, kind, g, 1)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(nplain):
-        kind, g, s = draw()
-        t1 = time.perf_counter()
-        _single(G, graphs, xs, kind, g, s)
+    def plain(self, nq):
+        """The same mix one query at a time through the single-query functions, every
+        graph's per-matrix analysis built first: (queries/s, latencies in s)."""
+        import torch
+        import gpugraphs as G
+        for g in range(16):
+            for kind in ((0, 1) if g in self.ints else (1, 2)):
+                _single(G, self.graphs, self.xs, kind, g, 1)
         torch.cuda.synchronize()
-        plain_lat.append(time.perf_counter() - t1)
-    plain_qps = nplain / (time.perf_counter() - t0)
+        lat = []
+        t0 = time.perf_counter()
+        for _ in range(nq):
+            kind, g, s = self.draw()
+            t1 = time.perf_counter()
+            _single(G, self.graphs, self.xs, kind, g, s)
+            torch.cuda.synchronize()
+            lat.append(time.perf_counter() - t1)
+        return nq / (time.perf_counter() - t0), lat
 
-    srv = Server(reserve_bytes=1 << 30, device=local)
-    ids = [srv.add_graph(A) for A in graphs]
-    sweep = []
-    clk = ClockSampler(local)
-    clk.start()
-    for lam in (1e2, 3e2, 1e3, 3e3, 1e4, 3e4, 1e5):
-        nreq = int(min(lam * 2.0, 3000))
-        gaps = rng.exponential(1.0 / lam, nreq)
-        reqs = [draw() for _ in range(nreq)]
+    def poisson(self, srv, ids, lam, nreq):
+        """Open-loop Poisson submissions at rate lam; the server's own submit->result
+        latencies give p50 / p99."""
+        import numpy as np
+        gaps = self.rng.exponential(1.0 / lam, nreq)
+        reqs = [self.draw() for _ in range(nreq)]
         t_start = time.perf_counter()
         t_next = t_start
         for i, (kind, g, s) in enumerate(reqs):
@@ -815,14 +924,63 @@ def run_serve(args):
             elif kind == 1:
                 srv.submit_sssp(ids[g], s)
             else:
-                srv.submit_spmv_iter(ids[g], xs[g], steps=20)
+                srv.submit_spmv_iter(ids[g], self.xs[g], steps=20)
         t_sub = time.perf_counter() - t_start
         done = srv.wait(timeout=600)
         t_all = time.perf_counter() - t_start
         lat = np.array(sorted(v[1] for v in done.values()))
-        sweep.append({"lambda": lam, "requests": nreq, "offered_qps": round(nreq / t_sub, 1),
-                      "qps": round(nreq / t_all, 1), "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
-                      "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3)})
+        return {"lambda": lam, "requests": nreq, "offered_qps": round(nreq / t_sub, 1),
+                "qps": round(nreq / t_all, 1), "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3)}
+
+
+def serve_summary(device):
+    """Serving at a low and a saturating rate (lambda = 1e2 and 1e4 requests/s) against
+    the one-query-at-a-time path: queries/s and p50 / p99 latency."""
+    import numpy as np
+    from gpugraphs.serving import Server
+    t0 = time.time()
+    mix = ServeMix(device)
+    plain_qps, pl = mix.plain(30)
+    srv = Server(reserve_bytes=1 << 30, device=device.index or 0)
+    ids = [srv.add_graph(A) for A in mix.graphs]
+    low = mix.poisson(srv, ids, 1e2, 200)
+    high = mix.poisson(srv, ids, 1e4, 2000)
+    srv.close()
+    pl = np.array(pl)
+    return {"lambda_1e2": low, "lambda_1e4": high,
+            "best_qps": max(low["qps"], high["qps"]),
+            "plain": {"qps": round(plain_qps, 1), "p50_ms": round(float(np.percentile(pl, 50)) * 1e3, 3),
+                      "p99_ms": round(float(np.percentile(pl, 99)) * 1e3, 3)},
+            "speedup_vs_plain": round(max(low["qps"], high["qps"]) / plain_qps, 2),
+            "p50_low_load_vs_plain": round(low["p50_ms"] / (float(np.percentile(pl, 50)) * 1e3), 2),
+            "mix": "1/3 BFS, 1/3 SSSP, 1/3 SpMV x20 over 16 R-MAT graphs (scales 16..23)",
+            "took_s": round(time.time() - t0, 1)}
+
+
+def run_serve(args):
+    """Poisson-rate sweep of the serving loop (ServeMix) and per-kind saturation, against
+    the same kind of mix one query at a time through the single-query functions."""
+    import numpy as np
+    import torch
+    import gpugraphs as G
+    from gpugraphs.serving import Server
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    mix = ServeMix(device)
+    graphs, ints, xs, rng = mix.graphs, mix.ints, mix.xs, mix.rng
+    nplain = max(30, args.steps)
+    plain_qps, plain_lat = mix.plain(nplain)
+
+    srv = Server(reserve_bytes=1 << 30, device=local)
+    ids = [srv.add_graph(A) for A in graphs]
+    sweep = []
+    clk = ClockSampler(local)
+    clk.start()
+    for lam in (1e2, 3e2, 1e3, 3e3, 1e4, 3e4, 1e5):
+        sweep.append(mix.poisson(srv, ids, lam, int(min(lam * 2.0, 3000))))
     # per kind at saturation (every request submitted at once) against the same kind
     # one query at a time
     per_kind = {}
@@ -1027,6 +1185,8 @@ def main():
     ap.add_argument("--workload", default="spmv_csr_rmat22")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-secondary", action="store_true", help="headline SpMV only")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the checks of this run's results against the oracle")
     ap.add_argument("--graphs", type=int, default=1000, help="graph count of --workload multigraph")
     ap.add_argument("--sell-variant", default=None, choices=["registers", "bulk_copy"],
                     help="SpMV workloads: kernel variant over the SELL-32 copy (default: built-in)")

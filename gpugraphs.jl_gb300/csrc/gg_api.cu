@@ -332,6 +332,12 @@ int gg_set_stream(gg_ctx* ctx, void* stream) {
   return GG_OK;
 }
 
+int gg_set_wait_limit(gg_ctx* ctx, uint64_t polls) {
+  if (!ctx) return set_error(GG_ERR_ARGUMENT, "ctx is NULL");
+  ctx->wait_polls = polls;
+  return GG_OK;
+}
+
 int gg_stream_sync(gg_ctx* ctx) {
   if (!ctx) return set_error(GG_ERR_ARGUMENT, "ctx is NULL");
   GG_CUDA(cudaStreamSynchronize(ctx->stream));

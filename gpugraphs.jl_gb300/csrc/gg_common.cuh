@@ -469,6 +469,7 @@ struct gg_ctx {
   unsigned int* d_flags = nullptr;  // small device word array for status flags
   unsigned int* h_flags = nullptr;  // pinned mirror
   unsigned int* d_err = nullptr;    // set by kernels whose bounded waits ran out
+  unsigned long long wait_polls = 0;  // gg_set_wait_limit; 0 = the built-in limits
   // launch tracing (gg_trace_begin / gg_trace_end): kernel launches of the SpMV /
   // SpMM paths are counted and their main kernel bracketed by events from a pool
   bool trace_on = false;
@@ -478,6 +479,19 @@ struct gg_ctx {
 };
 
 namespace gg {
+// poll limits of the bounded device-side waits: grid barriers of the persistent
+// kernels (each poll sleeps ~100 ns) and bulk-copy completions of the staged SpMV
+// kernels (mbarrier try_wait polls); gg_set_wait_limit replaces both
+static const unsigned kBarrierPolls = 1u << 26;
+static const unsigned kCopyPolls = 1u << 22;
+inline unsigned barrier_polls(const gg_ctx* c) {
+  return c->wait_polls ? (unsigned)(c->wait_polls < 0xffffffffull ? c->wait_polls : 0xffffffffull)
+                       : kBarrierPolls;
+}
+inline unsigned copy_polls(const gg_ctx* c) {
+  return c->wait_polls ? (unsigned)(c->wait_polls < 0xffffffffull ? c->wait_polls : 0xffffffffull)
+                       : kCopyPolls;
+}
 static const int kTraceMax = 4096;
 // count n kernel launches of the current call
 inline void trace_count(gg_ctx* c, int n) {

@@ -769,9 +769,9 @@ __global__ void __launch_bounds__(1024)
 // Persistent cooperative levels for graphs without hubs (grids, meshes: out-degree
 // <= kCoopMaxDeg) while the frontier is medium-sized: one launch runs level after
 // level over all SMs with a grid barrier in between, instead of one launch and one
-// host round trip per level.  The barrier's wait is bounded (about 7 s): when it runs
-// out, the kernel records an error, every block returns, and the call reports
-// GG_ERR_TIMEOUT.  Queue counters rotate over three words so that the counter being
+// host round trip per level.  The barrier's wait is bounded (by default 2^26 polls of
+// 100 ns, about 7 s; gg_set_wait_limit sets another count): when it runs out, the
+// kernel records an error, every block returns, and the call reports GG_ERR_TIMEOUT.  Queue counters rotate over three words so that the counter being
 // zeroed is never the one being read or appended.
 // ---------------------------------------------------------------------------------
 static const int kCoopMaxDeg = 64;
@@ -781,7 +781,7 @@ static const double kNearFarScale = 8.0;  // near-far band width = this x the me
 
 struct CoopCtl {
   unsigned long long cnt[3];
-  unsigned bar[4];  // arrivals, generation, error, unused
+  unsigned bar[4];  // arrivals, generation, error, poll limit of the barrier's waits
   long long nf_out;
   int level_out;    // last completed level / round (relative for SSSP)
   int which_out;    // queue holding the remaining frontier: 0 = first, 1 = second
@@ -793,6 +793,7 @@ __device__ __forceinline__ bool coop_grid_sync(unsigned* bar, unsigned nblocks) 
     volatile unsigned* vgen = bar + 1;
     volatile unsigned* verr = bar + 2;
     const unsigned gen = *vgen;
+    const unsigned long long limit = bar[3];  // set by the control block's init kernel
     __threadfence();
     if (atomicAdd(bar, 1u) == nblocks - 1) {
       bar[0] = 0;
@@ -801,7 +802,7 @@ __device__ __forceinline__ bool coop_grid_sync(unsigned* bar, unsigned nblocks) 
     } else {
       unsigned long long polls = 0;
       while (*vgen == gen && *verr == 0) {
-        if (++polls > (1ull << 26)) {
+        if (++polls > limit) {
           atomicExch(bar + 2, 1u);
           break;
         }
@@ -814,11 +815,12 @@ __device__ __forceinline__ bool coop_grid_sync(unsigned* bar, unsigned nblocks) 
   return *((volatile unsigned*)(bar + 2)) == 0;
 }
 
-__global__ void k_coop_init(CoopCtl* cc, long long nf0) {
+__global__ void k_coop_init(CoopCtl* cc, long long nf0, unsigned polls) {
   cc->cnt[0] = 0;
   cc->cnt[1] = 0;
   cc->cnt[2] = (unsigned long long)nf0;
-  cc->bar[0] = cc->bar[1] = cc->bar[2] = cc->bar[3] = 0;
+  cc->bar[0] = cc->bar[1] = cc->bar[2] = 0;
+  cc->bar[3] = polls;
   cc->nf_out = 0;
   cc->level_out = 0;
   cc->which_out = 0;
@@ -1131,7 +1133,7 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
   while (nf > 0) {
     if (coop_ok && !pull && nf <= kClusterCap) {
       // small and medium frontiers of hub-free graphs: one cluster, cluster barriers
-      k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf);
+      k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf, barrier_polls(ctx));
       k_bfs_cluster<<<kClusterCtas, kCoopThreads, 0, ctx->stream>>>(
           P.rowptr, P.colval, sc.q[cur], sc.q[cur ^ 1], sc.visited, dist, sc.cc, (int32_t)level,
           kClusterCap);
@@ -1151,7 +1153,7 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
       hc = reinterpret_cast<CoopCtl*>(ctx->h_flags);
       if (nf <= coop_hi) {
         // larger frontier: the grid-wide persistent kernel takes it from here
-        k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf);
+        k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf, barrier_polls(ctx));
         int32_t* qa = sc.q[cur];
         int32_t* qb = sc.q[cur ^ 1];
         int32_t lv0 = (int32_t)level;
@@ -1173,7 +1175,7 @@ static int bfs_run(gg_ctx* ctx, gg_mat* A, int32_t s, int which, int32_t* dist,
       // frontier above the persistent kernels' range: push / pull levels below
     }
     if (coop_ok && !pull && nf > small_cap && nf <= coop_hi) {
-      k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf);
+      k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf, barrier_polls(ctx));
       int32_t* qa = sc.q[cur];
       int32_t* qb = sc.q[cur ^ 1];
       int32_t lv0 = (int32_t)level;
@@ -1679,12 +1681,13 @@ struct NfCtl {
   int status;  // 1 finished, 2 step budget exhausted
 };
 
-__global__ void k_nf_init(NfCtl* cc, long long nf0) {
+__global__ void k_nf_init(NfCtl* cc, long long nf0, unsigned polls) {
   cc->cnt[0] = 0;
   cc->cnt[1] = 0;
   cc->cnt[2] = (unsigned long long)nf0;
   cc->fcnt[0] = cc->fcnt[1] = cc->fcnt[2] = 0;
-  cc->bar[0] = cc->bar[1] = cc->bar[2] = cc->bar[3] = 0;
+  cc->bar[0] = cc->bar[1] = cc->bar[2] = 0;
+  cc->bar[3] = polls;  // poll limit of the barrier's waits
   cc->steps_out = 0;
   cc->status = 0;
 }
@@ -2092,7 +2095,7 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
     T delta = static_cast<T>(dd);
     if (!(delta > T(0))) delta = T(1);
     NfCtl* ncc = reinterpret_cast<NfCtl*>(sc.cc);
-    k_nf_init<<<1, 1, 0, ctx->stream>>>(ncc, nf);
+    k_nf_init<<<1, 1, 0, ctx->stream>>>(ncc, nf, barrier_polls(ctx));
     int32_t* qa = sc.q[cur];
     int32_t* qb = sc.q[cur ^ 1];
     unsigned* ia = sc.fb[cur];
@@ -2116,7 +2119,7 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
   while (nf > 0) {
     if (rounds > max_rounds) return set_error(GG_ERR_NOT_CONVERGED, "shortest_path did not converge");
     if (coop_ok && nf > small_cap && nf <= coop_hi && mf * 8 <= P.nnz) {
-      k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf);
+      k_coop_init<<<1, 1, 0, ctx->stream>>>(sc.cc, nf, barrier_polls(ctx));
       int32_t* qa = sc.q[cur];
       int32_t* qb = sc.q[cur ^ 1];
       unsigned* ia = sc.fb[cur];

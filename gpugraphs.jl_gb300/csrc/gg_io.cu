@@ -260,6 +260,14 @@ static int read_rb(const char* path, int expand, HostMatrix* H, int* kind_out) {
       rc = set_error(GG_ERR_ARGUMENT, "%s: column pointers do not span 1:nnz+1", path);
       break;
     }
+    // every pointer in 1:nnz+1 and non-decreasing before any entry is read through them
+    bool ptr_ok = true;
+    for (int64_t j = 0; j < ncol && ptr_ok; ++j)
+      ptr_ok = cp[(size_t)j] >= 1 && cp[(size_t)j] <= cp[(size_t)j + 1] && cp[(size_t)j + 1] <= nnz + 1;
+    if (!ptr_ok) {
+      rc = set_error(GG_ERR_ARGUMENT, "%s: column pointers out of range or decreasing", path);
+      break;
+    }
     std::vector<int64_t> col, row;
     std::vector<double> val;
     col.reserve((size_t)nnz * (expand ? 2 : 1));
@@ -282,6 +290,11 @@ static int read_rb(const char* path, int expand, HostMatrix* H, int* kind_out) {
       }
     }
     if (bad) { rc = set_error(GG_ERR_ARGUMENT, "%s: row index or pointer out of range", path); break; }
+    if ((int64_t)col.size() >= (1LL << 31) - 1) {
+      rc = set_error(GG_ERR_ARGUMENT, "%s: %lld entries after symmetric expansion do not fit Int32 indices",
+                     path, (long long)col.size());
+      break;
+    }
     H->m = nrow;
     H->n = ncol;
     finish_csc(nrow, ncol, col, row, val, &H->ptr, &H->idx, &H->val);
@@ -332,7 +345,7 @@ static int read_edgelist(const char* path, int base, HostMatrix* H, int* weighte
   }
   std::fclose(f);
   if (rc != GG_OK) return rc;
-  if ((int64_t)src.size() >= (1LL << 31)) return set_error(GG_ERR_ARGUMENT, "%s: too many edges", path);
+  if ((int64_t)src.size() >= (1LL << 31) - 1) return set_error(GG_ERR_ARGUMENT, "%s: too many edges", path);
   // adjacency A[u, v] for edge u -> v, as CSC (column v lists its in-neighbours u):
   // the CSR storage of A_T, the form every graph call takes
   H->m = nv;
@@ -424,6 +437,11 @@ static int read_mtx(const char* path, int expand, HostMatrix* H, int* kind_out) 
     }
     if (rc != GG_OK) break;
     if (got < nnz) { rc = set_error(GG_ERR_ARGUMENT, "%s: %lld of %lld entries", path, got, nnz); break; }
+    if ((int64_t)col.size() >= (1LL << 31) - 1) {
+      rc = set_error(GG_ERR_ARGUMENT, "%s: %lld entries after symmetric expansion do not fit Int32 indices",
+                     path, (long long)col.size());
+      break;
+    }
     H->m = m;
     H->n = n;
     finish_csc(m, n, col, row, val, &H->ptr, &H->idx, &H->val);

@@ -41,9 +41,10 @@ struct gg_multigraph {
   unsigned* visited = nullptr;
   int32_t* q[2] = {nullptr, nullptr};
   unsigned long long* ctr = nullptr;  // [3] rotating queue counters
-  unsigned* bar = nullptr;            // [4] barrier count, generation, error, levels
+  unsigned* bar = nullptr;  // [8] barrier count, generation, error, levels, poll limit
   int64_t* d_src = nullptr;           // [G] global source ids
   int32_t* dist_bound = nullptr;      // dist pointer captured in the graph
+  unsigned polls_set = 0;  // poll limit last written to bar[4] (0: none yet)
   cudaGraphExec_t gexec = nullptr;
   int grid = 0;
   // persistent shortest-path state (allocated on first use)
@@ -52,6 +53,18 @@ struct gg_multigraph {
   cudaGraphExec_t sssp_gexec = nullptr;
   int nonneg = -1;  // all stored values >= 0 (and not NaN)? -1: not yet checked
 };
+
+// the context's barrier poll limit into bar[4] (kept across launches: the captured
+// graphs clear bar[0..3] only)
+static int mg_set_polls(gg_ctx* ctx, gg_multigraph* M) {
+  const unsigned p = gg::barrier_polls(ctx);
+  if (M->polls_set != p) {
+    GG_CUDA(cudaMemcpyAsync(M->bar + 4, &p, sizeof(unsigned), cudaMemcpyHostToDevice, ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    M->polls_set = p;
+  }
+  return GG_OK;
+}
 
 namespace gg {
 
@@ -93,14 +106,16 @@ __device__ __forceinline__ bool mg_odd(const void* nz, int tv, int64_t k) {
   return false;
 }
 
-// grid-wide barrier for a cooperative launch; the wait gives up after a bounded
-// number of polls and records an error so that every block can return
+// grid-wide barrier for a cooperative launch; the wait gives up after bar[4] polls
+// (the context's limit, gg_set_wait_limit) and records an error so that every block
+// can return.  bar: arrivals, generation, error, levels / rounds done, poll limit.
 __device__ __forceinline__ bool mg_grid_sync(unsigned* bar, unsigned nblocks) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned* vgen = bar + 1;
     volatile unsigned* verr = bar + 2;
     const unsigned gen = *vgen;
+    const unsigned long long limit = bar[4];  // written by the host before each launch
     __threadfence();
     if (atomicAdd(bar, 1u) == nblocks - 1) {
       bar[0] = 0;
@@ -109,7 +124,7 @@ __device__ __forceinline__ bool mg_grid_sync(unsigned* bar, unsigned nblocks) {
     } else {
       unsigned long long polls = 0;
       while (*vgen == gen && *verr == 0) {
-        if (++polls > (1ull << 26)) {
+        if (++polls > limit) {
           atomicExch(bar + 2, 1u);
           break;
         }
@@ -405,7 +420,8 @@ int gg_multigraph_create(gg_ctx* ctx, const gg_mat* const* graphs, int64_t ngrap
   if (e == cudaSuccess) e = cudaMalloc((void**)&M->q[0], (M->total_n + 1) * sizeof(int32_t));
   if (e == cudaSuccess) e = cudaMalloc((void**)&M->q[1], (M->total_n + 1) * sizeof(int32_t));
   if (e == cudaSuccess) e = cudaMalloc((void**)&M->ctr, 4 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&M->bar, 4 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&M->bar, 8 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(M->bar, 0, 8 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMalloc((void**)&M->d_src, ngraphs * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
@@ -514,6 +530,7 @@ int gg_multigraph_bfs(gg_ctx* ctx, gg_multigraph* M, const int64_t* sources, int
     if (e != cudaSuccess) return cuda_error(e, "multigraph BFS graph capture");
     M->dist_bound = dist;
   }
+  GG_CHECK(mg_set_polls(ctx, M));
   GG_CUDA(cudaGraphLaunch(M->gexec, ctx->stream));
   unsigned hb[4] = {0, 0, 0, 0};
   GG_CUDA(cudaMemcpyAsync(hb, M->bar, sizeof(hb), cudaMemcpyDeviceToHost, ctx->stream));
@@ -611,6 +628,7 @@ int gg_multigraph_sssp(gg_ctx* ctx, gg_multigraph* M, const int64_t* sources, vo
       default: GG_CHECK(mg_sssp_capture<double>(ctx, M, static_cast<double*>(dist))); break;
     }
   }
+  GG_CHECK(mg_set_polls(ctx, M));
   GG_CUDA(cudaGraphLaunch(M->sssp_gexec, ctx->stream));
   unsigned hb[4] = {0, 0, 0, 0};
   GG_CUDA(cudaMemcpyAsync(hb, M->bar, sizeof(hb), cudaMemcpyDeviceToHost, ctx->stream));

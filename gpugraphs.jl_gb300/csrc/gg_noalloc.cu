@@ -14,8 +14,6 @@
 // rejected.  The search is bottom-up only (every level scans the unvisited
 // vertices' in-edges), so it needs neither the transposed graph nor any analysis,
 // and costs O(levels * (n + nnz)) work.
-#include <mutex>
-
 #include "gg_common.cuh"
 
 namespace gg {
@@ -26,21 +24,16 @@ static const int64_t kNoAllocWords = kNoAllocMaxN / 32;
 // [visited | frontier A | frontier B] bitmaps, then the level counter
 static __device__ __align__(256) unsigned g_noalloc_scratch[3 * kNoAllocWords + 64];
 
-// Host-side address of g_noalloc_scratch per device.  The symbol's name in host code
-// is only a stand-in, never a device address, so it is looked up on the device.
-static std::mutex g_noalloc_mu;
-static unsigned* g_noalloc_addr[256];
-
-static int noalloc_scratch(int dev, unsigned** out) {
-  if (dev < 0 || dev >= 256) return set_error(GG_ERR_ARGUMENT, "device ordinal %d out of range", dev);
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-    g_noalloc_addr[dev] = static_cast<unsigned*>(p);
-  }
-  *out = g_noalloc_addr[dev];
+// Device address of g_noalloc_scratch on the current device.  The symbol's name in
+// host code is only a stand-in, never a device address, so it is looked up through
+// the runtime -- on every call, with the caller's device current: the lookup
+// allocates nothing, and a cached address would go stale once cudaDeviceReset has
+// unloaded the module (it may load elsewhere afterwards).
+static int noalloc_scratch(unsigned** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+  *out = static_cast<unsigned*>(p);
   return GG_OK;
 }
 
@@ -113,7 +106,7 @@ extern "C" int gg_bfs_levels_noalloc(const int32_t* rowptr, const int32_t* colva
   int dev = 0;
   GG_CUDA(cudaGetDevice(&dev));
   unsigned* base = nullptr;
-  GG_CHECK(noalloc_scratch(dev, &base));
+  GG_CHECK(noalloc_scratch(&base));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int num_sms = 0;
   GG_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));

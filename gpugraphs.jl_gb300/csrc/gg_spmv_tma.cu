@@ -20,8 +20,10 @@
 // 512-byte bulk copies per stage and one wait per 4 columns cost more than the L1
 // work they remove.  It stays available as an autotuner candidate (sell_variant 1).
 //
-// Every wait on an mbarrier is bounded: after kTWaitPolls polls the kernel records a
-// timeout in `err`, waits (bounded again) for the copies it issued, and returns.
+// Every wait on an mbarrier is bounded: after `polls` polls (the context's limit) the
+// kernel records a timeout in `err`, waits for the copies it issued (bounded by the
+// built-in kTWaitPolls, whatever the context's limit, so that none is left in flight
+// when the CTA ends), and returns.
 #include "gg_semiring.cuh"
 #include "gg_tma.cuh"
 
@@ -59,7 +61,7 @@ __global__ void __launch_bounds__(kTW * 32, 1)
     k_sell_tma32(const float* __restrict__ nz, const float* __restrict__ xr, float* __restrict__ y,
                  const int32_t* __restrict__ colval, const int32_t* __restrict__ perm, int64_t m,
                  const int4* __restrict__ pitems, int64_t nitems, float* partials, int hot,
-                 unsigned* err) {
+                 unsigned* err, unsigned polls) {
   extern __shared__ __align__(128) unsigned char smem[];
   float* sx = reinterpret_cast<float*>(smem);
   int32_t* sbuf = reinterpret_cast<int32_t*>(smem + kTSmemHot);
@@ -122,7 +124,7 @@ __global__ void __launch_bounds__(kTW * 32, 1)
     const uint32_t parity = (uint32_t)((consumed / kTStages) & 1);
     unsigned ok = 0;
     if (lane == 0) {
-      for (unsigned p = 0; p < kTWaitPolls; ++p)
+      for (unsigned p = 0; p < polls; ++p)
         if (mbar_try_wait(wbar + 8 * slot, parity)) {
           ok = 1;
           break;
@@ -266,7 +268,7 @@ int launch_sell_tma(gg_ctx* ctx, gg_mat* A, const float* nzv, const float* xr, f
     const int tr = trace_main_begin(ctx);
     k_sell_tma32<<<ctx->num_sms, kTW * 32, kTSmem, ctx->stream>>>(
         nzv, xr, y, colval, A->sigma > 1 ? A->perm : nullptr, A->m, P->pitems, P->npitems,
-        static_cast<float*>(P->partials), hot, ctx->d_err);
+        static_cast<float*>(P->partials), hot, ctx->d_err, copy_polls(ctx));
     trace_main_end(ctx, tr);
     trace_count(ctx, 1);
   }

@@ -24,8 +24,8 @@
 // issues the copy of window j + 2 into the same buffer).  At the end of a unit the
 // pieces of every row are added in piece order, so every sum is formed in one fixed
 // order and repeated calls give identical results.  Every wait on a copy is bounded
-// (kWinPolls polls, then the error flag, a drain of the copies in flight and an
-// orderly return).  Sums differ from the storage-order fold by rounding only.
+// (the context's poll limit, by default kWinPolls; then the error flag, a drain of the
+// copies in flight bounded by kWinPolls whatever the limit, and an orderly return).  Sums differ from the storage-order fold by rounding only.
 #include <algorithm>
 #include <numeric>
 #include <queue>
@@ -45,8 +45,8 @@ static const int kWinDump = kWinRows - 1;  // accumulator slot of the padding en
 // smem: two windows | accumulators | counters, flag, copies issued | 2 mbarriers
 static const size_t kWinSmem = (size_t)2 * kWinCols * 4 + (size_t)kWinRows * 4 + 32 + 16;
 
-__device__ __forceinline__ bool win_wait(uint32_t bar, uint32_t parity) {
-  for (unsigned p = 0; p < kWinPolls; ++p)
+__device__ __forceinline__ bool win_wait(uint32_t bar, uint32_t parity, unsigned limit = kWinPolls) {
+  for (unsigned p = 0; p < limit; ++p)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(kWinThreads, 1)
                const int32_t* __restrict__ vptr, const int4* __restrict__ units,
                const int32_t* __restrict__ cta_ptr, const int32_t* __restrict__ cta_wptr,
                const int32_t* __restrict__ cta_win, const float* __restrict__ yt,
-               float* __restrict__ partials, unsigned* err) {
+               float* __restrict__ partials, unsigned* err, unsigned polls) {
   extern __shared__ __align__(128) unsigned char smem[];
   float* sw = reinterpret_cast<float*>(smem);
   float* acc = sw + 2 * kWinCols;
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kWinThreads, 1)
       const int32_t p0 = ws[s], p1 = ws[s + 1];
       {
         const int b = j & 1;
-        const bool ok = scnt[2] == 0 && win_wait(bar0 + 8 * b, (uint32_t)((j >> 1) & 1));
+        const bool ok = scnt[2] == 0 && win_wait(bar0 + 8 * b, (uint32_t)((j >> 1) & 1), polls);
         if (!ok) {
           if (lane == 0) {
             scnt[2] = 1;
@@ -856,7 +856,7 @@ int launch_spmv_win(gg_ctx* ctx, gg_mat* A, const float* x, float* y) {
                            P->tail->colval, false));
   k_spmv_win<<<P->grid, kWinThreads, kWinSmem, ctx->stream>>>(
       P->idx, P->val, P->xr, y, P->rowperm, P->tiles, P->segbase, P->wseg, P->vptr, P->units,
-      P->cta_ptr, P->cta_wptr, P->cta_win, P->yt, P->partials, ctx->d_err);
+      P->cta_ptr, P->cta_wptr, P->cta_win, P->yt, P->partials, ctx->d_err, copy_polls(ctx));
   trace_main_end(ctx, tr);
   trace_count(ctx, 1);
   if (P->nsplit > 0) {

@@ -18,7 +18,8 @@ from .errors import (ArgumentError, BoundsError, DimensionMismatch, GPUGraphsErr
                      SpmmAssertionError, UnsupportedError)
 from .ewise import gpu_apply_, gpu_ewise_, gpu_reduce
 from .fileio import RBData, read_edgelist, read_mtx, read_rb
-from .ops import gpu_spmm_, gpu_spmspv, gpu_spmspv_, gpu_spmv_, gpu_spmv_rows_, synchronize
+from .ops import (gpu_spmm_, gpu_spmspv, gpu_spmspv_, gpu_spmv_, gpu_spmv_rows_, set_wait_limit,
+                  synchronize)
 from .storage import (AbstractSparseGPUMatrix, SparseGPUMatrixCSC, SparseGPUMatrixCSR,
                       SparseGPUMatrixSELL, sprand_gpu)
 from .tuning import autotune, spmv_layout
@@ -29,6 +30,7 @@ __all__ = [
     "gpu_spmm_", "SparseGPUMatrixCSC", "SparseGPUVector", "gpu_spmspv_", "gpu_spmspv", "gpu_spmv_rows_",
     "gpu_ewise_", "gpu_apply_", "gpu_reduce", "RBData", "read_rb", "read_mtx", "read_edgelist", "sprand_gpu", "autotune", "spmv_layout", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
     "bfs_parents_", "shortest_path", "shortest_path_", "monoid_neutral", "monoid_absorb", "synchronize",
+    "set_wait_limit",
     "GPUGraphs_add", "GPUGraphs_safe_add", "GPUGraphs_mul", "GPUGraphs_second",
     "GPUGraphs_band", "GPUGraphs_bor", "GPUGraphs_any", "GPUGraphs_secondi", "GPUGraphs_max",
     "GPUGraphs_min", "GPUGraphs_first", "GPUGraphs_pair", "GPUGraphs_minus", "GPUGraphs_rminus",

@@ -26,6 +26,7 @@ SIGNATURES = {
     "gg_destroy": [P],
     "gg_set_stream": [P, P],
     "gg_stream_sync": [P],
+    "gg_set_wait_limit": [P, U64],
     "gg_trace_begin": [P],
     "gg_trace_end": [P, PI64, PI64, ctypes.POINTER(ctypes.c_double)],
     "gg_csr_create": [P, I64, I64, I64, P, P, P, I, I, PP],

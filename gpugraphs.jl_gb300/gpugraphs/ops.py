@@ -202,3 +202,12 @@ def synchronize(device=None):
     """KernelAbstractions.synchronize(backend) (test/spmv.jl:25)."""
     L = core.lib()
     check(L.gg_stream_sync(core.ctx(device)), L)
+
+
+def set_wait_limit(polls, device=None):
+    """Poll limit of the device-side waits of later calls on this device's context
+    (grid barriers of the persistent searches, bulk-copy waits of the staged SpMV
+    kernels); 0 restores the built-in limits.  A wait that runs out makes the call
+    raise TimeoutError_ and leaves the context usable."""
+    L = core.lib()
+    check(L.gg_set_wait_limit(core.ctx(device), int(polls)), L)

@@ -116,6 +116,18 @@ int gg_set_stream(gg_ctx* ctx, void* stream);
 /* Replaces KernelAbstractions.synchronize(backend) (test/spmv.jl:25). */
 int gg_stream_sync(gg_ctx* ctx);
 
+/* Poll limit of the bounded device-side waits of this context's later calls (no
+ * reference counterpart: the reference's host loops wait on nothing on the device).
+ * It bounds the grid barriers of the persistent kernels (cooperative BFS and
+ * shortest-path phases of hub-free graphs, the near-far search, the many-graph BFS /
+ * shortest paths; each poll sleeps ~100 ns) and the bulk-copy waits of the staged
+ * SpMV kernels.  A wait that runs out records an error; every block returns, and the
+ * call (or, for asynchronous SpMV calls, the next gg_stream_sync) returns
+ * GG_ERR_TIMEOUT with partial results.  The context stays usable.  polls = 0
+ * restores the built-in limits (2^26 barrier polls, about 7 s; 2^22 copy polls);
+ * values above 2^32 - 1 are clamped. */
+int gg_set_wait_limit(gg_ctx* ctx, uint64_t polls);
+
 /* Launch tracing (no reference counterpart).  Between gg_trace_begin and
  * gg_trace_end, the kernel launches of gg_spmv / gg_spmm calls on this context are
  * counted, and the main kernel of each call (the one that streams the matrix) is
@@ -398,8 +410,10 @@ int gg_sssp_batch(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, int64_
  * device, on `stream` (NULL = legacy default stream).  Calls no cudaMalloc /
  * cudaFree: its working state lives in a fixed array of the library sized for at
  * most 4,194,304 vertices (1.5 MiB, held by every GPU that loads the library until
- * exit); larger n returns GG_ERR_ARGUMENT.  The first call on a device looks up that
- * array's device address, so make it before any stream capture.  All calls share
+ * exit); larger n returns GG_ERR_ARGUMENT.  Every call looks up that array's device
+ * address on the current device (the lookup allocates nothing); the first call on a
+ * device also loads the library's device code there, so make it before any stream
+ * capture.  All calls share
  * the one array: calls whose work overlaps on the GPU race and must be ordered by
  * the caller.  Bottom-up only: O(levels * (n + nnz)) work.  The CSR arrays are not
  * validated.  Synchronous.

@@ -111,6 +111,7 @@ def test_null_handles_are_argument_errors(libpath):
         L.gg_read_mtx(None, 1, None, None, None, None, None, None, None),
         L.gg_read_edgelist(None, 1, None, None, None, None, None, None),
         L.gg_mat_values_changed(None, None),
+        L.gg_set_wait_limit(None, 5),
     ]
     for rc in cases:
         assert rc == ARG

@@ -94,6 +94,11 @@ def test_rb_skew_and_errors(tmp_path):
     (tmp_path / "b.rb").write_text(bad)
     with pytest.raises(G.ArgumentError):
         fileio.read_rb(str(tmp_path / "b.rb"))
+    # a middle pointer far beyond nnz + 1: rejected before any entry is read through it
+    far = txt.replace("  1  3  3  3", "  1999  3  3")
+    (tmp_path / "f.rb").write_text(far)
+    with pytest.raises(G.ArgumentError, match="column pointers"):
+        fileio.read_rb(str(tmp_path / "f.rb"))
 
 
 def test_edgelist_to_transposed_adjacency(tmp_path):
