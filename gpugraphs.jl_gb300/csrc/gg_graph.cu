@@ -49,11 +49,15 @@ struct GraphAux {
   PushCSR push[3];       // 0: odd-valued edges, 1: all edges, 2: all edges + weights
   int64_t max_in_deg = -1;  // largest row of the view (-1: not computed yet)
   double avg_w = -1.0;      // mean stored weight in the distance type (-1: not yet)
+  // shortest-path pull rounds of large CSR handles: SELL-32 copy of A_T with rows
+  // sorted by length (coalesced column / weight loads, a lane per row)
+  gg_mat* pull_sell = nullptr;
 };
 
 void free_graph_aux(gg_mat* A) {
   GraphAux* g = A->aux;
   if (!g) return;
+  if (g->pull_sell) gg_mat_destroy(g->pull_sell);
   if (g->owns_view) {
     cudaFree(g->vrowptr);
     cudaFree(g->vcolval);
@@ -1322,6 +1326,8 @@ template <> __device__ __forceinline__ double atomic_min_t<double>(double* p, do
 }
 
 template <typename T> __device__ __forceinline__ T ld_cg(const T* p) { return __ldcg(p); }
+// coherent-cached load (ld.global.ca): may return a value another SM has since lowered
+template <typename T> __device__ __forceinline__ T ld_l1(const T* p) { return __ldca(p); }
 
 // safe_add on non-negative, non-NaN operands (algebra.jl:47-48)
 template <typename T> __device__ __forceinline__ T relax_add(T w, T d) {
@@ -2042,6 +2048,124 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Pull round over the SELL-32 copy of A_T (rows sorted by length, slice-column-major):
+// one warp per work item of the copy's plan (a chunk of <= 128 columns of a slice, or
+// a group of narrow slices), lane = stored row, so every column / weight load of a
+// warp is one 128-byte line.  Each row takes the minimum of w + dist[u] over all its
+// in-edges of the item (an in-edge whose source did not change cannot improve it, so
+// no membership test is made) and lowers dist[v] with an atomic min (the chunks of a
+// long row race only through that min).  Improved vertices join the next frontier
+// once (bitmap inq_next) with their out-degrees counted.  Distances are gathered
+// through L1 (a value lowered by another SM may be seen late: any distance read is an
+// upper bound of the fixpoint, and a vertex lowered in this round joins the next
+// frontier, so any order reaches the same fixpoint) and lowered in place.
+// ---------------------------------------------------------------------------------
+static const int kPullSellThreads = 512;
+// a round pulls when the frontier's out-edges exceed nnz / kPullSellDiv
+static const int64_t kPullSellDiv = 16;
+
+template <typename T>
+__device__ __forceinline__ void pull_lower(int64_t srow, int64_t m, const int32_t* __restrict__ perm,
+                                           T cand, T* dist, unsigned* inq_next, int32_t* qn,
+                                           Counters* ctr, const int32_t* __restrict__ prow) {
+  bool improved = false;
+  int32_t v = 0, deg = 0;
+  if (srow < m && cand != Lim<T>::max()) {
+    v = __ldg(perm + srow) - 1;
+    if (cand < ld_cg(dist + v)) {
+      const T old = atomic_min_t(dist + v, cand);
+      if (cand < old) {
+        const unsigned bit = 1u << (v & 31);
+        improved = !(atomicOr(inq_next + (v >> 5), bit) & bit);
+        if (improved) deg = __ldg(prow + v + 1) - __ldg(prow + v);
+      }
+    }
+  }
+  warp_append(improved, v, deg, qn, ctr);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPullSellThreads)
+    k_sssp_pull_sell(const int32_t* __restrict__ colval, const void* __restrict__ nz, int tv,
+                     const int32_t* __restrict__ perm, int64_t m, const int4* __restrict__ pitems,
+                     int64_t nitems, T* dist, unsigned* inq_next, int32_t* qn, Counters* ctr,
+                     const int32_t* __restrict__ prow) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int4 dn = gw < nitems ? __ldg(pitems + gw) : make_int4(0, 0, 0, -1);
+  for (int64_t it = gw; it < nitems; it += nw) {
+    const int4 d = dn;  // first position, first stored row, columns (or -slices), partial
+    if (it + nw < nitems) dn = __ldg(pitems + it + nw);
+    if (d.z < 0) {
+      // group of -d.z narrow slices (widths in 4-bit fields of d.w), <= 8 columns in all
+      const int ns = -d.z;
+      const uint32_t widths = (uint32_t)d.w;
+      int total = 0;
+      for (int t = 0; t < ns; ++t) total += (widths >> (4 * t)) & 15u;
+      T c[kNarrowCols];
+#pragma unroll
+      for (int u = 0; u < kNarrowCols; ++u) {
+        c[u] = Lim<T>::max();
+        if (u < total) {
+          const int32_t col = __ldg(colval + d.x + u * 32 + lane);
+          if (col > 0)
+            c[u] = relax_add(view_weight<T>(nz, tv, (int64_t)d.x + u * 32 + lane), ld_l1(dist + (col - 1)));
+        }
+      }
+      int u0 = 0;
+      for (int t = 0; t < ns; ++t) {
+        const int w = (int)((widths >> (4 * t)) & 15u);
+        T best = Lim<T>::max();
+#pragma unroll
+        for (int u = 0; u < kNarrowCols; ++u)
+          if (u >= u0 && u < u0 + w && c[u] < best) best = c[u];
+        u0 += w;
+        pull_lower(d.y + t * 32 + lane, m, perm, best, dist, inq_next, qn, ctr, prow);
+      }
+      continue;
+    }
+    const int64_t srow = (int64_t)d.y + lane;
+    T best = Lim<T>::max();
+    if (srow < m) {
+      for (int32_t j = 0; j < d.z; j += 8) {
+        int32_t col[8];
+        T w[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int64_t pos = (int64_t)d.x + lane + (int64_t)(j + u) * 32;
+          col[u] = j + u < d.z ? __ldg(colval + pos) : -1;
+          w[u] = j + u < d.z ? view_weight<T>(nz, tv, pos) : Lim<T>::max();
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (col[u] > 0) {
+            const T cand = relax_add(w[u], ld_l1(dist + (col[u] - 1)));
+            best = cand < best ? cand : best;
+          }
+        }
+      }
+    }
+    pull_lower(srow, m, perm, best, dist, inq_next, qn, ctr, prow);
+  }
+}
+
+// the SELL-32 copy (rows sorted by length) and its work plan, built on first use
+static int ensure_pull_sell(gg_ctx* ctx, gg_mat* A) {
+  GraphAux* g = A->aux;
+  if (g->pull_sell) return GG_OK;
+  gg_mat* S = nullptr;
+  GG_CHECK(gg_sell_create(ctx, A, 32, A->m, &S));
+  int rc = build_sell_plan(ctx, S);
+  if (rc != GG_OK) {
+    gg_mat_destroy(S);
+    return rc;
+  }
+  g->pull_sell = S;
+  return GG_OK;
+}
+
 template <typename T>
 static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
   GG_CHECK(ensure_push(ctx, A, 2));
@@ -2116,6 +2240,8 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
   }
   const int32_t small_cap = coop_ok ? kCoopLo : kSmallCap;
   const long long coop_hi = n / 8 > kCoopLo ? n / 8 : kCoopLo;
+  // large CSR handles pull over a SELL-32 copy (built at the first pull round)
+  const bool sell_pull = A->format == GG_FMT_CSR && n >= (1 << 16);
   while (nf > 0) {
     if (rounds > max_rounds) return set_error(GG_ERR_NOT_CONVERGED, "shortest_path did not converge");
     if (coop_ok && nf > small_cap && nf <= coop_hi && mf * 8 <= P.nnz) {
@@ -2166,7 +2292,27 @@ static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
     }
     ++rounds;
     GG_CUDA(cudaMemsetAsync(sc.ctr, 0, sizeof(Counters), ctx->stream));
-    if (mf * 4 > P.nnz) {
+    if (sell_pull && mf * kPullSellDiv > P.nnz) {
+      // large frontier: pull round over the SELL-32 copy, every in-edge
+      GG_CHECK(ensure_pull_sell(ctx, A));
+      const gg_mat* S = g->pull_sell;
+      const SellPlan* SP = S->sellplan;
+      if (SP->npitems > 0)
+        k_sssp_pull_sell<T><<<ctx->num_sms * (2048 / kPullSellThreads), kPullSellThreads, 0,
+                              ctx->stream>>>(S->colval, S->nzval, S->dtype, S->perm, S->m,
+                                             SP->pitems, SP->npitems, d, sc.fb[cur ^ 1],
+                                             sc.q[cur ^ 1], sc.ctr, P.rowptr);
+      // the consumed membership bitmap becomes the next round's target: clear it
+      GG_CUDA(cudaMemsetAsync(sc.fb[cur], 0, ((n + 31) / 32) * sizeof(unsigned), ctx->stream));
+      GG_CUDA(cudaGetLastError());
+      GG_CUDA(cudaMemcpyAsync(h, sc.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+      GG_CUDA(cudaStreamSynchronize(ctx->stream));
+      nf = (int64_t)h->nf;
+      mf = (int64_t)h->mf;
+      cur ^= 1;
+      continue;
+    }
+    if (!sell_pull && mf * 4 > P.nnz) {
       // large frontier: pull round (no atomics on the common path)
       k_sssp_pull<T><<<gridsz(ctx, n), 256, 0, ctx->stream>>>(
           n, g->vrowptr, g->vcolval, g->vnz, A->dtype, sc.fb[cur], d, sc.fb[cur ^ 1], sc.q[cur ^ 1],

@@ -177,6 +177,12 @@ __device__ __forceinline__ float4 ld_keep4(const float* p, uint64_t pol) {
   return r;
 }
 
+__device__ __forceinline__ void st_hint4(float* p, const float4& v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1,%2,%3,%4}, %5;" ::"l"(p), "f"(v.x),
+               "f"(v.y), "f"(v.z), "f"(v.w), "l"(pol)
+               : "memory");
+}
+
 // ---------------------------------------------------------------------------------
 // (GPUGraphs_mul, GPUGraphs_add, GPUGraphs_second) on Float32: the headline SpMV.
 // The early exit at +Inf follows monoid_absorb(Float32, GPUGraphs_add) (algebra.jl:45).

@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(256)
       }
       if (acc.x != acc.x || acc.y != acc.y || acc.z != acc.z || acc.w != acc.w)
         acc = spmm_refold4(acc, colval, nz, B + j, ldb, k0, k1);
-      *reinterpret_cast<float4*>(C + r * ldc + j) = acc;
+      st_hint4(C + r * ldc + j, acc, pol_s);
     }
   }
 }
@@ -368,7 +368,8 @@ __global__ void __launch_bounds__(256)
       if (acc.x != acc.x || acc.y != acc.y || acc.z != acc.z || acc.w != acc.w)
         acc = spmm_refold4(acc, colval, nz, Bj, ldb, d.y, d.z);
       float* out = d.w < 0 ? C + (int64_t)d.x * ldc + jlo + jj : partials + (int64_t)d.w * jn + jj;
-      *reinterpret_cast<float4*>(out) = acc;
+      if (d.w < 0) st_hint4(out, acc, pol_s);
+      else *reinterpret_cast<float4*>(out) = acc;
     }
   }
 }

@@ -23,7 +23,8 @@ export AbstractSparseGPUMatrix, SparseGPUMatrixCSR, SparseGPUMatrixSELL, gpu_spm
        sprand_gpu, monoid_neutral, monoid_absorb, bfs_distances, bfs_distances!, bfs_parents,
        bfs_parents!, shortest_path, shortest_path!, GPUGraphs_add, GPUGraphs_safe_add,
        GPUGraphs_mul, GPUGraphs_second, GPUGraphs_band, GPUGraphs_bor, GPUGraphs_any,
-       GPUGraphs_secondi, GPUGraphs_max, GPUGraphs_min, SparseGPUVector, SparseGPUMatrixCSC,
+       GPUGraphs_secondi, GPUGraphs_max, GPUGraphs_min, SparseGPUVector, AbstractSparseGPUVector,
+       SparseGPUMatrixCSC,
        gpu_spmspv!, gpu_spmspv, gpu_spmv_rows!, gpu_ewise!, gpu_apply!, gpu_reduce, read_rb,
        read_mtx, read_edgelist
 
@@ -356,7 +357,9 @@ shortest_path!(A_T::AbstractSparseGPUMatrix, sources::AbstractVector{<:Integer},
 # kernel (src/spmv/CSR.jl:90-115), CSC SpMV (src/spmv/CSC.jl) and the e-wise /
 # map-reduce steps the reference leaves to broadcasts
 # ---------------------------------------------------------------------------------
-mutable struct SparseGPUVector{Tv,Ti<:Integer}
+abstract type AbstractSparseGPUVector{Tv,Ti<:Integer} <: SparseArrays.AbstractSparseVector{Tv,Ti} end
+
+mutable struct SparseGPUVector{Tv,Ti<:Integer} <: AbstractSparseGPUVector{Tv,Ti}
     n::Int
     nzind::CuVector{Ti}
     nzval::CuVector{Tv}
@@ -374,6 +377,11 @@ function SparseGPUVector(v::Vector{Tv}, backend = nothing) where {Tv}
     nzind = findall(!iszero, v)
     return SparseGPUVector(length(v), nzind, v[nzind])
 end
+Base.size(V::AbstractSparseGPUVector) = (V.n,)
+Base.length(V::AbstractSparseGPUVector) = V.n
+SparseArrays.nnz(V::AbstractSparseGPUVector) = length(V.nzval)
+SparseArrays.nonzeroinds(V::AbstractSparseGPUVector) = V.nzind
+SparseArrays.nonzeros(V::AbstractSparseGPUVector) = V.nzval
 
 """
     gpu_spmspv!(C, A, B::SparseGPUVector; mul, add, accum) -> rows

@@ -201,6 +201,13 @@ int gg_mat_values_changed(gg_ctx* ctx, gg_mat* A);
  * any_dense_masked_csr_spmv_kernel! does (src/spmv/CSR.jl:147-171), and rows without
  * such a column are not written.  Checks of _validate_args (src/spmv/CSR.jl:358-408)
  * return GG_ERR_DIMENSION / GG_ERR_TYPE.
+ * Device memory: the first call of a kind builds its analysis on the handle, kept until
+ * gg_mat_destroy or gg_mat_values_changed.  The first plus-times Float32 call on a CSR
+ * handle of at least 65536 rows builds a SELL-32 copy of the matrix with rows sorted by
+ * length and relabelled columns: about 12 bytes per stored entry plus 16 per row, i.e.
+ * more than the CSR itself (about 1.6 GB at R-MAT scale 22, 6.5 GB at scale 24).  Other
+ * first calls add row-block descriptors (16 bytes per block of up to 256 entries).
+ * Later calls allocate nothing and are asynchronous.
  */
 int gg_spmv(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* y, int y_dtype,
             int64_t y_len, const void* x, int x_dtype, int64_t x_len, const void* mask,
@@ -250,9 +257,10 @@ int gg_spmspv(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* y
  *     y[j] = accum(y[j], add over the rows i of A holding column j, ascending, of
  *                        mul(A[i, j], x[i], j, i, i, 1))
  * with the absorb early exit, i.e. gg_spmv over the CSR storage of A', which the first
- * call builds on the handle (stable radix sort of the column ids).  x_len must be m,
- * y_len n; errors as gg_spmv; GG_ERR_UNSUPPORTED for a SELL handle.  Asynchronous
- * after the first call.
+ * call builds on the handle (stable radix sort of the column ids): a second matrix of
+ * 4(n+1) + 8 nnz bytes kept until gg_mat_destroy or gg_mat_values_changed, plus what
+ * gg_spmv builds on it.  x_len must be m, y_len n; errors as gg_spmv;
+ * GG_ERR_UNSUPPORTED for a SELL handle.  Asynchronous after the first call.
  */
 int gg_spmv_t(gg_ctx* ctx, const gg_mat* A, int mul, int add, int accum, void* y, int y_dtype,
               int64_t y_len, const void* x, int x_dtype, int64_t x_len, const void* mask,

@@ -6,6 +6,8 @@
   nzval with -1 / 0 padding).
 * csr_errors.json -- the constructor cases the reference expects to throw
   ArgumentError, transcribed from test/structs.jl:79-149.
+* reference_exports.json -- the names the reference module exports
+  (src/GPUGraphs.jl:25-51), which the Julia drop-in must export too.
 * graphs.npz -- the reference's BFS / shortest-path test graphs rebuilt with the same
   generator families (test/bfs.jl:11-12, test/shortest_path.jl:10-29):
   Barabasi-Albert(30, 3) and Dorogovtsev-Mendes(30), seeded, plus integer weights
@@ -91,9 +93,28 @@ def graphs():
     return out
 
 
+def reference_exports():
+    """The names GPUGraphs.jl exports (src/GPUGraphs.jl:25-51), transcribed: the drop-in
+    module must export every one of them."""
+    return {
+        "source": "GPUGraphs.jl src/GPUGraphs.jl:25-51",
+        "exports": [
+            "AbstractSparseGPUMatrix", "SparseGPUMatrixCSR", "SparseGPUMatrixCSC",
+            "SparseGPUMatrixSELL", "SparseGPUVector", "AbstractSparseGPUVector", "gpu_spmv!",
+            "gpu_spmm!", "sprand_gpu", "monoid_neutral", "monoid_absorb", "bfs_distances",
+            "bfs_distances!", "bfs_parents", "bfs_parents!", "shortest_path", "shortest_path!",
+            "GPUGraphs_add", "GPUGraphs_safe_add", "GPUGraphs_mul", "GPUGraphs_second",
+            "GPUGraphs_band", "GPUGraphs_bor", "GPUGraphs_any", "GPUGraphs_secondi",
+            "GPUGraphs_max", "GPUGraphs_min",
+        ],
+    }
+
+
 def main():
     with open(os.path.join(HERE, "sell_4x4.json"), "w") as f:
         json.dump(sell_4x4(), f, indent=1)
+    with open(os.path.join(HERE, "reference_exports.json"), "w") as f:
+        json.dump(reference_exports(), f, indent=1)
     with open(os.path.join(HERE, "csr_errors.json"), "w") as f:
         json.dump(csr_errors(), f, indent=1)
     np.savez_compressed(os.path.join(HERE, "graphs.npz"), **graphs())

@@ -275,3 +275,20 @@ def test_grid_persistent_paths_exact(wkind):
     for s in (1, 40000):
         lv, _ = O.bfs_levels(A.n, pr, pc, pn, s)
         assert (host(G.bfs_distances(P, s)) == lv).all(), s
+
+
+@pytest.mark.parametrize("wkind,directed", [(gen.W_INT_1_255, False), (gen.W_U01_F32, False),
+                                            (gen.W_INT_1_255, True)])
+def test_sssp_large_csr_pull_rounds(wkind, directed):
+    """CSR handles of >= 65536 rows run their pull rounds over a SELL-32 copy (every
+    in-edge, atomic min, in place); distances equal Dijkstra's bit for bit (Int32 and
+    Float32 weights; a directed R-MAT whose A_T differs from A), two sources each."""
+    A = gen.rmat(17, 16, seed=41, wkind=wkind, symmetrize=not directed, drop_loops=not directed)
+    rp, cv, nz = csr_host(A)
+    n = A.n
+    deg = np.diff(rp)
+    for s in (int(np.argmax(deg)) + 1, int(np.flatnonzero(deg > 0)[len(deg) // 3]) + 1):
+        d = host(G.shortest_path(A, s))
+        ref = O.sssp_dijkstra(n, rp, cv, nz, s, symmetric=not directed)
+        assert d.dtype == ref.dtype
+        assert np.array_equal(d.view(np.int32), ref.view(np.int32))

@@ -74,3 +74,25 @@ def test_every_ccall_matches_the_header():
         assert name in decl, name
         assert ntypes == decl[name], (name, ntypes, decl[name])
         assert nargs == ntypes, (name, nargs, ntypes)
+
+
+def julia_exports():
+    src = open(JULIA).read()
+    m = re.search(r"^export\s+(.*?)(?:\n\s*\n|\n#)", src, re.M | re.S)
+    assert m, "no export statement"
+    return {x.strip() for x in m.group(1).replace("\n", " ").split(",") if x.strip()}
+
+
+def test_module_exports_every_reference_name():
+    """The drop-in module exports every name the reference's module exports
+    (tests/golden/reference_exports.json, transcribed from src/GPUGraphs.jl:25-51),
+    and defines each exported type."""
+    import json
+    ref = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_exports.json")))
+    exported = julia_exports()
+    missing = [n for n in ref["exports"] if n not in exported]
+    assert not missing, missing
+    src = open(JULIA).read()
+    for name in ref["exports"]:
+        if name[0].isupper() and not name.startswith("GPUGraphs_"):
+            assert re.search(r"(struct|abstract type)\s+%s\b" % re.escape(name), src), name
