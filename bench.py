@@ -877,6 +877,8 @@ class ServeMix:
                    for g in self.flts}
         self.rng = np.random.default_rng(9)
 
+    KINDS = ("bfs", "sssp", "spmv_x20")
+
     def draw(self):
         rng = self.rng
         kind = int(rng.integers(0, 3))
@@ -898,6 +900,7 @@ class ServeMix:
                 _single(G, self.graphs, self.xs, kind, g, 1)
         torch.cuda.synchronize()
         lat = []
+        self.plain_kinds = []
         t0 = time.perf_counter()
         for _ in range(nq):
             kind, g, s = self.draw()
@@ -905,6 +908,7 @@ class ServeMix:
             _single(G, self.graphs, self.xs, kind, g, s)
             torch.cuda.synchronize()
             lat.append(time.perf_counter() - t1)
+            self.plain_kinds.append(kind)
         return nq / (time.perf_counter() - t0), lat
 
     def poisson(self, srv, ids, lam, nreq):
@@ -915,23 +919,31 @@ class ServeMix:
         reqs = [self.draw() for _ in range(nreq)]
         t_start = time.perf_counter()
         t_next = t_start
+        kind_of = {}
         for i, (kind, g, s) in enumerate(reqs):
             t_next += gaps[i]
             while time.perf_counter() < t_next:
                 pass
             if kind == 0:
-                srv.submit_bfs(ids[g], s)
+                rid = srv.submit_bfs(ids[g], s)
             elif kind == 1:
-                srv.submit_sssp(ids[g], s)
+                rid = srv.submit_sssp(ids[g], s)
             else:
-                srv.submit_spmv_iter(ids[g], self.xs[g], steps=20)
+                rid = srv.submit_spmv_iter(ids[g], self.xs[g], steps=20)
+            kind_of[rid] = kind
         t_sub = time.perf_counter() - t_start
         done = srv.wait(timeout=600)
         t_all = time.perf_counter() - t_start
         lat = np.array(sorted(v[1] for v in done.values()))
+        per_kind = {}
+        for k, name in enumerate(self.KINDS):
+            lk = np.array([v[1] for r, v in done.items() if kind_of.get(r) == k])
+            if len(lk):
+                per_kind[name] = {"n": int(len(lk)), "p50_ms": round(float(np.percentile(lk, 50)) * 1e3, 3),
+                                  "p99_ms": round(float(np.percentile(lk, 99)) * 1e3, 3)}
         return {"lambda": lam, "requests": nreq, "offered_qps": round(nreq / t_sub, 1),
                 "qps": round(nreq / t_all, 1), "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
-                "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3)}
+                "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3), "per_kind": per_kind}
 
 
 def serve_summary(device):
@@ -941,14 +953,17 @@ def serve_summary(device):
     from gpugraphs.serving import Server
     t0 = time.time()
     mix = ServeMix(device)
-    plain_qps, pl = mix.plain(30)
+    plain_qps, pl = mix.plain(60)
     srv = Server(reserve_bytes=1 << 30, device=device.index or 0)
     ids = [srv.add_graph(A) for A in mix.graphs]
     low = mix.poisson(srv, ids, 1e2, 200)
     high = mix.poisson(srv, ids, 1e4, 2000)
     srv.close()
     pl = np.array(pl)
-    return {"lambda_1e2": low, "lambda_1e4": high,
+    pk = np.array(mix.plain_kinds)
+    plain_kind = {name: round(float(np.percentile(pl[pk == k], 50)) * 1e3, 3)
+                  for k, name in enumerate(mix.KINDS) if (pk == k).any()}
+    return {"lambda_1e2": low, "lambda_1e4": high, "plain_p50_ms_per_kind": plain_kind,
             "best_qps": max(low["qps"], high["qps"]),
             "plain": {"qps": round(plain_qps, 1), "p50_ms": round(float(np.percentile(pl, 50)) * 1e3, 3),
                       "p99_ms": round(float(np.percentile(pl, 99)) * 1e3, 3)},

@@ -215,6 +215,8 @@ static void free_derived(gg_mat* A) {
     cudaFree(A->sellplan->pitems);
     cudaFree(A->sellplan->narrow);
     cudaFree(A->sellplan->wide);
+    cudaFree(A->sellplan->pitems256);
+    cudaFree(A->sellplan->multi256);
     delete A->sellplan;
     A->sellplan = nullptr;
   }

@@ -347,6 +347,12 @@ struct SellPlan {
   int4* narrow = nullptr;
   int4* wide = nullptr;
   int64_t nnarrow = 0, nwide = 0;
+  // the same warp items with chunks of kSegMM columns (the pieces of the SpMM fold)
+  // for the one-column plus-times SpMM; multi256: (first stored row, first partial,
+  // chunks) of the slices cut into several chunks; built on first use
+  int4* pitems256 = nullptr;
+  int4* multi256 = nullptr;
+  int64_t npitems256 = -1, nmulti256 = 0, npart256 = 0;
 };
 static const int kNarrowChunks = 8;
 static const int kNarrowCols = 8;
@@ -557,6 +563,7 @@ int spmv_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, v
                   const void* x, int tx, const void* mask, int tmask, int64_t lo, int64_t hi);
 int build_row_blocks(gg_ctx* ctx, gg_mat* A);
 int build_sell_plan(gg_ctx* ctx, gg_mat* A);
+int launch_col1_sell(gg_ctx* ctx, gg_mat* A, const float* x, float* y);  // gg_spmv.cu
 int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n);  // gg_batch.cu
 int launch_sell_tma(gg_ctx* ctx, gg_mat* A, const float* nzv, const float* xr, float* y,
                     const int32_t* colval);  // gg_spmv_tma.cu

@@ -2166,6 +2166,26 @@ static int ensure_pull_sell(gg_ctx* ctx, gg_mat* A) {
   return GG_OK;
 }
 
+// Builds, ahead of any concurrent use, every analysis a shortest-path search of A may
+// build on first use: the out-edge view with weights, the hub plan and (large CSR
+// handles) the SELL-32 copy of the pull rounds.  The serving loop calls it when a
+// graph is added, so concurrent searches only read these structures.
+int sssp_prepare(gg_ctx* ctx, gg_mat* A) {
+  GG_CHECK(ensure_push(ctx, A, 2));
+  GraphAux* g = A->aux;
+  if (g->max_in_deg < 0) {
+    GG_CUDA(cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned), ctx->stream));
+    k_max_deg<<<gridsz(ctx, A->m), 256, 0, ctx->stream>>>(A->m, g->vrowptr, ctx->d_flags);
+    GG_CUDA(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    g->max_in_deg = ctx->h_flags[0];
+  }
+  if (g->max_in_deg > 32) GG_CHECK(build_hub_plan(ctx, A, g->vrowptr, A->m));
+  if (A->format == GG_FMT_CSR && A->m >= (1 << 16)) GG_CHECK(ensure_pull_sell(ctx, A));
+  return GG_OK;
+}
+
 template <typename T>
 static int sssp_fixpoint(gg_ctx* ctx, gg_mat* A, T* d, int64_t* rounds_out) {
   GG_CHECK(ensure_push(ctx, A, 2));

@@ -24,6 +24,7 @@ int graph_view(gg_ctx* ctx, gg_mat* A, const int32_t** rp, const int32_t** cv, c
                bool* all_odd, bool* nonneg);  // gg_graph.cu
 int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n);  // gg_batch.cu
 int push_view(gg_ctx* ctx, gg_mat* A, const int32_t** prow, const int32_t** pcol);  // gg_graph.cu
+int sssp_prepare(gg_ctx* ctx, gg_mat* A);  // gg_graph.cu
 
 namespace {
 

@@ -216,6 +216,9 @@ struct gg_server {
   };
   std::vector<std::thread> solo_threads;
   std::vector<gg_ctx*> solo_ctx;
+  // each worker's two streams: highest priority for short queries (BFS, and every
+  // query on graphs below 2^20 vertices), lowest for long searches and iterations
+  std::vector<cudaStream_t> solo_hi, solo_lo;
   std::deque<SoloJob> solo_q;
   std::condition_variable solo_cv;
   int solo_idle = 0;
@@ -585,9 +588,12 @@ static const int kSoloWorkers = 4;
 
 // one request through the single-query engines (the plain per-query path); SpMV
 // iterations use the one-column SpMM so that they fold exactly like an executor slot
-static int solo_run(gg_server* S, gg_ctx* c, const Request& r) {
+static int solo_run(gg_server* S, int w, const Request& r) {
+  gg_ctx* c = S->solo_ctx[w];
   gg_mat* A = S->graphs[r.graph];
   const int64_t n = A->m;
+  const bool short_query = r.kind == GG_QUERY_BFS || n < (int64_t(1) << 20);
+  c->stream = short_query ? S->solo_hi[w] : S->solo_lo[w];
   if (r.kind == GG_QUERY_BFS) {
     // bfs_distances: typemax(Int32) for every vertex the search does not reach
     int32_t* out = static_cast<int32_t*>(r.out);
@@ -629,7 +635,7 @@ static void solo_loop(gg_server* S, int w) {
       job = S->solo_q.front();
       S->solo_q.pop_front();
     }
-    const int rc = solo_run(S, c, job.req);
+    const int rc = solo_run(S, w, job.req);
     const double t = now_s();
     std::string msg = rc ? gg_last_error() : "";
     {
@@ -799,19 +805,26 @@ int gg_server_create(gg_ctx* ctx, int64_t reserve_bytes, gg_server** out) {
     delete S;
     return cuda_error(e, "gg_server_create");
   }
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
   for (int w = 0; w < kSoloWorkers; ++w) {
     gg_ctx* c = nullptr;
     int rc = gg_init(ctx->device, &c);
-    cudaStream_t st = nullptr;
-    if (rc == GG_OK && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+    cudaStream_t hi = nullptr, lo = nullptr;
+    if (rc == GG_OK &&
+        (cudaStreamCreateWithPriority(&hi, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+         cudaStreamCreateWithPriority(&lo, cudaStreamNonBlocking, least) != cudaSuccess))
       rc = set_error(GG_ERR_CUDA, "solo worker stream");
-    if (rc == GG_OK) rc = gg_set_stream(c, st);
+    if (rc == GG_OK) rc = gg_set_stream(c, hi);
     if (rc != GG_OK) {
       if (c) gg_destroy(c);
-      if (st) cudaStreamDestroy(st);
+      if (hi) cudaStreamDestroy(hi);
+      if (lo) cudaStreamDestroy(lo);
       break;  // fewer solo workers; batching alone still serves every request
     }
     S->solo_ctx.push_back(c);
+    S->solo_hi.push_back(hi);
+    S->solo_lo.push_back(lo);
   }
   *out = S;
   return GG_OK;
@@ -845,8 +858,29 @@ int gg_server_add_graph(gg_server* S, const gg_mat* A_T, int* graph_id) {
       rc = gg_bfs_levels(&S->own, A, 1, static_cast<int32_t*>(tmp), n, nullptr);
     if (rc == GG_OK && nonneg && n > 0) {
       const int64_t one = 1;
-      rc = gg_sssp(&S->own, A, &one, 1, tmp, nullptr, A->dtype == GG_BOOL ? GG_INT32 : A->dtype, n,
-                   nullptr);
+      rc = sssp_prepare(&S->own, A);
+      if (rc == GG_OK)
+        rc = gg_sssp(&S->own, A, &one, 1, tmp, nullptr, A->dtype == GG_BOOL ? GG_INT32 : A->dtype,
+                     n, nullptr);
+    }
+    // every solo worker's scratch arena grows to this graph's needs now, not during
+    // serving (growing it frees and allocates, which waits for the whole device)
+    for (size_t w = 0; rc == GG_OK && w < S->solo_ctx.size() && n > 0; ++w) {
+      gg_ctx* c = S->solo_ctx[w];
+      if (!dtype_is_float(A->dtype))
+        rc = gg_bfs_levels(c, A, 1, static_cast<int32_t*>(tmp), n, nullptr);
+      if (rc == GG_OK && nonneg) {
+        const int64_t one = 1;
+        rc = gg_sssp(c, A, &one, 1, tmp, nullptr, A->dtype == GG_BOOL ? GG_INT32 : A->dtype, n,
+                     nullptr);
+      }
+      if (rc == GG_OK && A->dtype == GG_FLOAT32) {  // one step of a served SpMV iteration
+        float* xb = static_cast<float*>(tmp);
+        cudaMemsetAsync(xb, 0, (size_t)n * 4, c->stream);
+        rc = spmm_dispatch(c, A, GG_FLOAT32, GG_OP_MUL, GG_OP_ADD, GG_OP_SECOND, xb + n,
+                           GG_FLOAT32, 1, xb, GG_FLOAT32, 1, 1, GG_ROW_MAJOR, nullptr, 0, 0, 0);
+      }
+      if (rc == GG_OK) rc = gg_stream_sync(c);
     }
     if (rc == GG_OK && A->dtype == GG_FLOAT32 && n > 0) {
       float* xb = static_cast<float*>(tmp);
@@ -952,10 +986,10 @@ int gg_server_destroy(gg_server* S) {
   if (S->worker.joinable()) S->worker.join();
   for (auto& t : S->solo_threads)
     if (t.joinable()) t.join();
-  for (gg_ctx* c : S->solo_ctx) {
-    cudaStream_t st = c->stream;
-    gg_destroy(c);
-    if (st) cudaStreamDestroy(st);
+  for (size_t w = 0; w < S->solo_ctx.size(); ++w) {
+    gg_destroy(S->solo_ctx[w]);
+    cudaStreamDestroy(S->solo_hi[w]);
+    cudaStreamDestroy(S->solo_lo[w]);
   }
   cudaSetDevice(S->own.device);
   cudaStreamSynchronize(S->stream);

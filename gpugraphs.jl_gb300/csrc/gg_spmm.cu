@@ -570,11 +570,28 @@ static int build_mm_plan(gg_ctx* ctx, gg_mat* A) {
 // partial buffers are bounded: wide dense operands run in column windows
 static const int64_t kMMPartialBytes = (int64_t)256 << 20;
 
+// one dense column of plus-times Float32 over a large CSR handle: the SELL-32 copy's
+// kernel with the SpMM's fold order (launch_col1_sell, gg_spmv.cu); other semirings
+// and operands keep the kernels below
+template <class SR>
+static bool col1_sell_ok(const gg_mat*, const SR&, int64_t, const void*, int64_t) { return false; }
+static bool col1_sell_ok(const gg_mat* A, const SRPlusTimesF32MM& sr, int64_t k, const void* mask,
+                         int64_t lo) {
+  return A->format == GG_FMT_CSR && A->m >= (1 << 16) && k == 1 && !mask && lo == 0 &&
+         sr.ldb == 1 && sr.ldc == 1;
+}
+template <class SR>
+static int col1_sell(gg_ctx*, gg_mat*, const SR&) { return GG_ERR_UNSUPPORTED; }
+static int col1_sell(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32MM& sr) {
+  return launch_col1_sell(ctx, A, sr.x, sr.y);
+}
+
 template <class SR>
 static int launch_mm(gg_ctx* ctx, gg_mat* A, const SR& sr, int64_t k, const void* mask, int tmask,
                      int64_t lo, int64_t hi) {
   typedef typename SR::T T;
   const int64_t m = A->m;
+  if (col1_sell_ok(A, sr, k, mask, lo)) return col1_sell(ctx, A, sr);
   GG_CHECK(build_mm_plan(ctx, A));
   const MMPlan* P = A->mmplan;
   int64_t jwin = k;
@@ -676,6 +693,13 @@ static int spmm_generic(gg_ctx* ctx, gg_mat* A, int mul, int add, int accum, voi
 int spmm_dispatch(gg_ctx* ctx, gg_mat* A, int tc, int mul, int add, int accum, void* Cm, int tcm,
                   int64_t ldc, const void* B, int tb, int64_t ldb, int64_t k, int layout,
                   const void* mask, int tmask, int64_t lo, int64_t hi) {
+  if (k == 1 && layout == GG_COL_MAJOR) {
+    // one column-major dense column is the same memory as a row-major one with
+    // leading dimension 1, so the row-major one-column kernels serve it
+    layout = GG_ROW_MAJOR;
+    ldb = 1;
+    ldc = 1;
+  }
   if (layout == GG_ROW_MAJOR && A->dtype == GG_FLOAT32 && tb == GG_FLOAT32 && tcm == GG_FLOAT32 &&
       mul == GG_OP_MUL && add == GG_OP_ADD && accum == GG_OP_SECOND) {
     SRPlusTimesF32MM sr;

@@ -1160,6 +1160,262 @@ static int launch_sell_hot(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32& sr,
   return GG_OK;
 }
 
+// ---------------------------------------------------------------------------------
+// One-column plus-times SpMM y = A x over the SELL-32 copy of a large CSR handle, in
+// the SpMM's fold order: a row of at most kSegMM entries is folded in storage order
+// from 0; a longer row in pieces of kSegMM entries (its 256-column chunks in the
+// slice-column-major copy, since the copy keeps every row's entries in order), each
+// folded from 0, then added in order with the stop at +Inf (k_spmm_combine); a piece
+// whose fold ends NaN is folded again with that stop.  So the results equal the
+// one-column kernels of gg_spmm.cu and every column of the 32-column SpMM bit for bit
+// while the loads are those of the headline SpMV (a lane per row, one 128-byte line
+// per warp load, the hottest x values in shared memory).
+// ---------------------------------------------------------------------------------
+static int build_col1_plan(gg_ctx* ctx, gg_mat* S) {
+  GG_CHECK(build_sell_plan(ctx, S));
+  SellPlan* P = S->sellplan;
+  if (P->npitems256 >= 0) return GG_OK;
+  const int64_t ns = S->nslices;
+  std::vector<int32_t> sp(ns + 1);
+  GG_CUDA(cudaMemcpyAsync(sp.data(), S->slice_ptr, (ns + 1) * sizeof(int32_t),
+                          cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<int4> pitems, multi;
+  int32_t np = 0;
+  int64_t g_first = -1, g_cols = 0, g_count = 0;
+  uint32_t g_widths = 0;
+  auto flush_group = [&]() {
+    if (g_count > 0)
+      pitems.push_back(make_int4(sp[g_first] - 1, (int)(g_first * 32), -(int)g_count, (int)g_widths));
+    g_first = -1;
+    g_cols = 0;
+    g_count = 0;
+    g_widths = 0;
+  };
+  for (int64_t s = 0; s < ns; ++s) {
+    const int64_t L = ((int64_t)sp[s + 1] - sp[s]) / 32;
+    if (L <= kNarrowCols) {
+      if (g_count == 8 || g_cols + L > kNarrowCols) flush_group();
+      if (g_count == 0) g_first = s;
+      g_widths |= (uint32_t)L << (4 * g_count);
+      g_cols += L;
+      ++g_count;
+      continue;
+    }
+    flush_group();
+    if (L <= kSegMM) {
+      pitems.push_back(make_int4(sp[s] - 1, (int)(s * 32), (int)L, -1));
+      continue;
+    }
+    const int32_t nch = (int32_t)((L + kSegMM - 1) / kSegMM);
+    multi.push_back(make_int4((int)(s * 32), np, nch, 0));
+    for (int32_t c = 0; c < nch; ++c) {
+      const int64_t jb = (int64_t)c * kSegMM;
+      const int64_t je = jb + kSegMM < L ? jb + kSegMM : L;
+      pitems.push_back(make_int4((int)(sp[s] - 1 + jb * 32), (int)(s * 32), (int)(je - jb), np + c));
+    }
+    np += nch;
+  }
+  flush_group();
+  cudaError_t e = cudaMalloc((void**)&P->pitems256, (pitems.size() + 1) * sizeof(int4));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&P->multi256, (multi.size() + 1) * sizeof(int4));
+  if (e == cudaSuccess && !pitems.empty())
+    e = cudaMemcpyAsync(P->pitems256, pitems.data(), pitems.size() * sizeof(int4),
+                        cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess && !multi.empty())
+    e = cudaMemcpyAsync(P->multi256, multi.data(), multi.size() * sizeof(int4),
+                        cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(P->pitems256);
+    cudaFree(P->multi256);
+    P->pitems256 = P->multi256 = nullptr;
+    return cuda_error(e, "one-column SpMM plan");
+  }
+  P->npitems256 = (int64_t)pitems.size();
+  P->nmulti256 = (int64_t)multi.size();
+  P->npart256 = np;
+  return GG_OK;
+}
+
+// x value of relabelled column col (1-based): shared memory for the hot ones
+__device__ __forceinline__ float col1_x(const float* sx, const float* __restrict__ xr, int32_t col,
+                                        int hot, uint64_t pol_x) {
+  return col <= hot ? sx[col - 1] : ld_keep(xr + (col - 1), pol_x);
+}
+
+__global__ void __launch_bounds__(kHotThreads, 1)
+    k_col1_sell(const float* __restrict__ nz, const float* __restrict__ xr, float* __restrict__ y,
+                const int32_t* __restrict__ colval, const int32_t* __restrict__ perm, int64_t m,
+                const int4* __restrict__ pitems, int64_t nitems, float* partials, int hot) {
+  extern __shared__ float sx[];
+  for (int i = threadIdx.x; i < hot; i += blockDim.x) sx[i] = __ldg(xr + i);
+  __syncthreads();
+  const uint64_t pol_s = l2_evict_first(), pol_x = l2_evict_last();
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int4 dn = gw < nitems ? __ldg(pitems + gw) : make_int4(0, 0, 0, -1);
+  for (int64_t it = gw; it < nitems; it += nw) {
+    const int4 d = dn;  // first position, first stored row, columns (or -slices), partial
+    if (it + nw < nitems) dn = __ldg(pitems + it + nw);
+    if (d.z < 0) {
+      // group of -d.z narrow slices (widths in 4-bit fields of d.w), <= 8 columns in all
+      const int ns = -d.z;
+      const uint32_t widths = (uint32_t)d.w;
+      int total = 0;
+      for (int t = 0; t < ns; ++t) total += (widths >> (4 * t)) & 15u;
+      float p[kNarrowCols];
+#pragma unroll
+      for (int u = 0; u < kNarrowCols; ++u) {
+        p[u] = 0.0f;
+        if (u < total) {
+          const int32_t col = ld_stream_p(colval + d.x + u * 32 + lane, pol_s);
+          const float a = ld_stream_p(nz + d.x + u * 32 + lane, pol_s);
+          if (col > 0) p[u] = __fmul_rn(a, col1_x(sx, xr, col, hot, pol_x));
+        }
+      }
+      int u0 = 0;
+      for (int t = 0; t < ns; ++t) {
+        const int w = (int)((widths >> (4 * t)) & 15u);
+        float acc = 0.0f;
+#pragma unroll
+        for (int u = 0; u < kNarrowCols; ++u)
+          if (u >= u0 && u < u0 + w) acc = __fadd_rn(acc, p[u]);
+        if (acc != acc) {  // NaN: the sequential fold with the stop at +Inf
+          acc = 0.0f;
+          for (int u = u0; u < u0 + w; ++u) {
+            acc = __fadd_rn(acc, p[u]);
+            if (acc == __int_as_float(0x7f800000)) break;
+          }
+        }
+        u0 += w;
+        const int64_t srow = (int64_t)d.y + t * 32 + lane;
+        if (srow < m) __stcs(y + (__ldg(perm + srow) - 1), acc);
+      }
+      continue;
+    }
+    const int64_t srow = (int64_t)d.y + lane;
+    const bool live = srow < m;
+    const int32_t pos0 = d.x + lane;
+    int32_t pos = pos0;
+    float acc = 0.0f;
+    int32_t c[8];
+    float a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool in = live && u < d.z;
+      c[u] = in ? ld_stream_p(colval + pos + u * 32, pol_s) : -1;
+      a[u] = in ? ld_stream_p(nz + pos + u * 32, pol_s) : 0.0f;
+    }
+    for (int32_t j = 0; j < d.z; j += 8) {
+      const int32_t pn = pos + 8 * 32;
+      int32_t cn[8];
+      float an[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const bool in = live && j + 8 + u < d.z;
+        cn[u] = in ? ld_stream_p(colval + pn + u * 32, pol_s) : -1;
+        an[u] = in ? ld_stream_p(nz + pn + u * 32, pol_s) : 0.0f;
+      }
+      float p[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) p[u] = c[u] > 0 ? __fmul_rn(a[u], col1_x(sx, xr, c[u], hot, pol_x)) : 0.0f;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) acc = __fadd_rn(acc, p[u]);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        c[u] = cn[u];
+        a[u] = an[u];
+      }
+      pos = pn;
+    }
+    if (!live) continue;
+    if (acc != acc) {  // NaN: this row's piece again, in storage order, stopping at +Inf
+      acc = 0.0f;
+      for (int32_t j = 0; j < d.z; ++j) {
+        const int32_t col = colval[pos0 + j * 32];
+        if (col <= 0) break;  // padding: the row ended
+        acc = __fadd_rn(acc, __fmul_rn(nz[pos0 + j * 32], col1_x(sx, xr, col, hot, pol_x)));
+        if (acc == __int_as_float(0x7f800000)) break;
+      }
+    }
+    if (d.w < 0) __stcs(y + (__ldg(perm + srow) - 1), acc);
+    else partials[(int64_t)d.w * 32 + lane] = acc;
+  }
+}
+
+// rows of slices cut into several chunks: the pieces added in order, stopping at +Inf
+// (k_spmm_combine's order; chunks past a row's end hold +0.0, which changes no sum)
+__global__ void k_col1_combine(const int4* __restrict__ multi, int64_t nmulti,
+                               const float* __restrict__ partials, const int32_t* __restrict__ perm,
+                               int64_t m, float* __restrict__ y) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nmulti * 32;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int4 d = multi[t >> 5];  // first stored row, first partial, chunks
+    const int o = (int)(t & 31);
+    const int64_t srow = (int64_t)d.x + o;
+    if (srow >= m) continue;
+    float acc = 0.0f;
+    for (int c = 0; c < d.z; ++c) {
+      acc = __fadd_rn(acc, partials[(int64_t)(d.y + c) * 32 + o]);
+      if (acc == __int_as_float(0x7f800000)) break;
+    }
+    y[perm[srow] - 1] = acc;
+  }
+}
+
+// y = A x, one column, for a CSR handle of >= 65536 rows (gg_spmm with k == 1); the
+// relabelled x and the piece partials live in the context's scratch arena
+int launch_col1_sell(gg_ctx* ctx, gg_mat* A, const float* x, float* y) {
+  if (!A->sell_copy) {
+    GG_CHECK(gg_sell_create(ctx, A, 32, A->m, &A->sell_copy));
+    A->sell_copy->sell_variant = A->sell_variant;
+    A->sell_copy->hot_cols = A->hot_cols;
+  }
+  gg_mat* S = A->sell_copy;
+  GG_CHECK(build_colperm(ctx, S));
+  GG_CHECK(build_col1_plan(ctx, S));
+  const SellPlan* P = S->sellplan;
+  const int64_t n = A->n;
+  const size_t xr_bytes = ((size_t)n * sizeof(float) + 255) & ~(size_t)255;
+  GG_CHECK(ensure_scratch(ctx, xr_bytes + (size_t)(P->npart256 * 32 + 1) * sizeof(float)));
+  float* xr_buf = static_cast<float*>(ctx->scratch);
+  float* partials = reinterpret_cast<float*>(static_cast<char*>(ctx->scratch) + xr_bytes);
+  const float* xr = x;
+  const int32_t* colval = S->colval;
+  if (S->colperm->enabled) {
+    k_gather_x<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(x, S->colperm->inv, n, xr_buf);
+    trace_count(ctx, 1);
+    xr = xr_buf;
+    colval = S->colperm->colval_r;
+  }
+  const int hot_cap = S->hot_cols > 0 ? (S->hot_cols < kHotColsMax ? S->hot_cols : kHotColsMax)
+                                      : kHotCols;
+  const int hot = (int)std::min<int64_t>(n, hot_cap);
+  static bool attr_set[64] = {false};
+  if (ctx->device < 64 && !attr_set[ctx->device]) {
+    GG_CUDA(cudaFuncSetAttribute(k_col1_sell, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kHotColsMax * (int)sizeof(float)));
+    attr_set[ctx->device] = true;
+  }
+  if (P->npitems256 > 0) {
+    const int tr = trace_main_begin(ctx);
+    k_col1_sell<<<ctx->num_sms, kHotThreads, hot * sizeof(float), ctx->stream>>>(
+        static_cast<const float*>(S->nzval), xr, y, colval, S->perm, S->m, P->pitems256,
+        P->npitems256, partials, hot);
+    trace_main_end(ctx, tr);
+    trace_count(ctx, 1);
+  }
+  if (P->nmulti256 > 0) {
+    k_col1_combine<<<grid_for(ctx, P->nmulti256 * 32, 256), 256, 0, ctx->stream>>>(
+        P->multi256, P->nmulti256, partials, S->perm, S->m, y);
+    trace_count(ctx, 1);
+  }
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
 // plus-times Float32 y = A x over a CSR handle with the row-block pipeline kernel
 // (colval: the handle's own or relabelled column labels); trace_main brackets the
 // kernel as the call's main kernel

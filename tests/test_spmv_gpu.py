@@ -772,3 +772,43 @@ def test_spmm_wide_operand_power_law():
         ref = A.to_scipy().astype(np.float64)[rows] @ B.astype(np.float64)
     fin = np.isfinite(ref)
     np.testing.assert_allclose(Ch[rows][fin], ref[fin], rtol=RTOL, atol=1e-6)
+
+
+def test_spmm_one_column_large_csr_equals_the_wide_fold():
+    """One dense column on a CSR of >= 65536 rows runs over the SELL-32 copy with
+    256-column chunks; it must fold exactly like the 32-column SpMM (rows of <= 256
+    entries in storage order, longer rows in pieces of 256 added in order, NaN pieces
+    refolded with the stop at +Inf): every column of a 32-column product equals the
+    one-column product of that column bit for bit, with +Inf, -Inf and NaN in B, in
+    both dense layouts; sampled rows of <= 256 entries equal the oracle."""
+    from gpugraphs import generators as gen
+    A = gen.rmat(17, 16, seed=35, wkind=gen.W_U01_F32)
+    n = A.n
+    rp, cv, nz = host(A.rowptr), host(A.colval), host(A.nzval)
+    rng = np.random.default_rng(35)
+    B = rng.random((n, 32), dtype=np.float32)
+    cc = np.bincount(cv - 1, minlength=n)
+    order = np.argsort(-cc, kind="stable")
+    B[order[0], :8] = np.inf             # a hub column: many rows reach +Inf
+    B[order[3:300:7], 8:16] = np.nan
+    B[order[5:300:11], 16:24] = -np.inf
+    Bd = dev(B)
+    C = torch.zeros((n, 32), dtype=torch.float32, device="cuda")
+    G.gpu_spmm_(C, A, Bd)
+    Ch = host(C)
+    for j in (0, 3, 9, 17, 30):
+        for col in (Bd[:, j:j + 1].contiguous(), Bd[:, j].clone().view(n, 1)):
+            y = torch.full((n, 1), -5.0, dtype=torch.float32, device="cuda")
+            G.gpu_spmm_(y, A, col)
+            yh = host(y)[:, 0]
+            assert np.array_equal(np.isnan(yh), np.isnan(Ch[:, j]))
+            fin = ~np.isnan(yh)
+            assert np.array_equal(yh[fin].view(np.int32), Ch[fin, j].view(np.int32)), j
+    deg = np.diff(rp)
+    rows = np.unique(rng.integers(0, n, 800))
+    short = rows[deg[rows] <= SEG_MM]
+    srp = np.concatenate([[1], 1 + np.cumsum(deg[short])]).astype(np.int32)
+    idx = np.concatenate([np.arange(rp[r] - 1, rp[r + 1] - 1) for r in short])
+    Co = np.zeros((len(short), 32), np.float32)
+    O.csr_spmm(len(short), srp, cv[idx], nz[idx], Co, B, layout=1)
+    np.testing.assert_array_equal(Ch[short], Co)
