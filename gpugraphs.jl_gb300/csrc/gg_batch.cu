@@ -197,6 +197,8 @@ struct BsWork {
   int32_t* cq[2];
   int32_t* vlist;
   unsigned* mark;
+  int32_t* mhq;    // hubs among the changed vertices, marked in pieces
+  int32_t* mhoff;  // their piece offsets
   unsigned long long* ctr;
 };
 
@@ -227,6 +229,8 @@ static int bs_alloc(BsWork<T>& w, int64_t n, int64_t qcap, cudaStream_t st) {
   GG_CUDA(cudaMallocAsync((void**)&w.cq[1], (size_t)qcap * sizeof(int32_t), st));
   GG_CUDA(cudaMallocAsync((void**)&w.vlist, (size_t)(n + 64) * sizeof(int32_t), st));
   GG_CUDA(cudaMallocAsync((void**)&w.mark, (size_t)((n + 31) / 32 + 2) * sizeof(unsigned), st));
+  GG_CUDA(cudaMallocAsync((void**)&w.mhq, (size_t)(n + 64) * sizeof(int32_t), st));
+  GG_CUDA(cudaMallocAsync((void**)&w.mhoff, (size_t)(n + 65) * sizeof(int32_t), st));
   GG_CUDA(cudaMallocAsync((void**)&w.ctr, 64, st));
   w.c[0] = c;
   w.c[1] = c + n;
@@ -241,6 +245,8 @@ static void bs_free(BsWork<T>& w, cudaStream_t st) {
   cudaFreeAsync(w.cq[1], st);
   cudaFreeAsync(w.vlist, st);
   cudaFreeAsync(w.mark, st);
+  cudaFreeAsync(w.mhq, st);
+  cudaFreeAsync(w.mhoff, st);
   cudaFreeAsync(w.ctr, st);
 }
 
@@ -282,10 +288,8 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
   if (R.restricted) {
     GG_CUDA(cudaMemsetAsync(w.mark, 0, ((n + 31) / 32) * sizeof(unsigned), R.st));
     GG_CUDA(cudaMemsetAsync(w.ctr + 3, 0, sizeof(unsigned long long), R.st));
-    int64_t mb = (R.nchanged * 32 + 255) / 256;
-    if (mb > gcap) mb = gcap;
-    k_ms_mark<<<(int)(mb < 1 ? 1 : mb), 256, 0, R.st>>>(prow, pcol, w.cq[cur], ncq_cur, w.mark,
-                                                        w.vlist, w.ctr + 3);
+    GG_CUDA(launch_ms_mark(R.st, ctx->num_sms, R.nchanged, prow, pcol, w.cq[cur], ncq_cur, w.mark,
+                           w.vlist, w.ctr + 3, w.mhq, w.ctr + 4, w.mhoff));
     k_ms_round<T><<<(int)gcap, 256, 0, R.st>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr,
                                                w.vlist, w.ctr + 3, w.cq[cur ^ 1], ncq_nxt);
   } else {

@@ -2129,21 +2129,37 @@ __global__ void __launch_bounds__(kPullSellThreads)
     const int64_t srow = (int64_t)d.y + lane;
     T best = Lim<T>::max();
     if (srow < m) {
+      // the next 8 columns / weights are loaded (streamed past L1) while the current
+      // 8 distances are gathered
+      int32_t col[8];
+      T w[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int64_t pos = (int64_t)d.x + lane + (int64_t)u * 32;
+        col[u] = u < d.z ? __ldcs(colval + pos) : -1;
+        w[u] = u < d.z ? view_weight<T>(nz, tv, pos) : Lim<T>::max();
+      }
       for (int32_t j = 0; j < d.z; j += 8) {
-        int32_t col[8];
-        T w[8];
+        int32_t cn[8];
+        T wn[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          const int64_t pos = (int64_t)d.x + lane + (int64_t)(j + u) * 32;
-          col[u] = j + u < d.z ? __ldg(colval + pos) : -1;
-          w[u] = j + u < d.z ? view_weight<T>(nz, tv, pos) : Lim<T>::max();
+          const int64_t pos = (int64_t)d.x + lane + (int64_t)(j + 8 + u) * 32;
+          cn[u] = j + 8 + u < d.z ? __ldcs(colval + pos) : -1;
+          wn[u] = j + 8 + u < d.z ? view_weight<T>(nz, tv, pos) : Lim<T>::max();
+        }
+        T dv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) dv[u] = col[u] > 0 ? ld_l1(dist + (col[u] - 1)) : Lim<T>::max();
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const T cand = relax_add(w[u], dv[u]);
+          best = cand < best ? cand : best;
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          if (col[u] > 0) {
-            const T cand = relax_add(w[u], ld_l1(dist + (col[u] - 1)));
-            best = cand < best ? cand : best;
-          }
+          col[u] = cn[u];
+          w[u] = wn[u];
         }
       }
     }

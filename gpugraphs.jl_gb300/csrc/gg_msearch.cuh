@@ -382,36 +382,142 @@ __global__ void __launch_bounds__(256)
 
 // marking for a frontier-restricted round: the out-neighbours of the changed vertices
 // cq[0, *ncq) are the only vertices whose distances can drop; each is marked once in
-// the bitmap and listed in vlist
+// the bitmap and listed in vlist.  A changed vertex with more than kMarkHub out-edges
+// is not walked by one warp (a hub's list held one warp for milliseconds while the
+// others idled): it is queued in mhq and its out-list marked in pieces of kMarkPiece
+// edges by every warp (k_ms_mark_offsets, k_ms_mark_hub).
+static const int kMarkHub = 1024, kMarkPiece = 1024;
+
+__device__ __forceinline__ void ms_mark_range(const int32_t* __restrict__ pcol, int32_t k0,
+                                              int32_t k1, int lane, unsigned* mark, int32_t* vlist,
+                                              unsigned long long* nlist) {
+  for (int32_t kb = k0; kb < k1; kb += 32) {
+    const int32_t k = kb + lane;
+    bool add = false;
+    int32_t w = 0;
+    if (k < k1) {
+      w = __ldg(pcol + k);
+      const unsigned bit = 1u << (w & 31);
+      if (!(__ldcg(mark + (w >> 5)) & bit)) add = !(atomicOr(mark + (w >> 5), bit) & bit);
+    }
+    const unsigned b = __ballot_sync(kFullB, add);
+    if (b) {
+      const int leader = __ffs(b) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(nlist, (unsigned long long)__popc(b));
+      base = __shfl_sync(kFullB, base, leader);
+      if (add) vlist[base + __popc(b & ((1u << lane) - 1u))] = w;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256)
     k_ms_mark(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
               const int32_t* __restrict__ cq, const unsigned long long* ncq, unsigned* mark,
-              int32_t* vlist, unsigned long long* nlist) {
+              int32_t* vlist, unsigned long long* nlist, int32_t* mhq, unsigned long long* nmh) {
   const int lane = threadIdx.x & 31;
   const int64_t total = (int64_t)*((volatile const unsigned long long*)ncq);
   for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < total;
        i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int32_t u = cq[i];
     const int32_t k0 = prow[u], k1 = prow[u + 1];
-    for (int32_t kb = k0; kb < k1; kb += 32) {
-      const int32_t k = kb + lane;
-      bool add = false;
-      int32_t w = 0;
-      if (k < k1) {
-        w = __ldg(pcol + k);
-        const unsigned bit = 1u << (w & 31);
-        if (!(__ldcg(mark + (w >> 5)) & bit)) add = !(atomicOr(mark + (w >> 5), bit) & bit);
-      }
-      const unsigned b = __ballot_sync(kFullB, add);
-      if (b) {
-        const int leader = __ffs(b) - 1;
-        unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(nlist, (unsigned long long)__popc(b));
-        base = __shfl_sync(kFullB, base, leader);
-        if (add) vlist[base + __popc(b & ((1u << lane) - 1u))] = w;
-      }
+    if (k1 - k0 > kMarkHub) {  // left to the piece kernel
+      if (lane == 0) mhq[atomicAdd(nmh, 1ull)] = u;
+      continue;
     }
+    ms_mark_range(pcol, k0, k1, lane, mark, vlist, nlist);
   }
+}
+
+// piece offsets of the queued hubs: mhoff[h] = pieces of hubs before h, mhoff[nh] = all
+__global__ void __launch_bounds__(1024)
+    k_ms_mark_offsets(const int32_t* __restrict__ prow, const int32_t* __restrict__ mhq,
+                      const unsigned long long* nmh, int32_t* mhoff) {
+  __shared__ int32_t wsum[32];
+  __shared__ int32_t carry;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t nh = (int64_t)*((volatile const unsigned long long*)nmh);
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t b0 = 0; b0 < nh; b0 += 1024) {
+    const int64_t i = b0 + threadIdx.x;
+    int32_t np = 0;
+    if (i < nh) {
+      const int32_t u = mhq[i];
+      np = (prow[u + 1] - prow[u] + kMarkPiece - 1) / kMarkPiece;
+    }
+    int32_t x = np;  // inclusive scan within the warp, then over the warp totals
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t t = __shfl_up_sync(kFullB, x, o);
+      if (lane >= o) x += t;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int32_t y = wsum[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t t = __shfl_up_sync(kFullB, y, o);
+        if (lane >= o) y += t;
+      }
+      wsum[lane] = y;
+    }
+    __syncthreads();
+    const int32_t incl = x + (wid > 0 ? wsum[wid - 1] : 0);
+    const int32_t c = carry;
+    if (i < nh) mhoff[i] = c + incl - np;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = c + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) mhoff[nh] = carry;
+}
+
+__global__ void __launch_bounds__(256)
+    k_ms_mark_hub(const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+                  const int32_t* __restrict__ mhq, const unsigned long long* nmh,
+                  const int32_t* __restrict__ mhoff, unsigned* mark, int32_t* vlist,
+                  unsigned long long* nlist) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nh = (int64_t)*((volatile const unsigned long long*)nmh);
+  if (nh == 0) return;
+  const int64_t npieces = mhoff[nh];
+  int64_t h = 0;
+  for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < npieces;
+       q += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    // the hub holding piece q (q only grows, so search forward from the last one)
+    if (__ldg(mhoff + h + 1) <= q) {
+      int64_t lo = h + 1, hi = nh - 1;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(mhoff + mid) <= q) lo = mid; else hi = mid - 1;
+      }
+      h = lo;
+    }
+    const int32_t u = mhq[h];
+    const int32_t k0 = prow[u] + (int32_t)(q - mhoff[h]) * kMarkPiece;
+    const int32_t k1 = min(prow[u + 1], k0 + kMarkPiece);
+    ms_mark_range(pcol, k0, k1, lane, mark, vlist, nlist);
+  }
+}
+
+// the three marking launches of a frontier-restricted round; nmh: a device counter,
+// mhq / mhoff: room for n and n + 1 entries
+static inline cudaError_t launch_ms_mark(cudaStream_t st, int num_sms, int64_t nchanged,
+                                         const int32_t* prow, const int32_t* pcol,
+                                         const int32_t* cq, const unsigned long long* ncq,
+                                         unsigned* mark, int32_t* vlist, unsigned long long* nlist,
+                                         int32_t* mhq, unsigned long long* nmh, int32_t* mhoff) {
+  cudaError_t e = cudaMemsetAsync(nmh, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  int64_t mb = (nchanged * 32 + 255) / 256;
+  const int64_t gcap = (int64_t)num_sms * 8;
+  if (mb > gcap) mb = gcap;
+  k_ms_mark<<<(int)(mb < 1 ? 1 : mb), 256, 0, st>>>(prow, pcol, cq, ncq, mark, vlist, nlist, mhq, nmh);
+  k_ms_mark_offsets<<<1, 1024, 0, st>>>(prow, mhq, nmh, mhoff);
+  k_ms_mark_hub<<<(int)gcap, 256, 0, st>>>(prow, pcol, mhq, nmh, mhoff, mark, vlist, nlist);
+  return cudaGetLastError();
 }
 
 template <typename T> __device__ __forceinline__ T b_atomic_min(T* p, T v);

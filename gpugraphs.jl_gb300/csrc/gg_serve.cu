@@ -166,6 +166,8 @@ struct Executor {
   int32_t* cq[2] = {nullptr, nullptr};
   int32_t* vlist = nullptr;
   unsigned* mark = nullptr;
+  int32_t* mhq = nullptr;    // hubs among the changed vertices, marked in pieces
+  int32_t* mhoff = nullptr;  // their piece offsets
   int cq_cur = 0;
   int64_t nchanged = 0;
   const int32_t* prow = nullptr;
@@ -240,8 +242,8 @@ static int grid_s(gg_server* S, int64_t work) {
 static size_t exec_bytes(int kind, int64_t n, int dtype) {
   switch (kind) {
     case GG_QUERY_BFS: return (size_t)n * kBfsW * 4 * 3 + 4096;
-    // distances, changed-column masks (2 x 4n), changed queues and marks (~12n)
-    case GG_QUERY_SSSP: return (size_t)n * kColSlots * dtype_size(dtype) + 20 * (size_t)n + 4096;
+    // distances, changed-column masks (2 x 4n), changed queues, marks and hub lists (~20n)
+    case GG_QUERY_SSSP: return (size_t)n * kColSlots * dtype_size(dtype) + 28 * (size_t)n + 4096;
     default: return (size_t)n * kColSlots * 4 * 2 + 4096;
   }
 }
@@ -262,6 +264,8 @@ static void exec_free(Executor& E) {
   cudaFree(E.cq[1]);
   cudaFree(E.vlist);
   cudaFree(E.mark);
+  cudaFree(E.mhq);
+  cudaFree(E.mhoff);
   cudaFree(E.X);
   cudaFree(E.Y);
   cudaFree(E.d_slots);
@@ -347,6 +351,8 @@ static int exec_create(gg_server* S, int gi, int kind, Executor& E) {
     GG_CUDA(cudaMalloc((void**)&E.cq[1], qcap * sizeof(int32_t)));
     GG_CUDA(cudaMalloc((void**)&E.vlist, (n + 64) * sizeof(int32_t)));
     GG_CUDA(cudaMalloc((void**)&E.mark, ((n + 31) / 32 + 2) * sizeof(unsigned)));
+    GG_CUDA(cudaMalloc((void**)&E.mhq, (n + 64) * sizeof(int32_t)));
+    GG_CUDA(cudaMalloc((void**)&E.mhoff, (n + 65) * sizeof(int32_t)));
     GG_CUDA(cudaMemsetAsync(E.d_cnt, 0, 64, st));  // [0] count, [1]/[2] queue lengths, [3] marked
     GG_CHECK(push_view(&S->own, S->graphs[gi], &E.prow, &E.pcol));
     // every column starts at the fixpoint of "no source": typemax everywhere
@@ -462,8 +468,8 @@ static void ss_round(gg_server* S, Executor& E, const SrvGraph& sg, const HubPla
   if (restricted) {
     cudaMemsetAsync(E.mark, 0, ((n + 31) / 32) * sizeof(unsigned), st);
     cudaMemsetAsync(E.d_cnt + 3, 0, sizeof(unsigned long long), st);
-    k_ms_mark<<<grid_s(S, E.nchanged * 32), 256, 0, st>>>(E.prow, E.pcol, E.cq[cur], ncq_cur, E.mark,
-                                                          E.vlist, E.d_cnt + 3);
+    launch_ms_mark(st, S->own.num_sms, E.nchanged, E.prow, E.pcol, E.cq[cur], ncq_cur, E.mark,
+                   E.vlist, E.d_cnt + 3, E.mhq, E.d_cnt + 4, E.mhoff);
     k_ms_round<T><<<grid_s(S, n * 32), 256, 0, st>>>(n, sg.g, D, E.c0, E.c1, E.d_cnt, E.d_amask,
                                                       E.vlist, E.d_cnt + 3, E.cq[cur ^ 1], ncq_nxt);
   } else {
