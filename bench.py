@@ -704,6 +704,11 @@ def secondary_large(args, device, parity, rank):
         del A, d0, run
         torch.cuda.empty_cache()
     out["serve_summary"] = serve_summary(device)
+    torch.cuda.empty_cache()
+    mgm = multigraph_measure(device, 1000, 10, 3, parity=rank == 0 and not args.no_parity)
+    if "parity" in mgm:
+        parity["multigraph_1000"] = mgm.pop("parity")
+    out["multigraph_1000"] = mgm
     out["large_configs_s"] = round(time.time() - t0, 1)
     return out
 
@@ -1062,22 +1067,21 @@ def _single(G, graphs, xs, kind, g, s):
 # many graphs: 1000 Erdos-Renyi graphs in one launch
 # ---------------------------------------------------------------------------------
 
-def run_multigraph(args):
+def multigraph_measure(device, ng, steps, warmup, parity=True):
     """1000 symmetric Erdos-Renyi graphs, n = round(10^U[3,6]), average degree U[4,32]
     (seed 2), Float32 values U[0,1).  One plus-times SpMV over all graphs in one launch,
-    and one BFS per graph in one persistent cooperative launch (CUDA graph), against
-    the same work as one call per graph."""
+    one BFS and one shortest-path search per graph in one persistent cooperative launch
+    each (CUDA graphs), against the same work as one call per graph; with `parity`,
+    sampled graphs (every 100th and the last three, whose entry offsets in the
+    concatenation pass 2^31) are checked against the oracle."""
     import numpy as np
+    import scipy.sparse as sp
     import torch
     import gpugraphs as G
     from gpugraphs import generators as gen
     from gpugraphs.multigraph import MultiGraph
 
-    ws, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    device = torch.device("cuda", local)
     rng = np.random.default_rng(2)
-    ng = args.graphs
     ns = np.round(10 ** rng.uniform(3, 6, ng)).astype(np.int64)
     degs = rng.uniform(4, 32, ng)
     t0 = time.time()
@@ -1089,9 +1093,7 @@ def run_multigraph(args):
     N, NNZ = mg.total_n, mg.total_nnz
     x = gen.uniform_vector(N, seed=3, device=device)
     y = torch.empty(N, dtype=torch.float32, device=device)
-    clk = ClockSampler(local)
-    clk.start()
-    ms = time_steps(lambda: mg.spmv(x, y), args.steps, warmup=max(args.warmup, 3))
+    ms = time_steps(lambda: mg.spmv(x, y), steps, warmup=max(warmup, 3))
     B = spmv_bytes(N, NNZ) + 8 * (ng + 1)
     xs = mg.split(x)
     ys = [torch.empty_like(v) for v in xs]
@@ -1100,12 +1102,12 @@ def run_multigraph(args):
         for A, xv, yv in zip(graphs, xs, ys):
             G.gpu_spmv_(yv, A, xv)
 
-    ms_loop = time_steps(per_graph, max(3, args.steps // 4), warmup=1)
+    ms_loop = time_steps(per_graph, max(3, steps // 4), warmup=1)
     src = [int(rng.integers(1, int(n) + 1)) for n in ns]
     d = torch.empty(N, dtype=torch.int32, device=device)  # fixed buffer: the CUDA graph is reused
     mg.bfs(src, d)
     torch.cuda.synchronize()
-    tb = time_host(lambda i: mg.bfs(src, d), max(3, args.steps // 4), warmup=1)
+    tb = time_host(lambda i: mg.bfs(src, d), max(3, steps // 4), warmup=1)
     t_bfs = statistics.median(tb)
     reached = int((d != I32MAX).sum().item())
     # traversed edges: entries of reached vertices, halved (symmetric graphs)
@@ -1116,29 +1118,76 @@ def run_multigraph(args):
     pats = [G.SparseGPUMatrixCSR(A.m, A.n, A.rowptr, A.colval,
                                  torch.ones(A.nnz(), dtype=torch.bool, device=device)) for A in graphs]
     tl = time_host(lambda i: [G.bfs_distances(P, s) for P, s in zip(pats, src)], 1, warmup=1)
-    ok = all(torch.equal(dv, G.bfs_distances(P, s))
-             for P, s, dv in list(zip(pats, src, mg.split(d)))[:: max(1, ng // 20)])
+    same_bfs = all(torch.equal(dv, G.bfs_distances(P, s))
+                   for P, s, dv in list(zip(pats, src, mg.split(d)))[:: max(1, ng // 20)])
     del pats
     t_loop = statistics.median(tl)
+    dsp = torch.empty(N, dtype=torch.float32, device=device)
+    mg.sssp(src, dsp)
+    torch.cuda.synchronize()
+    tsp = statistics.median(time_host(lambda i: mg.sssp(src, dsp), 2, warmup=0))
+    out = {"graphs": ng, "total_n": N, "total_nnz": NNZ, "build_s": round(build_s, 1),
+           "spmv_ms": round(ms, 4), "spmv_gbs": round(B / ms / 1e6, 2), "spmv_bytes": B,
+           "spmv_per_graph_ms": round(ms_loop, 3), "spmv_speedup_of_one_launch": round(ms_loop / ms, 2),
+           "bfs_ms": round(t_bfs * 1e3, 3), "bfs_gteps": round(mcc / t_bfs / 1e9, 2),
+           "bfs_levels": mg.last_levels, "bfs_reached": reached,
+           "bfs_per_graph_calls_ms": round(t_loop * 1e3, 1),
+           "bfs_speedup_of_one_launch": round(t_loop / t_bfs, 2), "bfs_equal_to_per_graph": same_bfs,
+           "sssp_ms": round(tsp * 1e3, 3), "sssp_rounds": mg.last_rounds}
+    if parity:
+        from oracle import oracle as O
+        t1 = time.time()
+        idx = sorted(set(range(0, ng, 100)) | {ng - 3, ng - 2, ng - 1})
+        offs = [sum(A.nnz() for A in graphs[:g]) for g in (idx[-3], idx[-1])]
+        ok_bfs = ok_sp = ok_mv = True
+        worst = 0.0
+        yl, dl, sl = mg.split(y), mg.split(d), mg.split(dsp)
+        for g in idx:
+            A = graphs[g]
+            rp, cv, nz = A.rowptr.cpu().numpy(), A.colval.cpu().numpy(), A.nzval.cpu().numpy()
+            lv, _ = O.bfs_levels_fast(A.n, rp, cv, None, src[g], symmetric=True)
+            ok_bfs &= bool(np.array_equal(dl[g].cpu().numpy(), lv))
+            ref = O.sssp_dijkstra(A.n, rp, cv, nz, src[g], symmetric=True)
+            ok_sp &= bool(np.array_equal(sl[g].cpu().numpy().view(np.int32), ref.view(np.int32)))
+            M = sp.csr_matrix((nz.astype(np.float64), cv - 1, rp - 1), shape=(A.n, A.n))
+            r64 = M @ xs[g].cpu().numpy().astype(np.float64)
+            dd = np.abs(yl[g].cpu().numpy().astype(np.float64) - r64)
+            err = float(np.max(np.where(r64 != 0, dd / np.where(r64 != 0, np.abs(r64), 1), dd))) if A.n else 0.0
+            worst = max(worst, err)
+        ok_mv = worst <= 1e-5
+        out["parity"] = {"graphs_checked": len(idx), "entry_offset_of_last_checked": offs[-1],
+                         "bfs_levels_equal": ok_bfs, "sssp_equal": ok_sp,
+                         "spmv_max_rel_err_vs_fp64": worst, "ok": bool(ok_bfs and ok_sp and ok_mv),
+                         "oracle": "frontier BFS, Float32 Dijkstra, FP64 SpMV", "check_s": round(time.time() - t1, 1)}
+    return out
+
+
+def run_multigraph(args):
+    """The many-graph workload (multigraph_measure) as one JSON line."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    clk = ClockSampler(local)
+    clk.start()
+    m = multigraph_measure(device, args.graphs, args.steps, args.warmup,
+                           parity=rank == 0 and not args.no_parity)
     clocks = clk.stop()
     peak, peak_kind = peak_hbm()
     out = {
         "metric": "multi-graph SpMV GB/s (1000 Erdos-Renyi graphs, one launch)",
-        "value": round(ws * B / ms / 1e6, 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "value": round(ws * m["spmv_gbs"], 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": m["spmv_ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Erdos-Renyi generator on the device)",
-        "config": {"workload": "multigraph", "graphs": ng, "total_n": N, "total_nnz": NNZ,
-                   "n": "round(10^U[3,6])", "avg_degree": "U[4,32]", "build_s": round(build_s, 1),
-                   "l2": "inputs larger than L2 (%.1f GB CSR)" % ((4 * N + 8 * NNZ) / 1e9)},
-        "roofline": {"bound": "hbm", "achieved": round(B / ms / 1e6, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(B / ms / 1e6 / peak, 4), "traffic": None, "peak_kind": peak_kind,
-                     "algorithmic_bytes": B},
-        "per_graph_launches": {"ms": round(ms_loop, 3), "speedup_of_one_launch": round(ms_loop / ms, 2)},
-        "bfs": {"ms": round(t_bfs * 1e3, 3), "gteps": round(mcc / t_bfs / 1e9, 2), "levels": mg.last_levels,
-                "reached": reached, "per_graph_calls_ms": round(t_loop * 1e3, 1),
-                "speedup_of_one_launch": round(t_loop / t_bfs, 2), "equal_to_per_graph": ok},
-        "e2e": None, "gpu_launches": args.steps, "clocks": clocks,
+        "config": {"workload": "multigraph", "graphs": m["graphs"], "total_n": m["total_n"],
+                   "total_nnz": m["total_nnz"], "n": "round(10^U[3,6])", "avg_degree": "U[4,32]",
+                   "build_s": m["build_s"],
+                   "l2": "inputs larger than L2 (%.1f GB CSR)" % ((4 * m["total_n"] + 8 * m["total_nnz"]) / 1e9)},
+        "roofline": {"bound": "hbm", "achieved": m["spmv_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": round(m["spmv_gbs"] / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                     "algorithmic_bytes": m["spmv_bytes"]},
+        "detail": m, "e2e": None, "gpu_launches": args.steps, "clocks": clocks,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)

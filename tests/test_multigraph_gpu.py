@@ -73,3 +73,36 @@ def test_multigraph_bfs_float_graphs_use_the_pattern():
         P = G.SparseGPUMatrixCSR(g.m, g.n, g.rowptr, g.colval,
                                  torch.ones(g.nnz(), dtype=torch.bool, device="cuda"))
         assert torch.equal(part, G.bfs_distances(P, 1))
+
+
+def test_multigraph_entry_offsets_past_int32():
+    """Six symmetric Erdos-Renyi graphs of 2^22 vertices with about 108 entries per row
+    hold more than 2^31 stored entries together, so the last graphs' entry offsets in
+    the concatenation exceed Int32 (the 1000-graph configuration holds about 2.6 G).
+    Their SpMV (within rtol 1e-5 of FP64), BFS levels (exact, against the oracle's
+    frontier BFS) and shortest paths (exact, against the single-graph path) from the
+    one-launch structure equal the per-graph results."""
+    import scipy.sparse as sp
+    from oracle import oracle as O
+    n = 1 << 22
+    gs = [gen.erdos_renyi(n, 54, seed=70 + i, wkind=gen.W_F32_1_10, symmetric=True) for i in range(6)]
+    mg = MultiGraph(gs)
+    assert mg.total_nnz > 2 ** 31 and int(mg.offsets[-1]) == 6 * n
+    last = gs[-1]
+    rp, cv, nz = (t.cpu().numpy() for t in (last.rowptr, last.colval, last.nzval))
+    before = sum(g.nnz() for g in gs[:-1])
+    assert before > 2 ** 31  # every entry of the last graph sits past Int32 offsets
+    x = torch.rand(mg.total_n, device="cuda", generator=torch.Generator(device="cuda").manual_seed(7))
+    y = mg.spmv(x)
+    xl = mg.split(x)[-1].cpu().numpy().astype(np.float64)
+    ref = sp.csr_matrix((nz.astype(np.float64), cv - 1, rp - 1), shape=(n, n)) @ xl
+    np.testing.assert_allclose(mg.split(y)[-1].cpu().numpy(), ref, rtol=1e-5, atol=1e-6)
+    src = [1 + 97 * i for i in range(len(gs))]
+    d = mg.bfs(src)
+    torch.cuda.synchronize()
+    lv, _ = O.bfs_levels_fast(n, rp, cv, None, src[-1], symmetric=True)
+    assert (mg.split(d)[-1].cpu().numpy() == lv).all()
+    ds = mg.sssp(src)
+    torch.cuda.synchronize()
+    for g, s, part in list(zip(gs, src, mg.split(ds)))[-2:]:
+        assert torch.equal(part, G.shortest_path(g, s))
