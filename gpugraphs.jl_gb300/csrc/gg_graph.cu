@@ -781,7 +781,7 @@ __global__ void __launch_bounds__(1024)
 static const int kCoopMaxDeg = 64;
 static const int kCoopLo = 1024;   // the single-CTA kernel takes smaller frontiers
 static const int kCoopThreads = 1024;
-static const double kNearFarScale = 8.0;  // near-far band width = this x the mean weight
+static const double kNearFarScale = 32.0;  // near-far band width = this x the mean weight
 
 struct CoopCtl {
   unsigned long long cnt[3];
