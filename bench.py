@@ -439,8 +439,13 @@ def run_spmv_rmat(args, scale=22):
     if layout == "window_tiles":
         kernel_label = ("k_spmv_pipe (tail rows) + k_spmv_win (column-window tiles: rows sorted "
                         "by length, x windows of 16384 relabelled columns staged in shared memory)")
+    elif G.spmv_hub_rows(A) > 0:
+        kernel_label = ("k_sell_hot32 (SELL-32 copy sorted by row length, relabelled columns) "
+                        "+ k_hubwin / k_hw_combine (the %d hub rows folded from shared-memory "
+                        "column windows)" % G.spmv_hub_rows(A))
     else:
-        kernel_label = ({"registers": "k_sell_hot32", "bulk_copy": "k_sell_tma32"}[
+        kernel_label = ({"registers": "k_sell_hot32", "bulk_copy": "k_sell_tma32",
+                         "hub_windows": "k_sell_hot32"}[
             args.sell_variant or "registers"]
             + " (SELL-32 copy sorted by row length, relabelled columns)")
     # parity of this run's own output, every row, after the timed region
@@ -677,7 +682,7 @@ def secondary_large(args, device, parity, rank):
         "n": A.n, "nnz": A.nnz(), "ms": round(m["per_step_ms"], 4), "gbs": round(m["value"], 1),
         "kernel_ms": round(m["kernel_ms"], 4), "kernel_gbs": round(m["achieved"], 1),
         "frac": round(m["frac"], 4), "peak": m["peak"], "e2e_gbs": round(m["e2e"], 1),
-        "layout": G.spmv_layout(A)}
+        "layout": G.spmv_layout(A), "hub_rows_from_windows": G.spmv_hub_rows(A)}
     del A, x, m
     torch.cuda.empty_cache()
     for kind, graph, reps, budget in (("bfs", "rmat24", 8, 40), ("sssp", "rmat24", 4, 4),
@@ -1252,7 +1257,7 @@ def main():
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the checks of this run's results against the oracle")
     ap.add_argument("--graphs", type=int, default=1000, help="graph count of --workload multigraph")
-    ap.add_argument("--sell-variant", default=None, choices=["registers", "bulk_copy"],
+    ap.add_argument("--sell-variant", default=None, choices=["registers", "bulk_copy", "hub_windows"],
                     help="SpMV workloads: kernel variant over the SELL-32 copy (default: built-in)")
     ap.add_argument("--layout", default=None, choices=["sell", "window_tiles"],
                     help="spmv workloads: run this plus-times layout instead of the built-in choice")

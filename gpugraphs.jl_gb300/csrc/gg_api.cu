@@ -208,16 +208,9 @@ static void free_derived(gg_mat* A) {
     delete A->mmplan;
     A->mmplan = nullptr;
   }
+  free_hubwin_plan(A);
   if (A->sellplan) {
-    cudaFree(A->sellplan->items);
-    cudaFree(A->sellplan->multi);
-    cudaFree(A->sellplan->partials);
-    cudaFree(A->sellplan->pitems);
-    cudaFree(A->sellplan->narrow);
-    cudaFree(A->sellplan->wide);
-    cudaFree(A->sellplan->pitems256);
-    cudaFree(A->sellplan->multi256);
-    delete A->sellplan;
+    free_sell_plan(A->sellplan);
     A->sellplan = nullptr;
   }
 }

@@ -458,6 +458,39 @@ static const int kWinCols = 16384;
 static const int kWinShift = 19;
 static const int32_t kSegWindow = 1 << 30;
 
+// Hub rows of a sorted SELL-32 copy folded from shared-memory column windows
+// (gg_spmv_hub.cu).  The first np stored rows (the longest, all above kSellChunk
+// entries) are cut into groups of at most pg rows; row i of a group is accumulator
+// slot i and belongs to warp i mod 32 of the CTA that runs the group.  Columns are
+// the frequency ranks of ColPerm, cut into windows of kHwCols ranks whose x values a
+// CTA stages in shared memory with bulk copies.  For every (group, warp, window) the
+// warp's rows with entries in that window form SELL-32 slices (lane = row, rows
+// sorted by their entry count in the window, padded with the zero slot kHwCols),
+// entries in storage order: col = rank - window * kHwCols (16 bits), val, and a
+// 16-bit accumulator slot per slice lane (0xffff = no row).  items: (first entry,
+// first slice lane, width | -(slices), widths packed 4 bits per slice) per warp in
+// (group, warp, window) order; itemptr[(group * 32 + warp) * nwin + w] is the first
+// item of window w.  A unit (group and group-warp range, first window, end window,
+// partial slot) is run by one CTA; a row's value is its slots' partials added in
+// window order.
+struct HubWinPlan {
+  bool enabled = false;
+  int64_t np = 0, nwin = 0, nunits = 0, nitems = 0, nslices = 0, nentries = 0;
+  int pg = 0, ngroups = 0;
+  uint16_t* col = nullptr;
+  float* val = nullptr;
+  uint16_t* rowid = nullptr;
+  int4* items = nullptr;
+  int32_t* itemptr = nullptr;
+  int4* units = nullptr;         // grouped by CTA: CTA b runs units[cptr[b] .. cptr[b + 1])
+  int32_t* cptr = nullptr;
+  int grid = 0;
+  int32_t* gptr = nullptr;       // partial slots of group g: gptr[g] .. gptr[g + 1] - 1
+  float* partials = nullptr;     // nunits x pg
+  SellPlan* rest = nullptr;      // SELL-32 work items of the stored rows >= np
+};
+static const int kHwCols = 8192;
+
 static const int kBlockNnz = 256;
 static const int kShortRow = 32;
 static const int kBlockRows = 256;
@@ -537,6 +570,7 @@ struct gg_mat {
   gg::MMPlan* mmplan = nullptr;
   gg::HubPlan* hubplan = nullptr;
   gg::WinPlan* winplan = nullptr;
+  gg::HubWinPlan* hubwin = nullptr;  // SELL-32 copies: hub rows from column windows
   gg::SpvPlan* spv = nullptr;
   gg_mat* sell_copy = nullptr;  // CSR handles: SELL-32 copy (rows sorted by length) for plus-times
   gg_mat* tr_copy = nullptr;    // CSR handles: CSR storage of the transpose (gg_spmv_t)
@@ -548,7 +582,9 @@ struct gg_mat {
   int block_rows = 0;
   int mm_cpl = 0;
   // SELL-32 plus-times kernel: 0 = register loads (k_sell_hot32), 1 = matrix stream
-  // staged by bulk copies (k_sell_tma32)
+  // staged by bulk copies (k_sell_tma32), 2 = register loads with the hub rows folded
+  // from shared-memory column windows where the hub groups are dense enough
+  // (gg_spmv_hub.cu)
   int sell_variant = 0;
   int hot_cols = 0;  // x values staged in shared memory by the register kernels (0: 32768)
   int last_layout = 0;  // layout of the last plus-times Float32 SpMV (gg_spmv_layout)
@@ -571,6 +607,11 @@ int launch_pipe_f32(gg_ctx* ctx, gg_mat* A, const float* nz, const float* x, flo
                     const int32_t* colval, bool trace_main);  // gg_spmv.cu
 int build_win_plan(gg_ctx* ctx, gg_mat* A);  // gg_spmv_win.cu
 int launch_spmv_win(gg_ctx* ctx, gg_mat* A, const float* x, float* y);
+int build_sell_plan_from(gg_ctx* ctx, const gg_mat* A, int64_t s0, SellPlan** out);  // gg_spmv.cu
+void free_sell_plan(SellPlan* P);
+int build_hubwin_plan(gg_ctx* ctx, gg_mat* S);  // gg_spmv_hub.cu
+int launch_hubwin(gg_ctx* ctx, gg_mat* S, const float* xr, float* y);
+void free_hubwin_plan(gg_mat* A);
 void free_win_plan(gg_mat* A);
 void free_spv_plan(gg_mat* A);  // gg_spmspv.cu
 // out[0..n] = base + exclusive prefix sums of cnt (gg_graph.cu; synchronises the stream)

@@ -583,8 +583,27 @@ __global__ void __launch_bounds__(kHotThreads, 1)
   }
 }
 
+void free_sell_plan(SellPlan* P) {
+  if (!P) return;
+  cudaFree(P->items);
+  cudaFree(P->multi);
+  cudaFree(P->partials);
+  cudaFree(P->pitems);
+  cudaFree(P->narrow);
+  cudaFree(P->wide);
+  cudaFree(P->pitems256);
+  cudaFree(P->multi256);
+  delete P;
+}
+
 int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
   if (A->sellplan) return GG_OK;
+  return build_sell_plan_from(ctx, A, 0, &A->sellplan);
+}
+
+// work items of the slices s0, s0 + 1, ... (s0 > 0: the rows before slice s0 are
+// computed elsewhere, e.g. the hub rows of gg_spmv_hub.cu)
+int build_sell_plan_from(gg_ctx* ctx, const gg_mat* A, int64_t s0, SellPlan** out) {
   const int64_t ns = A->nslices, C = A->slice_size;
   std::vector<int32_t> sp(ns + 1);
   GG_CUDA(cudaMemcpyAsync(sp.data(), A->slice_ptr, (ns + 1) * sizeof(int32_t),
@@ -603,7 +622,7 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
     g_count = 0;
     g_widths = 0;
   };
-  for (int64_t s = 0; s < ns; ++s) {
+  for (int64_t s = s0; s < ns; ++s) {
     const int64_t L = C > 0 ? ((int64_t)sp[s + 1] - sp[s]) / C : 0;
     if (C == 32 && L <= kNarrowCols) {
       if (g_count == 8 || g_cols + L > kNarrowCols) flush_group();
@@ -660,16 +679,10 @@ int build_sell_plan(gg_ctx* ctx, gg_mat* A) {
                         ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
-    cudaFree(P->items);
-    cudaFree(P->multi);
-    cudaFree(P->partials);
-    cudaFree(P->pitems);
-    cudaFree(P->narrow);
-    cudaFree(P->wide);
-    delete P;
+    free_sell_plan(P);
     return cuda_error(e, "SELL analysis");
   }
-  A->sellplan = P;
+  *out = P;
   return GG_OK;
 }
 
@@ -919,7 +932,12 @@ static int build_colperm(gg_ctx* ctx, gg_mat* A) {
   e = cudaMemcpyAsync(cnt, rank.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaMalloc((void**)&P->colval_r, (len > 0 ? len : 1) * sizeof(int32_t));
   if (e == cudaSuccess) e = cudaMalloc((void**)&P->inv, n * sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&P->xr, n * sizeof(float));
+  // xr padded with zeros to whole column windows (the bulk copies of gg_spmv_hub.cu
+  // read complete windows)
+  const int64_t npad = (n + kHwCols - 1) / kHwCols * kHwCols;
+  if (e == cudaSuccess) e = cudaMalloc((void**)&P->xr, npad * sizeof(float));
+  if (e == cudaSuccess && npad > n)
+    e = cudaMemsetAsync(P->xr + n, 0, (npad - n) * sizeof(float), ctx->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(P->inv, inv.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) {
@@ -1112,8 +1130,16 @@ __global__ void __launch_bounds__(kHotThreads, 1)
 static int launch_sell_hot(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32& sr,
                            const int32_t* colval) {
   GG_CHECK(build_sell_plan(ctx, A));
-  SellPlan* P = A->sellplan;
   const int64_t C = A->slice_size;
+  // sell_variant 2 on a SELL-32 layout: the hub rows from shared-memory column windows
+  // (gg_spmv_hub.cu) when the analysis found dense enough hub groups; the SELL-32
+  // kernel then runs the other rows only
+  bool hub = false;
+  if (C == 32 && A->sell_variant == 2) {
+    GG_CHECK(build_hubwin_plan(ctx, A));
+    hub = A->hubwin->enabled;
+  }
+  SellPlan* P = hub ? A->hubwin->rest : A->sellplan;
   const int hot_cap = A->hot_cols > 0 ? (A->hot_cols < kHotColsMax ? A->hot_cols : kHotColsMax)
                                       : kHotCols;
   const int hot = (int)std::min<int64_t>(A->n, hot_cap);
@@ -1127,18 +1153,19 @@ static int launch_sell_hot(gg_ctx* ctx, gg_mat* A, const SRPlusTimesF32& sr,
   }
   if (P->nitems > 0 && C == 32 && A->sell_variant == 1) {
     GG_CHECK(launch_sell_tma(ctx, A, sr.nz, sr.x, sr.y, colval));  // brackets its own kernel
-  } else if (P->nitems > 0) {
+  } else if (P->nitems > 0 || hub) {
     const int tr = trace_main_begin(ctx);
-    if (C == 32)
+    if (C == 32 && P->npitems > 0)
       k_sell_hot32<<<ctx->num_sms, kHotThreads, hot * sizeof(float), ctx->stream>>>(
           sr.nz, sr.x, sr.y, colval, A->sigma > 1 ? A->perm : nullptr, A->m, P->pitems, P->npitems,
           static_cast<float*>(P->partials), hot);
-    else
+    else if (C != 32)
       k_sell_hot<<<ctx->num_sms, kHotThreads, hot * sizeof(float), ctx->stream>>>(
           sr.nz, sr.x, sr.y, A->slice_ptr, colval, A->sigma > 1 ? A->perm : nullptr, C, A->m,
           P->items, P->nitems, static_cast<float*>(P->partials), hot);
+    if (hub) GG_CHECK(launch_hubwin(ctx, A, sr.x, sr.y));  // counts its own launches
     trace_main_end(ctx, tr);
-    trace_count(ctx, 1);
+    trace_count(ctx, P->npitems > 0 || C != 32 ? 1 : 0);
   }
   // SELL-32: narrow chunked slices a thread per row, the wide ones a warp per row
   const bool split = C == 32;

@@ -167,10 +167,11 @@ static int tune_spmv(gg_ctx* ctx, gg_mat* A, gg_tune_result* out) {
         A->tuned_spmv = 2;
         bool keep = false;
         // kernels over the copy: register loads with 32768 or 16384 hot x values in
-        // shared memory, or the bulk-copy staged kernel (SELL-32 only)
-        const int nvar = C == 32 ? 3 : 2;
+        // shared memory, the bulk-copy staged kernel and register loads with the hub
+        // rows from column windows (SELL-32 only)
+        const int nvar = C == 32 ? 4 : 2;
         for (int vi = 0; vi < nvar && rc == GG_OK; ++vi) {
-          const int variant = vi == 2 ? 1 : 0;
+          const int variant = vi == 2 ? 1 : (vi == 3 ? 2 : 0);
           const int hc = vi == 1 ? 16384 : 32768;
           S->sell_variant = variant;
           S->hot_cols = hc;
@@ -341,7 +342,7 @@ extern "C" int gg_tune_apply(gg_ctx* ctx, gg_mat* A, const gg_tune_result* choic
     return set_error(GG_ERR_ARGUMENT, "spmv_kernel must be 0, 1, 2 or 3");
   }
   if (cpl) A->mm_cpl = cpl;
-  if (choice->sell_variant == 0 || choice->sell_variant == 1) {
+  if (choice->sell_variant >= 0 && choice->sell_variant <= 2) {
     A->sell_variant = choice->sell_variant;
     if (A->sell_copy) A->sell_copy->sell_variant = choice->sell_variant;
   }

@@ -22,13 +22,13 @@ from .ops import (gpu_spmm_, gpu_spmspv, gpu_spmspv_, gpu_spmv_, gpu_spmv_rows_,
                   synchronize)
 from .storage import (AbstractSparseGPUMatrix, SparseGPUMatrixCSC, SparseGPUMatrixCSR,
                       SparseGPUMatrixSELL, sprand_gpu)
-from .tuning import autotune, spmv_layout
+from .tuning import autotune, spmv_layout, spmv_hub_rows
 from .vectors import SparseGPUVector
 
 __all__ = [
     "AbstractSparseGPUMatrix", "SparseGPUMatrixCSR", "SparseGPUMatrixSELL", "gpu_spmv_",
     "gpu_spmm_", "SparseGPUMatrixCSC", "SparseGPUVector", "gpu_spmspv_", "gpu_spmspv", "gpu_spmv_rows_",
-    "gpu_ewise_", "gpu_apply_", "gpu_reduce", "RBData", "read_rb", "read_mtx", "read_edgelist", "sprand_gpu", "autotune", "spmv_layout", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
+    "gpu_ewise_", "gpu_apply_", "gpu_reduce", "RBData", "read_rb", "read_mtx", "read_edgelist", "sprand_gpu", "autotune", "spmv_layout", "spmv_hub_rows", "bfs_distances", "bfs_distances_", "bfs_distances_batch", "bfs_parents",
     "bfs_parents_", "shortest_path", "shortest_path_", "monoid_neutral", "monoid_absorb", "synchronize",
     "set_wait_limit",
     "GPUGraphs_add", "GPUGraphs_safe_add", "GPUGraphs_mul", "GPUGraphs_second",

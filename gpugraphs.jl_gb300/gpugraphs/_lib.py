@@ -67,13 +67,15 @@ SIGNATURES = {
     "gg_tune": [P, P, I64, P],
     "gg_tune_apply": [P, P, P],
     "gg_spmv_layout": [P],
+    "gg_spmv_hub_rows": [P],
     "gg_bfs_levels_noalloc": [P, P, P, I, I64, I64, I64, P, P, PI64],
     "gg_gen_rmat_edges": [P, I, I64, D, D, D, U64, I, P, P, P],
     "gg_gen_er_edges": [P, I64, I64, U64, I, P, P, P],
     "gg_gen_grid_edges": [P, I64, I64, U64, I, P, P, P],
     "gg_gen_uniform_f32": [P, I64, U64, P],
 }
-_RESTYPE = {"gg_last_error": ctypes.c_char_p, "gg_version": ctypes.c_char_p}
+_RESTYPE = {"gg_last_error": ctypes.c_char_p, "gg_version": ctypes.c_char_p,
+            "gg_spmv_hub_rows": ctypes.c_int64}
 
 _lock = threading.Lock()
 _lib = None

@@ -20,7 +20,10 @@ class TuneResult(ctypes.Structure):
                 ("candidates", ctypes.c_int), ("sell_variant", ctypes.c_int),
                 ("hot_cols", ctypes.c_int)]
 
-SELL_VARIANTS = ("registers", "bulk_copy")
+# SELL-32 plus-times kernels: register loads (the built-in choice), the matrix stream
+# staged by bulk copies, register loads with the hub rows folded from shared-memory
+# column windows where dense enough
+SELL_VARIANTS = ("registers", "bulk_copy", "hub_windows")
 KERNELS = {1: "csr_row_blocks", 2: "sell", 3: "window_tiles"}
 
 
@@ -95,3 +98,10 @@ def spmv_layout(A):
     """Layout the last plus-times Float32 gpu_spmv_ of A ran on: None (no such call
     yet), "csr_row_blocks", "sell" or "window_tiles"."""
     return KERNELS.get(core.lib().gg_spmv_layout(A.handle))
+
+
+def spmv_hub_rows(A):
+    """Rows of A whose plus-times Float32 gpu_spmv_ is folded from shared-memory column
+    windows (the hub rows of the sorted SELL-32 layout; 0 when none qualified or no
+    such call ran yet)."""
+    return int(core.lib().gg_spmv_hub_rows(A.handle))

@@ -506,9 +506,11 @@ typedef struct gg_tune_result {
   int mm_cols_per_lane;    /* SpMM column tile: 32 x this columns per warp pass */
   double spmm_ms;          /* median time of the chosen SpMM tile (spmm_k > 0) */
   int candidates;          /* configurations timed */
-  int sell_variant;        /* SELL-32 plus-times kernel: 0 = register loads, 1 = matrix stream
-                              staged in shared memory by bulk copies (-1 in gg_tune_apply:
-                              leave as is) */
+  int sell_variant;        /* SELL-32 plus-times kernel: 0 = register loads, 1 = matrix
+                              stream staged in shared memory by bulk copies, 2 = register
+                              loads with the hub rows folded from shared-memory column
+                              windows where dense enough (gg_spmv_hub_rows) (-1 in
+                              gg_tune_apply: leave as is) */
   int hot_cols;            /* most frequent x values staged in shared memory by the register
                               kernel (0: built-in 32768; at most 53248) */
 } gg_tune_result;
@@ -532,6 +534,15 @@ int gg_tune_apply(gg_ctx* ctx, gg_mat* A, const gg_tune_result* choice);
  * blocks, 2 = a SELL-C-sigma layout (the handle itself or a copy), 3 = column-window
  * tiles.  No reference counterpart (introspection of the layouts gg_tune chooses). */
 int gg_spmv_layout(const gg_mat* A);
+/* Rows of A whose plus-times Float32 gg_spmv is folded from shared-memory column
+ * windows (sell_variant 2 of gg_tune_apply): the hub rows (more than 128 entries,
+ * longest first) of the sorted SELL-32 layout, when its analysis (run by the first
+ * such call) found groups of them dense enough; 0 otherwise.  Those rows are summed in a fixed order (window after window,
+ * storage order inside a window), so results are identical from call to call and
+ * within rounding of the storage-order fold.  The layout costs about 6 bytes per hub
+ * entry of extra device memory beside the SELL-32 copy.  No reference counterpart
+ * (introspection of the layouts gg_tune chooses). */
+int64_t gg_spmv_hub_rows(const gg_mat* A);
 
 /* ---- seeded synthetic inputs (no reference counterpart: the reference's benchmark
  *      draws its inputs with Julia's sprand / Graphs.jl generators,

@@ -14,7 +14,7 @@ HEADER = os.path.join(ROOT, "include", "gpugraphs.h")
 
 def header_functions():
     src = open(HEADER).read()
-    return sorted(set(re.findall(r"^(?:int|const char\*)\s+(gg_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^(?:int|int64_t|const char\*)\s+(gg_\w+)\s*\(", src, re.M)))
 
 
 def header_enums():

@@ -31,7 +31,7 @@ def header_arity():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     out = {}
-    for m in re.finditer(r"^(?:int|const char\*)\s+(gg_\w+)\s*\(([^;]*?)\)\s*;", src, re.M | re.S):
+    for m in re.finditer(r"^(?:int|int64_t|const char\*)\s+(gg_\w+)\s*\(([^;]*?)\)\s*;", src, re.M | re.S):
         params = m.group(2).strip()
         out[m.group(1)] = 0 if params in ("", "void") else len(_split_top(params))
     return out

@@ -486,8 +486,13 @@ def test_spmv_plus_times_large_csr_sorted_sell_path():
     deg = np.diff(rowptr)
     first = None
     from gpugraphs import tuning
-    # register loads and bulk-copy staging: the same bits
-    for rep, variant in enumerate(["registers", "registers", "bulk_copy", "bulk_copy"]):
+    # register loads, bulk-copy staging and hub rows from column windows: the same bits
+    # for every row of <= 128 entries; long rows within rounding, and the register and
+    # bulk-copy kernels (the same chunk tree) bit for bit; every kernel gives the same
+    # bits twice
+    seen = {}
+    for variant in ["registers", "registers", "bulk_copy", "bulk_copy",
+                    "hub_windows", "hub_windows"]:
         tuning.apply(A, {"spmv_kernel": "sell", "slice_size": 32, "sigma": n,
                          "sell_variant": variant})
         y = torch.full((n,), -1.0, dtype=torch.float32, device="cuda")
@@ -496,10 +501,10 @@ def test_spmv_plus_times_large_csr_sorted_sell_path():
         exact = deg <= SELL_CHUNK
         assert (yh[exact] == yo[exact]).all()
         np.testing.assert_allclose(yh, ref, rtol=RTOL, atol=1e-6)
-        if first is None:
-            first = yh
-        else:
-            assert (yh == first).all()
+        if variant in seen:
+            assert (yh == seen[variant]).all()
+        seen[variant] = yh
+    assert (seen["bulk_copy"] == seen["registers"]).all()
 
 
 def test_spmv_long_rows_keep_the_absorb_stop():
