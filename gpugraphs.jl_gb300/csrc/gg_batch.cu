@@ -269,7 +269,7 @@ static int bs_start(gg_ctx* ctx, int64_t n, BsRun<T>& R) {
 // one round of group R, enqueued on its stream; the counters land in R.h
 template <typename T>
 static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, const HubPlan* hp,
-                    const int32_t* prow, const int32_t* pcol, BsRun<T>& R) {
+                    const int32_t* prow, const int32_t* pcol, const gg_mat* sell, BsRun<T>& R) {
   int64_t gb = (n * 32 + 255) / 256;
   if (gb > (int64_t)ctx->num_sms * 8) gb = (int64_t)ctx->num_sms * 8;
   int64_t pb = (hp->npiece * 32 + 255) / 256;
@@ -284,7 +284,9 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
   GG_CUDA(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long), R.st));
   GG_CUDA(cudaMemsetAsync(ncq_nxt, 0, sizeof(unsigned long long), R.st));
   GG_CUDA(cudaMemsetAsync(w.c[cur ^ 1], 0, (size_t)n * sizeof(unsigned), R.st));
-  R.restricted = R.nchanged * avg_deg * 4 < nnz;
+  // with the SELL-32 full rounds (about 2/3 of the vertex rounds' cost) a round is
+  // restricted to the marked vertices only while the changed ones are fewer
+  R.restricted = R.nchanged * avg_deg * (sell ? 8 : 4) < nnz;
   if (R.restricted) {
     GG_CUDA(cudaMemsetAsync(w.mark, 0, ((n + 31) / 32) * sizeof(unsigned), R.st));
     GG_CUDA(cudaMemsetAsync(w.ctr + 3, 0, sizeof(unsigned long long), R.st));
@@ -292,6 +294,17 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
                            w.vlist, w.ctr + 3, w.mhq, w.ctr + 4, w.mhoff));
     k_ms_round<T><<<(int)gcap, 256, 0, R.st>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr,
                                                w.vlist, w.ctr + 3, w.cq[cur ^ 1], ncq_nxt);
+  } else if (sell) {
+    // every vertex over the SELL-32 copy (hubs included, as chunks of their rows)
+    if constexpr (sizeof(T) == 4) {
+      const size_t smem = kMsSellWarps * sizeof(MsSellWarpSmem<T>);
+      k_ms_round_sell<T><<<ctx->num_sms * 3, kMsSellWarps * 32, smem, R.st>>>(
+          sell->colval, sell->nzval, sell->dtype, sell->perm, sell->m, sell->sellplan->pitems,
+          sell->sellplan->npitems, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, w.cq[cur ^ 1], ncq_nxt);
+      GG_CUDA(cudaGetLastError());
+      GG_CUDA(cudaMemcpyAsync(R.h, w.ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, R.st));
+      return GG_OK;
+    }
   } else {
     // every non-hub vertex, in the plan's order: the long rows first, spread over the warps
     k_ms_round<T><<<(int)gb, 256, 0, R.st>>>(n, g, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr,
@@ -318,6 +331,15 @@ static int sssp_batch_t(gg_ctx* ctx, gg_mat* A, const BatchGraph& g, const int64
   const int32_t* pcol = nullptr;
   GG_CHECK(push_view(ctx, A, &prow, &pcol));
   const HubPlan* hp = A->hubplan;
+  // full rounds over the SELL-32 copy of large CSR graphs (4-byte distances: a warp
+  // keeps 32 rows x 32 columns of minima in registers)
+  const gg_mat* sell = nullptr;
+  if constexpr (sizeof(T) == 4) {
+    GG_CHECK(pull_sell_copy(ctx, A, &sell));
+    if (sell)
+      GG_CUDA(cudaFuncSetAttribute(k_ms_round_sell<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(kMsSellWarps * sizeof(MsSellWarpSmem<T>))));
+  }
   // a hub may enter a changed queue once per piece
   const int64_t qcap = n + hp->npiece + 64;
   const int64_t nnz = (int64_t)A->nnz;
@@ -364,7 +386,7 @@ static int sssp_batch_t(gg_ctx* ctx, gg_mat* A, const BatchGraph& g, const int64
   while (active && rc == GG_OK) {
     active = false;
     for (auto& R : runs)
-      if (!R.done && rc == GG_OK) rc = bs_issue<T>(ctx, n, nnz, g, hp, prow, pcol, R);
+      if (!R.done && rc == GG_OK) rc = bs_issue<T>(ctx, n, nnz, g, hp, prow, pcol, sell, R);
     for (auto& R : runs) {
       if (R.done || rc != GG_OK) continue;
       if (cudaStreamSynchronize(R.st) != cudaSuccess) {

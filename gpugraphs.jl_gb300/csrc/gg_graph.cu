@@ -2182,6 +2182,17 @@ static int ensure_pull_sell(gg_ctx* ctx, gg_mat* A) {
   return GG_OK;
 }
 
+// The SELL-32 copy (rows sorted by length, with its work items) of the shortest-path
+// pull rounds, built on first use; nullptr for SELL handles and CSR handles of fewer
+// than 65536 rows.
+int pull_sell_copy(gg_ctx* ctx, gg_mat* A, const gg_mat** out) {
+  *out = nullptr;
+  if (A->format != GG_FMT_CSR || A->m < (1 << 16) || !A->aux) return GG_OK;
+  GG_CHECK(ensure_pull_sell(ctx, A));
+  *out = A->aux->pull_sell;
+  return GG_OK;
+}
+
 // Builds, ahead of any concurrent use, every analysis a shortest-path search of A may
 // build on first use: the out-edge view with weights, the hub plan and (large CSR
 // handles) the SELL-32 copy of the pull rounds.  The serving loop calls it when a

@@ -25,6 +25,7 @@ int graph_view(gg_ctx* ctx, gg_mat* A, const int32_t** rp, const int32_t** cv, c
 int build_hub_plan(gg_ctx* ctx, gg_mat* A, const int32_t* rowptr, int64_t n);  // gg_batch.cu
 int push_view(gg_ctx* ctx, gg_mat* A, const int32_t** prow, const int32_t** pcol);  // gg_graph.cu
 int sssp_prepare(gg_ctx* ctx, gg_mat* A);  // gg_graph.cu
+int pull_sell_copy(gg_ctx* ctx, gg_mat* A, const gg_mat** out);  // gg_graph.cu
 
 namespace {
 
@@ -534,6 +535,154 @@ template <> __device__ __forceinline__ float b_atomic_min<float>(float* p, float
 }
 template <> __device__ __forceinline__ double b_atomic_min<double>(double* p, double v) {
   return __longlong_as_double(atomicMin((long long*)p, __double_as_longlong(v)));
+}
+
+// Full round over the SELL-32 copy of the graph (4-byte distance types): a warp takes
+// one work item of the copy's plan (a chunk of up to kSellChunk entry columns of a
+// slice, or a group of narrow slices), i.e. 32 rows.  Entry columns are read 8 at a
+// time (lane = row): in-neighbours, their changed-column masks and weights, all loads
+// independent; the entries whose in-neighbour changed last round go to a per-warp
+// queue in shared memory.  The queue is then drained 16 entries at a time, lane =
+// source column: 16 rows of D (128 bytes each) in flight per warp, candidates folded
+// into the warp's 32 x 32 minima in shared memory.  The vertex-per-warp round waits on
+// one vertex's chain of loads at a time instead.  Rows are lowered in place with atomic
+// min (a long row's chunks are separate items; min is exact in any order, so the
+// fixpoint is unchanged), and a vertex enters the next changed queue once, by the warp
+// whose atomic OR first set a bit of it.
+static const int kMsSellWarps = 8;
+static const int kMsSellQ = 8 * 32;  // queue entries of one 8-column step
+static const int kMsSellBatch = 16;  // rows of D a warp reads at once
+
+template <typename T>
+struct MsSellWarpSmem {
+  T acc[32 * 32];       // row l, column q at l * 32 + q
+  int4 q[kMsSellQ];     // (in-neighbour, weight bits, changed columns, row)
+};
+
+template <typename T>
+__device__ __forceinline__ int ms_bits(T w);
+template <> __device__ __forceinline__ int ms_bits<int32_t>(int32_t w) { return w; }
+template <> __device__ __forceinline__ int ms_bits<float>(float w) { return __float_as_int(w); }
+template <typename T>
+__device__ __forceinline__ T ms_unbits(int b);
+template <> __device__ __forceinline__ int32_t ms_unbits<int32_t>(int b) { return b; }
+template <> __device__ __forceinline__ float ms_unbits<float>(int b) { return __int_as_float(b); }
+
+template <typename T>
+__device__ __forceinline__ void ms_sell_slice(const int32_t* __restrict__ colval, const void* nz,
+                                              int tv, int64_t pos0, int width, int64_t row0,
+                                              int64_t m, const int32_t* __restrict__ perm, T* D,
+                                              const unsigned* __restrict__ chg, unsigned* chg_next,
+                                              unsigned long long* count, int32_t* cq,
+                                              unsigned long long* ncq, int lane,
+                                              MsSellWarpSmem<T>& sm) {
+#pragma unroll 4
+  for (int l = 0; l < 32; ++l) sm.acc[l * 32 + lane] = Lim<T>::max();
+  for (int j0 = 0; j0 < width; j0 += 8) {
+    int32_t c[8];
+    unsigned cm[8];
+    T wv[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      c[k] = j0 + k < width ? __ldcs(colval + pos0 + (int64_t)(j0 + k) * 32 + lane) : -1;
+      wv[k] = j0 + k < width ? b_weight<T>(nz, tv, pos0 + (int64_t)(j0 + k) * 32 + lane) : T(0);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) cm[k] = c[k] > 0 ? __ldcg(chg + (c[k] - 1)) : 0u;
+    __syncwarp();  // the previous step's queue has been drained
+    int nq = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const unsigned b = __ballot_sync(kFullB, cm[k] != 0);
+      if (cm[k]) sm.q[nq + __popc(b & ((1u << lane) - 1u))] = make_int4(c[k] - 1, ms_bits<T>(wv[k]), (int)cm[k], lane);
+      nq += __popc(b);
+    }
+    __syncwarp();
+    for (int e0 = 0; e0 < nq; e0 += kMsSellBatch) {
+      T dv[kMsSellBatch];
+#pragma unroll
+      for (int t = 0; t < kMsSellBatch; ++t) {
+        dv[t] = Lim<T>::max();
+        if (e0 + t < nq) {
+          const int4 qe = sm.q[e0 + t];
+          if (((unsigned)qe.z >> lane) & 1u) dv[t] = D[(int64_t)qe.x * 32 + lane];
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < kMsSellBatch; ++t) {
+        if (e0 + t < nq) {
+          const int4 qe = sm.q[e0 + t];
+          const T cand = b_relax(ms_unbits<T>(qe.y), dv[t]);
+          T* a = sm.acc + qe.w * 32 + lane;
+          if (cand < *a) *a = cand;
+        }
+      }
+    }
+  }
+  __syncwarp();
+  // lower the rows 8 at a time: their D rows read together, the drops sent as atomic
+  // min without waiting (a column counts as dropped when the minimum is below the value
+  // read; another warp lowering it further in the meantime changed it as well), and
+  // the changed-column bookkeeping of the 8 rows done by lanes 0..7 at once
+  const int32_t vl = row0 + lane < m ? __ldg(perm + row0 + lane) - 1 : -1;
+  for (int l0 = 0; l0 < 32; l0 += 8) {
+    T best[8], cur[8];
+    int32_t v[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      v[t] = __shfl_sync(kFullB, vl, l0 + t);
+      best[t] = sm.acc[(l0 + t) * 32 + lane];
+      cur[t] = (v[t] >= 0 && best[t] != Lim<T>::max()) ? __ldcg(D + (int64_t)v[t] * 32 + lane)
+                                                        : Lim<T>::max();
+    }
+    unsigned mine = 0;
+    int32_t myv = -1;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const bool dropped = best[t] < cur[t];
+      if (dropped) b_atomic_min<T>(D + (int64_t)v[t] * 32 + lane, best[t]);
+      const unsigned b = __ballot_sync(kFullB, dropped);
+      if (lane == t) {
+        mine = b;
+        myv = v[t];
+      }
+    }
+    if (mine && myv >= 0 && atomicOr(chg_next + myv, mine) == 0u) {
+      atomicAdd(count, 1ull);
+      if (cq) cq[atomicAdd(ncq, 1ull)] = myv;
+    }
+  }
+  __syncwarp();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kMsSellWarps * 32, 3)
+    k_ms_round_sell(const int32_t* __restrict__ colval, const void* __restrict__ nz, int tv,
+                    const int32_t* __restrict__ perm, int64_t m, const int4* __restrict__ pitems,
+                    int64_t nitems, T* D, const unsigned* __restrict__ chg, unsigned* chg_next,
+                    unsigned long long* count, int32_t* cq, unsigned long long* ncq) {
+  extern __shared__ __align__(16) unsigned char ms_smem[];
+  const int lane = threadIdx.x & 31;
+  MsSellWarpSmem<T>& sm = reinterpret_cast<MsSellWarpSmem<T>*>(ms_smem)[threadIdx.x >> 5];
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int4 dn = gw < nitems ? __ldg(pitems + gw) : make_int4(0, 0, 0, 0);
+  for (int64_t it = gw; it < nitems; it += nw) {
+    const int4 d = dn;  // first position, first stored row, columns (or -slices), partial
+    if (it + nw < nitems) dn = __ldg(pitems + it + nw);
+    if (d.z < 0) {  // -d.z narrow slices, widths in 4-bit fields of d.w
+      int64_t pos = d.x;
+      for (int t = 0; t < -d.z; ++t) {
+        const int w = (int)(((uint32_t)d.w >> (4 * t)) & 15u);
+        ms_sell_slice<T>(colval, nz, tv, pos, w, (int64_t)d.y + t * 32, m, perm, D, chg, chg_next,
+                         count, cq, ncq, lane, sm);
+        pos += (int64_t)w * 32;
+      }
+    } else {
+      ms_sell_slice<T>(colval, nz, tv, d.x, d.z, d.y, m, perm, D, chg, chg_next, count, cq, ncq,
+                       lane, sm);
+    }
+  }
 }
 
 // hub pieces: one warp per piece, atomic min into the hub's 32 columns

@@ -150,3 +150,29 @@ def test_single_source_hub_pieces(dtype):
             if dtype == np.int32:
                 lv, _ = O.bfs_levels(n, rp2, cv2, nz2, s)
                 assert (host(G.bfs_distances(B, s)) == lv).all(), s
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.float32])
+def test_sssp_batch_sell_full_rounds(dtype):
+    """Graphs of at least 65536 vertices: the batched rounds that visit every vertex run
+    over the SELL-32 copy (32 rows x 32 source columns of minima per warp, hubs as row
+    chunks lowered with atomic min).  R-MAT scale 16 (Int32 1..255 or Float32 [1,10))
+    with 40 sources (two groups) and a directed graph with hubs of 6000 / 9000 in-edges,
+    every column equal to the oracle."""
+    wk = gen.W_INT_1_255 if dtype == np.int32 else gen.W_F32_1_10
+    A = gen.rmat(16, 16, seed=35, wkind=wk)
+    rp, cv, nz = csr_host(A)
+    rng = np.random.default_rng(35)
+    src = rng.integers(1, A.n + 1, 40)
+    ref, _ = O.sssp(A.n, rp, cv, nz, src)
+    got = host(G.shortest_path(A, src))
+    assert got.dtype == dtype and (got == ref).all()
+    n = 70000
+    rp, cv, nz = hub_graph(n, 44, dtype)
+    B = G.SparseGPUMatrixCSR(n, n, rp, cv, nz)
+    src = np.concatenate([[1, 2, 3], rng.integers(1, n + 1, 34)]).astype(np.int64)
+    ref, _ = O.sssp(n, rp, cv, nz, src)
+    for rep in range(2):
+        got = host(G.shortest_path(B, src))
+        assert (got == ref).all(), rep
+
