@@ -284,9 +284,9 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
   GG_CUDA(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long), R.st));
   GG_CUDA(cudaMemsetAsync(ncq_nxt, 0, sizeof(unsigned long long), R.st));
   GG_CUDA(cudaMemsetAsync(w.c[cur ^ 1], 0, (size_t)n * sizeof(unsigned), R.st));
-  // with the SELL-32 full rounds (about 2/3 of the vertex rounds' cost) a round is
+  // with the SELL-32 full rounds (about half the vertex rounds' cost) a round is
   // restricted to the marked vertices only while the changed ones are fewer
-  R.restricted = R.nchanged * avg_deg * (sell ? 8 : 4) < nnz;
+  R.restricted = R.nchanged * avg_deg * (sell ? 16 : 4) < nnz;
   if (R.restricted) {
     GG_CUDA(cudaMemsetAsync(w.mark, 0, ((n + 31) / 32) * sizeof(unsigned), R.st));
     GG_CUDA(cudaMemsetAsync(w.ctr + 3, 0, sizeof(unsigned long long), R.st));

@@ -255,14 +255,17 @@ __device__ __forceinline__ T b_weight(const void* nz, int tv, int64_t k) {
   return static_cast<T>(static_cast<const double*>(nz)[k]);
 }
 
-// pull over in-edges [k0, k1) of v from in-neighbours that changed last round:
-// per-lane (source column) minimum of D[u] + w.  chg[u] holds the columns of u that
-// dropped in the previous round; only those lanes read D[u], so a vertex whose
-// distances changed for few sources costs few 32-byte sectors.
+// pull over in-edges [k0, k1) of v from in-neighbours that changed last round or
+// already in this one: per-lane (source column) minimum of D[u] + w.  chg[u] holds the
+// columns of u that dropped in the previous round, chg_cur[u] those dropped so far in
+// this round (a drop made earlier in the round travels on at once, so fewer rounds
+// are needed; any order of relaxations reaches the same fixpoint); only those lanes
+// read D[u], so a vertex whose distances changed for few sources costs few 32-byte
+// sectors.
 template <typename T>
 __device__ __forceinline__ bool bs_pull(const BatchGraph& g, const T* D,
-                                        const unsigned* __restrict__ chg, int64_t k0, int64_t k1,
-                                        int lane, T& best) {
+                                        const unsigned* __restrict__ chg, const unsigned* chg_cur,
+                                        int64_t k0, int64_t k1, int lane, T& best) {
   bool any = false;
   for (int64_t kb = k0; kb < k1; kb += 32) {
     const int64_t kk = kb + lane;
@@ -271,7 +274,7 @@ __device__ __forceinline__ bool bs_pull(const BatchGraph& g, const T* D,
     T wl = T(0);
     if (kk < k1) {
       const int32_t c = __ldg(g.colval + kk) - 1;
-      cm = __ldcg(chg + c);
+      cm = __ldcg(chg + c) | __ldcg(chg_cur + c);
       if (cm) {
         u = c;
         wl = b_weight<T>(g.nz, g.tv, kk);
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(256)
       const int64_t k0 = __shfl_sync(kFullB, k0j, j), k1 = __shfl_sync(kFullB, k1j, j);
       if (k1 - k0 > kHubDegB) continue;
       T best = Lim<T>::max();
-      const bool any = bs_pull<T>(g, D, chg, k0, k1, lane, best);
+      const bool any = bs_pull<T>(g, D, chg, chg_next, k0, k1, lane, best);
       bool dropped = false;
       if (any) {
         T* dv = D + v * 32 + lane;
@@ -542,16 +545,17 @@ template <> __device__ __forceinline__ double b_atomic_min<double>(double* p, do
 // slice, or a group of narrow slices), i.e. 32 rows.  Entry columns are read 8 at a
 // time (lane = row): in-neighbours, their changed-column masks and weights, all loads
 // independent; the entries whose in-neighbour changed last round go to a per-warp
-// queue in shared memory.  The queue is then drained 16 entries at a time, lane =
-// source column: 16 rows of D (128 bytes each) in flight per warp, candidates folded
-// into the warp's 32 x 32 minima in shared memory.  The vertex-per-warp round waits on
+// queue in shared memory.  The queue is then drained 16 entries at a time, 4 entries
+// per warp instruction (8 lanes per entry, 4 source columns per lane, 16-byte loads of
+// D): 16 rows of D in flight per warp, candidates folded with shared-memory atomic min
+// into the warp's 32 x 32 minima.  The vertex-per-warp round waits on
 // one vertex's chain of loads at a time instead.  Rows are lowered in place with atomic
 // min (a long row's chunks are separate items; min is exact in any order, so the
 // fixpoint is unchanged), and a vertex enters the next changed queue once, by the warp
 // whose atomic OR first set a bit of it.
 static const int kMsSellWarps = 8;
 static const int kMsSellQ = 8 * 32;  // queue entries of one 8-column step
-static const int kMsSellBatch = 16;  // rows of D a warp reads at once
+static const int kMsSellBatch = 16;  // queue entries a warp drains per step (4 at once)
 
 template <typename T>
 struct MsSellWarpSmem {
@@ -588,7 +592,8 @@ __device__ __forceinline__ void ms_sell_slice(const int32_t* __restrict__ colval
       wv[k] = j0 + k < width ? b_weight<T>(nz, tv, pos0 + (int64_t)(j0 + k) * 32 + lane) : T(0);
     }
 #pragma unroll
-    for (int k = 0; k < 8; ++k) cm[k] = c[k] > 0 ? __ldcg(chg + (c[k] - 1)) : 0u;
+    for (int k = 0; k < 8; ++k)
+      cm[k] = c[k] > 0 ? (__ldcg(chg + (c[k] - 1)) | __ldcg(chg_next + (c[k] - 1))) : 0u;
     __syncwarp();  // the previous step's queue has been drained
     int nq = 0;
 #pragma unroll
@@ -598,23 +603,43 @@ __device__ __forceinline__ void ms_sell_slice(const int32_t* __restrict__ colval
       nq += __popc(b);
     }
     __syncwarp();
+    // 4 queue entries per warp step: lanes 8e .. 8e + 7 take entry e, 4 source columns
+    // each (16-byte loads of D); kMsSellBatch / 4 steps' loads in flight.  Two entries
+    // of one step may share a row, so the minima are folded with shared-memory atomic
+    // min (distances are non-negative: floats order like their bit patterns).
+    const int es = lane >> 3, cq4 = (lane & 7) * 4;
     for (int e0 = 0; e0 < nq; e0 += kMsSellBatch) {
-      T dv[kMsSellBatch];
+      T dv[kMsSellBatch / 4][4];
+      int4 qe[kMsSellBatch / 4];
 #pragma unroll
-      for (int t = 0; t < kMsSellBatch; ++t) {
-        dv[t] = Lim<T>::max();
-        if (e0 + t < nq) {
-          const int4 qe = sm.q[e0 + t];
-          if (((unsigned)qe.z >> lane) & 1u) dv[t] = D[(int64_t)qe.x * 32 + lane];
+      for (int b = 0; b < kMsSellBatch / 4; ++b) {
+        const int e = e0 + b * 4 + es;
+        qe[b] = e < nq ? sm.q[e] : make_int4(0, 0, 0, 0);
+        const unsigned bits = ((unsigned)qe[b].z >> cq4) & 15u;
+        dv[b][0] = dv[b][1] = dv[b][2] = dv[b][3] = Lim<T>::max();
+        if (bits) {
+          const T* row = D + (int64_t)qe[b].x * 32 + cq4;
+          if constexpr (sizeof(T) == 4) {
+            const int4 r4 = __ldcg(reinterpret_cast<const int4*>(row));
+            if (bits & 1u) dv[b][0] = ms_unbits<T>(r4.x);
+            if (bits & 2u) dv[b][1] = ms_unbits<T>(r4.y);
+            if (bits & 4u) dv[b][2] = ms_unbits<T>(r4.z);
+            if (bits & 8u) dv[b][3] = ms_unbits<T>(r4.w);
+          }
         }
       }
 #pragma unroll
-      for (int t = 0; t < kMsSellBatch; ++t) {
-        if (e0 + t < nq) {
-          const int4 qe = sm.q[e0 + t];
-          const T cand = b_relax(ms_unbits<T>(qe.y), dv[t]);
-          T* a = sm.acc + qe.w * 32 + lane;
-          if (cand < *a) *a = cand;
+      for (int b = 0; b < kMsSellBatch / 4; ++b) {
+        if (e0 + b * 4 + es < nq) {
+          const T w = ms_unbits<T>(qe[b].y);
+          int* a = reinterpret_cast<int*>(sm.acc + qe[b].w * 32 + cq4);
+          const int4 cur = *reinterpret_cast<const int4*>(a);  // may be stale: atomics decide
+          const int cv[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int cb = ms_bits<T>(b_relax(w, dv[b][k]));
+            if (cb < cv[k]) atomicMin(a + k, cb);
+          }
         }
       }
     }
@@ -701,7 +726,7 @@ __global__ void __launch_bounds__(256)
     const int64_t v = hubs[p.x];
     if (mark && !((__ldcg(mark + (v >> 5)) >> (v & 31)) & 1u)) continue;
     T best = Lim<T>::max();
-    const bool any = bs_pull<T>(g, D, chg, p.y, p.z, lane, best);
+    const bool any = bs_pull<T>(g, D, chg, chg_next, p.y, p.z, lane, best);
     bool dropped = false;
     if (any) {
       T* dv = D + v * 32 + lane;
