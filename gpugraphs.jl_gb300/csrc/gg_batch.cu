@@ -300,7 +300,8 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
       const size_t smem = kMsSellWarps * sizeof(MsSellWarpSmem<T>);
       k_ms_round_sell<T><<<ctx->num_sms * 3, kMsSellWarps * 32, smem, R.st>>>(
           sell->colval, sell->nzval, sell->dtype, sell->perm, sell->m, sell->sellplan->pitems,
-          sell->sellplan->npitems, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, w.cq[cur ^ 1], ncq_nxt);
+          sell->sellplan->npitems, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr, w.cq[cur ^ 1],
+          ncq_nxt);
       GG_CUDA(cudaGetLastError());
       GG_CUDA(cudaMemcpyAsync(R.h, w.ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, R.st));
       return GG_OK;

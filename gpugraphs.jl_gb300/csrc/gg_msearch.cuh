@@ -579,7 +579,7 @@ __device__ __forceinline__ void ms_sell_slice(const int32_t* __restrict__ colval
                                               const unsigned* __restrict__ chg, unsigned* chg_next,
                                               unsigned long long* count, int32_t* cq,
                                               unsigned long long* ncq, int lane,
-                                              MsSellWarpSmem<T>& sm) {
+                                              MsSellWarpSmem<T>& sm, unsigned& dropped_cols) {
 #pragma unroll 4
   for (int l = 0; l < 32; ++l) sm.acc[l * 32 + lane] = Lim<T>::max();
   for (int j0 = 0; j0 < width; j0 += 8) {
@@ -667,6 +667,7 @@ __device__ __forceinline__ void ms_sell_slice(const int32_t* __restrict__ colval
       const bool dropped = best[t] < cur[t];
       if (dropped) b_atomic_min<T>(D + (int64_t)v[t] * 32 + lane, best[t]);
       const unsigned b = __ballot_sync(kFullB, dropped);
+      dropped_cols |= b;
       if (lane == t) {
         mine = b;
         myv = v[t];
@@ -685,8 +686,10 @@ __global__ void __launch_bounds__(kMsSellWarps * 32, 3)
     k_ms_round_sell(const int32_t* __restrict__ colval, const void* __restrict__ nz, int tv,
                     const int32_t* __restrict__ perm, int64_t m, const int4* __restrict__ pitems,
                     int64_t nitems, T* D, const unsigned* __restrict__ chg, unsigned* chg_next,
-                    unsigned long long* count, int32_t* cq, unsigned long long* ncq) {
+                    unsigned long long* count, unsigned* drop, int32_t* cq,
+                    unsigned long long* ncq) {
   extern __shared__ __align__(16) unsigned char ms_smem[];
+  unsigned dropped_cols = 0;  // source columns that dropped anywhere (drop, when given)
   const int lane = threadIdx.x & 31;
   MsSellWarpSmem<T>& sm = reinterpret_cast<MsSellWarpSmem<T>*>(ms_smem)[threadIdx.x >> 5];
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -700,14 +703,15 @@ __global__ void __launch_bounds__(kMsSellWarps * 32, 3)
       for (int t = 0; t < -d.z; ++t) {
         const int w = (int)(((uint32_t)d.w >> (4 * t)) & 15u);
         ms_sell_slice<T>(colval, nz, tv, pos, w, (int64_t)d.y + t * 32, m, perm, D, chg, chg_next,
-                         count, cq, ncq, lane, sm);
+                         count, cq, ncq, lane, sm, dropped_cols);
         pos += (int64_t)w * 32;
       }
     } else {
       ms_sell_slice<T>(colval, nz, tv, d.x, d.z, d.y, m, perm, D, chg, chg_next, count, cq, ncq,
-                       lane, sm);
+                       lane, sm, dropped_cols);
     }
   }
+  if (drop && lane == 0 && dropped_cols) atomicOr(drop, dropped_cols);
 }
 
 // hub pieces: one warp per piece, atomic min into the hub's 32 columns

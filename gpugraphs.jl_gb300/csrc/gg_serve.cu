@@ -452,9 +452,17 @@ static int exec_admit(gg_server* S, int gi, Executor& E, std::vector<Request>& w
   return k;
 }
 
+// shared memory of the SELL-32 full rounds (more than the default 48 KB per CTA)
+template <typename T>
+static int sell_round_attr() {
+  GG_CUDA(cudaFuncSetAttribute(k_ms_round_sell<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(kMsSellWarps * sizeof(MsSellWarpSmem<T>))));
+  return GG_OK;
+}
+
 template <typename T>
 static void ss_round(gg_server* S, Executor& E, const SrvGraph& sg, const HubPlan* hp,
-                     int64_t nnz) {
+                     int64_t nnz, const gg_mat* sell) {
   cudaStream_t st = E.ectx.stream;
   const int64_t n = sg.n;
   T* D = static_cast<T*>(E.D);
@@ -464,7 +472,7 @@ static void ss_round(gg_server* S, Executor& E, const SrvGraph& sg, const HubPla
   cudaMemsetAsync(ncq_nxt, 0, sizeof(unsigned long long), st);
   const int64_t avg_deg = n > 0 ? (nnz + n - 1) / n : 1;
   // few changed vertices: visit only their out-neighbours (same fixpoint)
-  const bool restricted = E.nchanged * avg_deg * 4 < nnz;
+  const bool restricted = E.nchanged * avg_deg * (sell ? 16 : 4) < nnz;
   if (restricted) {
     cudaMemsetAsync(E.mark, 0, ((n + 31) / 32) * sizeof(unsigned), st);
     cudaMemsetAsync(E.d_cnt + 3, 0, sizeof(unsigned long long), st);
@@ -473,6 +481,17 @@ static void ss_round(gg_server* S, Executor& E, const SrvGraph& sg, const HubPla
     k_ms_round<T><<<grid_s(S, n * 32), 256, 0, st>>>(n, sg.g, D, E.c0, E.c1, E.d_cnt, E.d_amask,
                                                       E.vlist, E.d_cnt + 3, E.cq[cur ^ 1], ncq_nxt);
   } else {
+    if constexpr (sizeof(T) == 4) {
+      if (sell) {
+        // every vertex over the graph's SELL-32 copy (hubs as chunks of their rows), as
+        // the batched rounds do
+        k_ms_round_sell<T><<<S->own.num_sms * 3, kMsSellWarps * 32,
+                             kMsSellWarps * sizeof(MsSellWarpSmem<T>), st>>>(
+            sell->colval, sell->nzval, sell->dtype, sell->perm, sell->m, sell->sellplan->pitems,
+            sell->sellplan->npitems, D, E.c0, E.c1, E.d_cnt, E.d_amask, E.cq[cur ^ 1], ncq_nxt);
+        return;
+      }
+    }
     // every non-hub vertex in the plan's order (long rows first, spread over the warps)
     k_ms_round<T><<<grid_s(S, n * 32), 256, 0, st>>>(n, sg.g, D, E.c0, E.c1, E.d_cnt, E.d_amask,
                                                       hp->order, hp->d_norder, E.cq[cur ^ 1],
@@ -514,11 +533,13 @@ static int exec_tick(gg_server* S, int gi, Executor& E) {
     GG_CUDA(cudaMemsetAsync(E.d_amask, 0, 4, st));  // dropped columns of this round
     GG_CUDA(cudaMemsetAsync(E.c1, 0, (size_t)n * sizeof(unsigned), st));
     const int64_t nnz = S->graphs[gi]->nnz;
+    const gg_mat* sell = nullptr;  // built when the graph was added (sssp_prepare)
+    GG_CHECK(pull_sell_copy(&S->own, S->graphs[gi], &sell));
     switch (E.dtype) {
-      case GG_INT32: ss_round<int32_t>(S, E, sg, hp, nnz); break;
-      case GG_INT64: ss_round<int64_t>(S, E, sg, hp, nnz); break;
-      case GG_FLOAT32: ss_round<float>(S, E, sg, hp, nnz); break;
-      default: ss_round<double>(S, E, sg, hp, nnz); break;
+      case GG_INT32: ss_round<int32_t>(S, E, sg, hp, nnz, sell); break;
+      case GG_INT64: ss_round<int64_t>(S, E, sg, hp, nnz, nullptr); break;
+      case GG_FLOAT32: ss_round<float>(S, E, sg, hp, nnz, sell); break;
+      default: ss_round<double>(S, E, sg, hp, nnz, nullptr); break;
     }
     std::swap(E.c0, E.c1);
     GG_CUDA(cudaMemcpyAsync(E.h_result, E.d_amask, 4, cudaMemcpyDeviceToHost, st));
@@ -865,6 +886,11 @@ int gg_server_add_graph(gg_server* S, const gg_mat* A_T, int* graph_id) {
     if (rc == GG_OK && nonneg && n > 0) {
       const int64_t one = 1;
       rc = sssp_prepare(&S->own, A);
+      // the full rounds of the shortest-path executors run over the SELL-32 copy
+      if (rc == GG_OK)
+        rc = sell_round_attr<int32_t>();
+      if (rc == GG_OK)
+        rc = sell_round_attr<float>();
       if (rc == GG_OK)
         rc = gg_sssp(&S->own, A, &one, 1, tmp, nullptr, A->dtype == GG_BOOL ? GG_INT32 : A->dtype,
                      n, nullptr);
