@@ -187,6 +187,12 @@ __global__ void k_bs_out(const T* D, int64_t n, int64_t S, T* dist, int64_t ld) 
 }
 
 static const int kBsStreams = 8;  // 32-source groups run at once (8 x 32 bytes of ctx->h_flags)
+// with the SELL-32 full rounds a round is restricted to the marked vertices while the
+// changed vertices times the mean degree stay below nnz / kBsSellRestrict
+#ifndef GG_BS_SELL_RESTRICT
+#define GG_BS_SELL_RESTRICT 32
+#endif
+static const int64_t kBsSellRestrict = GG_BS_SELL_RESTRICT;
 
 // Work buffers of one batched shortest-path call.  ctr: [0] vertices changed this
 // round, [1] / [2] lengths of the changed queues cq[0] / cq[1], [3] marked vertices.
@@ -286,7 +292,7 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
   GG_CUDA(cudaMemsetAsync(w.c[cur ^ 1], 0, (size_t)n * sizeof(unsigned), R.st));
   // with the SELL-32 full rounds (about half the vertex rounds' cost) a round is
   // restricted to the marked vertices only while the changed ones are fewer
-  R.restricted = R.nchanged * avg_deg * (sell ? 16 : 4) < nnz;
+  R.restricted = R.nchanged * avg_deg * (sell ? kBsSellRestrict : 4) < nnz;
   if (R.restricted) {
     GG_CUDA(cudaMemsetAsync(w.mark, 0, ((n + 31) / 32) * sizeof(unsigned), R.st));
     GG_CUDA(cudaMemsetAsync(w.ctr + 3, 0, sizeof(unsigned long long), R.st));

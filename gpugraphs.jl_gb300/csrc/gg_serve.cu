@@ -472,7 +472,7 @@ static void ss_round(gg_server* S, Executor& E, const SrvGraph& sg, const HubPla
   cudaMemsetAsync(ncq_nxt, 0, sizeof(unsigned long long), st);
   const int64_t avg_deg = n > 0 ? (nnz + n - 1) / n : 1;
   // few changed vertices: visit only their out-neighbours (same fixpoint)
-  const bool restricted = E.nchanged * avg_deg * (sell ? 16 : 4) < nnz;
+  const bool restricted = E.nchanged * avg_deg * (sell ? 32 : 4) < nnz;
   if (restricted) {
     cudaMemsetAsync(E.mark, 0, ((n + 31) / 32) * sizeof(unsigned), st);
     cudaMemsetAsync(E.d_cnt + 3, 0, sizeof(unsigned long long), st);
