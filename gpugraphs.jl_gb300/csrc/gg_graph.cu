@@ -2063,7 +2063,10 @@ __global__ void __launch_bounds__(256)
 // ---------------------------------------------------------------------------------
 static const int kPullSellThreads = 512;
 // a round pulls when the frontier's out-edges exceed nnz / kPullSellDiv
-static const int64_t kPullSellDiv = 16;
+#ifndef GG_PULL_SELL_DIV
+#define GG_PULL_SELL_DIV 16
+#endif
+static const int64_t kPullSellDiv = GG_PULL_SELL_DIV;
 
 template <typename T>
 __device__ __forceinline__ void pull_lower(int64_t srow, int64_t m, const int32_t* __restrict__ perm,

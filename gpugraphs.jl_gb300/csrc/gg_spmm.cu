@@ -256,6 +256,11 @@ __device__ __forceinline__ void fold4(float4& acc, float a, const float4& b) {
   acc.w = __fadd_rn(acc.w, __fmul_rn(a, b.w));
 }
 
+#ifndef GG_MM_SHORT_STEP
+#define GG_MM_SHORT_STEP 4
+#endif
+static const int kMMShortStep = GG_MM_SHORT_STEP;  // entries of a short row per step
+
 __global__ void __launch_bounds__(256)
     k_spmm_short_f32x4(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colval,
                        const float* __restrict__ nz, const float* __restrict__ B, int64_t ldb,
@@ -276,31 +281,31 @@ __global__ void __launch_bounds__(256)
       const int64_t j = jlo + jb + 4 * sub;
       if (jb + 4 * sub >= jn) continue;
       float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-      // 4 entries per step in storage order, the next step's words loaded ahead
-      int32_t c[4], cn[4];
-      float a[4], an[4];
+      // kMMShortStep entries per step in storage order, the next step's words loaded ahead
+      int32_t c[kMMShortStep], cn[kMMShortStep];
+      float a[kMMShortStep], an[kMMShortStep];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < kMMShortStep; ++u) {
         const bool in = k0 + u < k1;
         c[u] = in ? ld_stream_p(colval + k0 + u, pol_s) - 1 : 0;
         a[u] = in ? ld_stream_p(nz + k0 + u, pol_s) : 0.0f;
       }
-      for (int32_t k = k0; k < k1; k += 4) {
+      for (int32_t k = k0; k < k1; k += kMMShortStep) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const bool in = k + 4 + u < k1;
-          cn[u] = in ? ld_stream_p(colval + k + 4 + u, pol_s) - 1 : 0;
-          an[u] = in ? ld_stream_p(nz + k + 4 + u, pol_s) : 0.0f;
+        for (int u = 0; u < kMMShortStep; ++u) {
+          const bool in = k + kMMShortStep + u < k1;
+          cn[u] = in ? ld_stream_p(colval + k + kMMShortStep + u, pol_s) - 1 : 0;
+          an[u] = in ? ld_stream_p(nz + k + kMMShortStep + u, pol_s) : 0.0f;
         }
-        float4 b[4];
+        float4 b[kMMShortStep];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < kMMShortStep; ++u)
           b[u] = k + u < k1 ? ld_keep4(B + (int64_t)c[u] * ldb + j, pol_b) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < kMMShortStep; ++u)
           if (k + u < k1) fold4(acc, a[u], b[u]);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kMMShortStep; ++u) {
           c[u] = cn[u];
           a[u] = an[u];
         }
@@ -315,8 +320,14 @@ __global__ void __launch_bounds__(256)
 // Rows of 33..kSegMM entries and the pieces of longer rows, plus-times Float32 on
 // 16-byte aligned row-major operands: four items per warp (longest first, so the four
 // have about the same length), 8 lanes per item, each lane 4 dense columns with float4
-// loads of B; every item is folded in storage order (4 entries per step, the next
-// step's column / value words loaded while the current B rows are in flight).
+// loads of B; every item is folded in storage order (kMMStep entries per step, the
+// next step's column / value words loaded while the current B rows are in flight;
+// 4 / 8 / 16 entries per step measured 3.67 / 3.23 / 3.98 ms at R-MAT scale 22, k = 32).
+#ifndef GG_MM_STEP
+#define GG_MM_STEP 8
+#endif
+static const int kMMStep = GG_MM_STEP;  // entries of an item folded per step
+
 __global__ void __launch_bounds__(256)
     k_spmm_items_f32x4(const int32_t* __restrict__ colval, const float* __restrict__ nz,
                        const float* __restrict__ B, int64_t ldb, float* __restrict__ C, int64_t ldc,
@@ -337,30 +348,30 @@ __global__ void __launch_bounds__(256)
       if (jj >= jn) continue;
       const float* Bj = B + jlo + jj;
       float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-      int32_t c[4], cn[4];
-      float a[4], an[4];
+      int32_t c[kMMStep], cn[kMMStep];
+      float a[kMMStep], an[kMMStep];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < kMMStep; ++u) {
         const bool in = d.y + u < d.z;
         c[u] = in ? ld_stream_p(colval + d.y + u, pol_s) - 1 : 0;
         a[u] = in ? ld_stream_p(nz + d.y + u, pol_s) : 0.0f;
       }
-      for (int32_t k = d.y; k < d.z; k += 4) {
+      for (int32_t k = d.y; k < d.z; k += kMMStep) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const bool in = k + 4 + u < d.z;
-          cn[u] = in ? ld_stream_p(colval + k + 4 + u, pol_s) - 1 : 0;
-          an[u] = in ? ld_stream_p(nz + k + 4 + u, pol_s) : 0.0f;
+        for (int u = 0; u < kMMStep; ++u) {
+          const bool in = k + kMMStep + u < d.z;
+          cn[u] = in ? ld_stream_p(colval + k + kMMStep + u, pol_s) - 1 : 0;
+          an[u] = in ? ld_stream_p(nz + k + kMMStep + u, pol_s) : 0.0f;
         }
-        float4 b[4];
+        float4 b[kMMStep];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < kMMStep; ++u)
           b[u] = k + u < d.z ? ld_keep4(Bj + (int64_t)c[u] * ldb, pol_b) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < kMMStep; ++u)
           if (k + u < d.z) fold4(acc, a[u], b[u]);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kMMStep; ++u) {
           c[u] = cn[u];
           a[u] = an[u];
         }
