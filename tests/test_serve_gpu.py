@@ -86,3 +86,27 @@ def test_server_admission_waits_for_memory():
 
 
 import time  # noqa: E402
+
+
+def test_server_large_graph_shortest_paths_equal_single():
+    """Graphs of at least 65536 vertices: the shortest-path executors' rounds over every
+    vertex run on the graph's SELL-32 copy (Int32 and Float32 weights); 40 queries per
+    graph, submitted in bursts, each equal to the single-query result."""
+    gs = [gen.rmat(16, 16, seed=47, wkind=gen.W_INT_1_255),
+          gen.rmat(16, 8, seed=48, wkind=gen.W_F32_1_10)]
+    srv = Server(reserve_bytes=0)
+    ids = [srv.add_graph(A) for A in gs]
+    rng = np.random.default_rng(49)
+    reqs = []
+    for i in range(80):
+        g = i % 2
+        s = int(rng.integers(1, gs[g].n + 1))
+        reqs.append((srv.submit_sssp(ids[g], s), g, s))
+        if i % 20 == 19:
+            time.sleep(0.003)
+    done = srv.wait(timeout=120)
+    assert len(done) == len(reqs)
+    for rid, g, s in reqs:
+        assert torch.equal(done[rid][0], G.shortest_path(gs[g], s)), (g, s)
+    srv.close()
+
