@@ -205,6 +205,7 @@ static void free_derived(gg_mat* A) {
     cudaFree(A->mmplan->first);
     cudaFree(A->mmplan->rows);
     cudaFree(A->mmplan->items);
+    cudaFree(A->mmplan->short_rows);
     delete A->mmplan;
     A->mmplan = nullptr;
   }

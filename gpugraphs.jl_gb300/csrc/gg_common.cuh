@@ -373,6 +373,10 @@ struct MMPlan {
   // of 33..kSegMM entries as (row, first entry, end entry, -1), longest first
   int4* items = nullptr;
   int64_t nitems = 0;
+  // CSR: the rows of at most 32 entries (the short-row kernel's), longest first, so
+  // the four rows a warp takes have about the same length
+  int32_t* short_rows = nullptr;
+  int64_t nshort = 0;
 };
 static const int kSegMM = 256;
 

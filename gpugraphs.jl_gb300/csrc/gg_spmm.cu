@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(256)
     k_spmm_short_f32x4(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colval,
                        const float* __restrict__ nz, const float* __restrict__ B, int64_t ldb,
                        float* __restrict__ C, int64_t ldc, int64_t row_lo, int64_t nrows,
-                       int64_t jlo, int64_t jn) {
+                       int64_t jlo, int64_t jn, const int32_t* __restrict__ rows) {
   const int lane = threadIdx.x & 31;
   const int grp = lane >> 3, sub = lane & 7;
   const uint64_t pol_s = l2_evict_first(), pol_b = l2_evict_last();
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(256)
   for (int64_t base = gw * 4; base < nrows; base += nw * 4) {
     const int64_t t = base + grp;
     if (t >= nrows) continue;
-    const int64_t r = row_lo + t;
+    const int64_t r = rows ? (int64_t)__ldg(rows + t) : row_lo + t;
     const int32_t k0 = __ldg(rowptr + r) - 1, k1 = __ldg(rowptr + r + 1) - 1;
     if (k1 - k0 > kShortMM) continue;
     for (int64_t jb = 0; jb < jn; jb += 32) {
@@ -456,7 +456,7 @@ template <class SR>
 struct ShortRowsMM {
   static bool ok(const SR&, int64_t, int64_t, const void*) { return false; }
   static void launch(gg_ctx*, const SR&, const int32_t*, const int32_t*, int64_t, int64_t, int64_t,
-                     int64_t) {}
+                     int64_t, const int32_t*) {}
   static void launch_items(gg_ctx*, const SR&, const int32_t*, const MMPlan*, int64_t, int64_t,
                            int64_t, int64_t, typename SR::T*) {}
   static bool ok1(const SR&, int64_t, const void*) { return false; }
@@ -470,10 +470,13 @@ struct ShortRowsMM<SRPlusTimesF32MM> {
                          sr.ldb % 4 == 0 && sr.ldc % 4 == 0;
     return !mask && aligned && jlo % 4 == 0 && jn % 4 == 0;
   }
+  // rows: the plan's short rows longest first (every row of the matrix), or nullptr
+  // for the rows row_lo .. row_lo + nrows - 1 in order
   static void launch(gg_ctx* ctx, const SRPlusTimesF32MM& sr, const int32_t* rowptr,
-                     const int32_t* colval, int64_t row_lo, int64_t nrows, int64_t jlo, int64_t jn) {
+                     const int32_t* colval, int64_t row_lo, int64_t nrows, int64_t jlo, int64_t jn,
+                     const int32_t* rows) {
     k_spmm_short_f32x4<<<grid_mm(ctx, (nrows + 3) / 4), 256, 0, ctx->stream>>>(
-        rowptr, colval, sr.nz, sr.x, sr.ldb, sr.y, sr.ldc, row_lo, nrows, jlo, jn);
+        rowptr, colval, sr.nz, sr.x, sr.ldb, sr.y, sr.ldc, row_lo, nrows, jlo, jn, rows);
   }
   // one dense column, no mask: the thread-per-row kernels
   static bool ok1(const SRPlusTimesF32MM&, int64_t jn, const void* mask) { return !mask && jn == 1; }
@@ -508,13 +511,26 @@ static int grid_mm(gg_ctx* ctx, int64_t warps) {
 static int build_mm_plan(gg_ctx* ctx, gg_mat* A) {
   if (A->mmplan) return GG_OK;
   std::vector<int4> segs, items;
-  std::vector<int32_t> first, rows;
+  std::vector<int32_t> first, rows, short_rows;
   if (A->format == GG_FMT_CSR) {
     const int64_t m = A->m;
     std::vector<int32_t> rp(m + 1);
     GG_CUDA(cudaMemcpyAsync(rp.data(), A->rowptr, (m + 1) * sizeof(int32_t),
                             cudaMemcpyDeviceToHost, ctx->stream));
     GG_CUDA(cudaStreamSynchronize(ctx->stream));
+    {
+      std::vector<int64_t> cnt(kShortMM + 2, 0);  // rows per length, longest first
+      for (int64_t r = 0; r < m; ++r) {
+        const int64_t L = rp[r + 1] - rp[r];
+        if (L <= kShortMM) ++cnt[kShortMM - L + 1];
+      }
+      for (int i = 1; i <= kShortMM + 1; ++i) cnt[i] += cnt[i - 1];
+      short_rows.resize(cnt[kShortMM + 1]);
+      for (int64_t r = 0; r < m; ++r) {
+        const int64_t L = rp[r + 1] - rp[r];
+        if (L <= kShortMM) short_rows[cnt[kShortMM - L]++] = (int32_t)r;
+      }
+    }
     for (int64_t r = 0; r < m; ++r) {
       const int64_t k0 = rp[r] - 1, k1 = rp[r + 1] - 1;
       if (k1 - k0 > kShortMM && k1 - k0 <= kSegMM) items.push_back(make_int4((int)r, (int)k0, (int)k1, -1));
@@ -565,12 +581,15 @@ static int build_mm_plan(gg_ctx* ctx, gg_mat* A) {
   up((void**)&P->first, first.data(), first.size() * sizeof(int32_t));
   up((void**)&P->rows, rows.data(), rows.size() * sizeof(int32_t));
   up((void**)&P->items, items.data(), (size_t)P->nitems * sizeof(int4));
+  P->nshort = (int64_t)short_rows.size();
+  up((void**)&P->short_rows, short_rows.data(), short_rows.size() * sizeof(int32_t));
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     cudaFree(P->segs);
     cudaFree(P->first);
     cudaFree(P->rows);
     cudaFree(P->items);
+    cudaFree(P->short_rows);
     delete P;
     return cuda_error(e, "SpMM long-row analysis");
   }
@@ -631,7 +650,10 @@ static int launch_mm(gg_ctx* ctx, gg_mat* A, const SR& sr, int64_t k, const void
       } else if (ShortRowsMM<SR>::ok(sr, jlo, jn, mask)) {
         // Float32 fast path: short rows four per warp, the rest (medium rows and the
         // pieces of long rows) by the item kernel
-        ShortRowsMM<SR>::launch(ctx, sr, A->rowptr, A->colval, row_lo, nrows, jlo, jn);
+        // every row (no range): the short rows longest first, four of a length per warp
+        const bool all = row_lo == 0 && nrows == m;
+        ShortRowsMM<SR>::launch(ctx, sr, A->rowptr, A->colval, row_lo, all ? P->nshort : nrows, jlo,
+                                jn, all ? P->short_rows : nullptr);
         trace_count(ctx, 1);
         tr = trace_main_begin(ctx);
         if (P->nitems > 0)
