@@ -215,10 +215,22 @@ __global__ void __launch_bounds__(256)
     for (int64_t jb = 0; jb < jn; jb += 32) {
       const int64_t jj = jb + lane;
       if (jj >= jn) continue;
+      // the pieces' partials 8 at a time (a hub row has hundreds of pieces; one load
+      // at a time left its warp long after the others), folded in order up to the stop
       T acc = sr.neutral();
-      for (int32_t q = q0; q < q1; ++q) {
-        acc = sr.addv(acc, partials[(int64_t)q * jn + jj]);
-        if (sr.is_absorb(acc)) break;
+      bool stop = false;
+      for (int32_t q = q0; q < q1 && !stop; q += 8) {
+        T v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          v[u] = q + u < q1 ? partials[(int64_t)(q + u) * jn + jj] : sr.neutral();
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (q + u < q1 && !stop) {
+            acc = sr.addv(acc, v[u]);
+            stop = sr.is_absorb(acc);
+          }
+        }
       }
       sr.write_mm(r0, jlo + jj, acc);
     }
