@@ -1383,10 +1383,21 @@ __global__ void k_col1_combine(const int4* __restrict__ multi, int64_t nmulti,
     const int o = (int)(t & 31);
     const int64_t srow = (int64_t)d.x + o;
     if (srow >= m) continue;
+    // the chunks' partials 8 at a time (a hub slice has hundreds of chunks), folded in
+    // order up to the stop at +Inf
     float acc = 0.0f;
-    for (int c = 0; c < d.z; ++c) {
-      acc = __fadd_rn(acc, partials[(int64_t)(d.y + c) * 32 + o]);
-      if (acc == __int_as_float(0x7f800000)) break;
+    bool stop = false;
+    for (int c = 0; c < d.z && !stop; c += 8) {
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = c + u < d.z ? partials[(int64_t)(d.y + c + u) * 32 + o] : 0.0f;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (c + u < d.z && !stop) {
+          acc = __fadd_rn(acc, v[u]);
+          stop = acc == __int_as_float(0x7f800000);
+        }
+      }
     }
     y[perm[srow] - 1] = acc;
   }
