@@ -186,11 +186,27 @@ __global__ void k_bs_out(const T* D, int64_t n, int64_t S, T* dist, int64_t ld) 
   }
 }
 
+// out-edges of the changed vertices of a round (the work of a restricted next round's
+// marking, and a bound of its pulls): sum over cq[0, *ncq) into *out
+__global__ void k_ms_degsum(const int32_t* __restrict__ cq, const unsigned long long* ncq,
+                            const int32_t* __restrict__ prow, unsigned long long* out) {
+  const int64_t total = (int64_t)*((volatile const unsigned long long*)ncq);
+  unsigned long long s = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t v = cq[i];
+    s += (unsigned long long)(prow[v + 1] - prow[v]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
+}
+
 static const int kBsStreams = 8;  // 32-source groups run at once (8 x 32 bytes of ctx->h_flags)
 // with the SELL-32 full rounds a round is restricted to the marked vertices while the
-// changed vertices times the mean degree stay below nnz / kBsSellRestrict
+// out-edges of the changed vertices stay below nnz / kBsSellRestrict
 #ifndef GG_BS_SELL_RESTRICT
-#define GG_BS_SELL_RESTRICT 32
+#define GG_BS_SELL_RESTRICT 16
 #endif
 static const int64_t kBsSellRestrict = GG_BS_SELL_RESTRICT;
 
@@ -220,7 +236,7 @@ struct BsRun {
   cudaStream_t st = nullptr;
   unsigned long long* h = nullptr;  // pinned counters of the last round
   const int64_t* dsrc = nullptr;
-  int64_t S = 0, nchanged = 0, r = 0;
+  int64_t S = 0, nchanged = 0, mchanged = 0, r = 0;  // changed vertices, their out-edges
   T* dist = nullptr;
   int cur = 0;
   bool restricted = false, done = false;
@@ -269,6 +285,17 @@ static int bs_start(gg_ctx* ctx, int64_t n, BsRun<T>& R) {
   R.h[3] = 0;
   GG_CUDA(cudaMemcpyAsync(R.w.ctr, R.h, 4 * sizeof(unsigned long long), cudaMemcpyHostToDevice, R.st));
   R.nchanged = R.S;
+  R.mchanged = -1;  // unknown before the first round
+  return GG_OK;
+}
+
+// ctr[3] (the marked count, used inside a restricted round only) becomes the out-edge
+// count of this round's changed vertices once the round's kernels are done
+static int bs_degsum(gg_ctx* ctx, const int32_t* prow, const int32_t* cq,
+                     const unsigned long long* ncq, unsigned long long* ctr, cudaStream_t st) {
+  GG_CUDA(cudaMemsetAsync(ctr + 3, 0, sizeof(unsigned long long), st));
+  k_ms_degsum<<<ctx->num_sms * 4, 256, 0, st>>>(cq, ncq, prow, ctr + 3);
+  GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
 
@@ -292,7 +319,8 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
   GG_CUDA(cudaMemsetAsync(w.c[cur ^ 1], 0, (size_t)n * sizeof(unsigned), R.st));
   // with the SELL-32 full rounds (about half the vertex rounds' cost) a round is
   // restricted to the marked vertices only while the changed ones are fewer
-  R.restricted = R.nchanged * avg_deg * (sell ? kBsSellRestrict : 4) < nnz;
+  R.restricted = (sell && R.mchanged >= 0) ? R.mchanged * kBsSellRestrict < nnz
+                                            : R.nchanged * avg_deg * 4 < nnz;
   if (R.restricted) {
     GG_CUDA(cudaMemsetAsync(w.mark, 0, ((n + 31) / 32) * sizeof(unsigned), R.st));
     GG_CUDA(cudaMemsetAsync(w.ctr + 3, 0, sizeof(unsigned long long), R.st));
@@ -309,6 +337,7 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
           sell->sellplan->npitems, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr, w.cq[cur ^ 1],
           ncq_nxt);
       GG_CUDA(cudaGetLastError());
+      GG_CHECK(bs_degsum(ctx, prow, w.cq[cur ^ 1], ncq_nxt, w.ctr, R.st));
       GG_CUDA(cudaMemcpyAsync(R.h, w.ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, R.st));
       return GG_OK;
     }
@@ -325,6 +354,7 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
                                                  ncq_nxt);
     GG_CUDA(cudaGetLastError());
   }
+  GG_CHECK(bs_degsum(ctx, prow, w.cq[cur ^ 1], ncq_nxt, w.ctr, R.st));
   GG_CUDA(cudaMemcpyAsync(R.h, w.ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, R.st));
   return GG_OK;
 }
@@ -410,6 +440,7 @@ static int sssp_batch_t(gg_ctx* ctx, gg_mat* A, const BatchGraph& g, const int64
         rc = set_error(GG_ERR_NOT_CONVERGED, "batched shortest paths did not converge");
       } else {
         R.nchanged = (int64_t)R.h[1 + (R.cur ^ 1)];
+        R.mchanged = (int64_t)R.h[3];
         R.cur ^= 1;
       }
       if (!R.done) active = true;
