@@ -643,8 +643,21 @@ struct HwTemp {
   }
 };
 
+static int build_hubwin_plan_impl(gg_ctx* ctx, gg_mat* S);
+
+// The layout is an optional speed-up: when the device has no room for it (the build
+// sorts the hub entries with about 24 bytes of temporaries each), the SELL-32 kernel
+// runs every row instead of the call failing.
 int build_hubwin_plan(gg_ctx* ctx, gg_mat* S) {
   if (S->hubwin) return GG_OK;
+  const int rc = build_hubwin_plan_impl(ctx, S);
+  if (rc == GG_OK || rc != GG_ERR_OOM) return rc;
+  free_hubwin_plan(S);
+  S->hubwin = new HubWinPlan();  // disabled
+  return GG_OK;
+}
+
+static int build_hubwin_plan_impl(gg_ctx* ctx, gg_mat* S) {
   HubWinPlan* P = new HubWinPlan();
   S->hubwin = P;  // disabled unless completed below
   if (S->format != GG_FMT_SELL || S->slice_size != 32 || S->dtype != GG_FLOAT32 ||
