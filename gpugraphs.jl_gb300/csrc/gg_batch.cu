@@ -372,7 +372,9 @@ static int sssp_batch_t(gg_ctx* ctx, gg_mat* A, const BatchGraph& g, const int64
   // keeps 32 rows x 32 columns of minima in registers)
   const gg_mat* sell = nullptr;
   if constexpr (sizeof(T) == 4) {
-    GG_CHECK(pull_sell_copy(ctx, A, &sell));
+    const int prc = pull_sell_copy(ctx, A, &sell);
+    if (prc == GG_ERR_OOM) sell = nullptr;  // no room for the copy: vertex rounds only
+    else GG_CHECK(prc);
     if (sell)
       GG_CUDA(cudaFuncSetAttribute(k_ms_round_sell<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(kMsSellWarps * sizeof(MsSellWarpSmem<T>))));
