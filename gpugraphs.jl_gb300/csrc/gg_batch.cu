@@ -332,7 +332,7 @@ static int bs_issue(gg_ctx* ctx, int64_t n, int64_t nnz, const BatchGraph& g, co
     // every vertex over the SELL-32 copy (hubs included, as chunks of their rows)
     if constexpr (sizeof(T) == 4) {
       const size_t smem = kMsSellWarps * sizeof(MsSellWarpSmem<T>);
-      k_ms_round_sell<T><<<ctx->num_sms * 3, kMsSellWarps * 32, smem, R.st>>>(
+      k_ms_round_sell<T><<<ctx->num_sms * 4, kMsSellWarps * 32, smem, R.st>>>(
           sell->colval, sell->nzval, sell->dtype, sell->perm, sell->m, sell->sellplan->pitems,
           sell->sellplan->npitems, w.D, w.c[cur], w.c[cur ^ 1], w.ctr, nullptr, w.cq[cur ^ 1],
           ncq_nxt);

@@ -542,10 +542,11 @@ template <> __device__ __forceinline__ double b_atomic_min<double>(double* p, do
 
 // Full round over the SELL-32 copy of the graph (4-byte distance types): a warp takes
 // one work item of the copy's plan (a chunk of up to kSellChunk entry columns of a
-// slice, or a group of narrow slices), i.e. 32 rows.  Entry columns are read 8 at a
+// slice, or a group of narrow slices), i.e. 32 rows.  Entry columns are read 4 at a
 // time (lane = row): in-neighbours, their changed-column masks and weights, all loads
 // independent; the entries whose in-neighbour changed last round go to a per-warp
-// queue in shared memory.  The queue is then drained 16 entries at a time, 4 entries
+// queue in shared memory (6 KB per warp with the minima, so 4 CTAs of 8 warps fit an
+// SM: the round waits on its loads, and 32 warps hide more of that than 24 did).  The queue is then drained 16 entries at a time, 4 entries
 // per warp instruction (8 lanes per entry, 4 source columns per lane, 16-byte loads of
 // D): 16 rows of D in flight per warp, candidates folded with shared-memory atomic min
 // into the warp's 32 x 32 minima.  The vertex-per-warp round waits on
@@ -554,7 +555,7 @@ template <> __device__ __forceinline__ double b_atomic_min<double>(double* p, do
 // fixpoint is unchanged), and a vertex enters the next changed queue once, by the warp
 // whose atomic OR first set a bit of it.
 static const int kMsSellWarps = 8;
-static const int kMsSellQ = 8 * 32;  // queue entries of one 8-column step
+static const int kMsSellQ = 4 * 32;  // queue entries of one 4-column step
 static const int kMsSellBatch = 16;  // queue entries a warp drains per step (4 at once)
 
 template <typename T>
@@ -582,22 +583,22 @@ __device__ __forceinline__ void ms_sell_slice(const int32_t* __restrict__ colval
                                               MsSellWarpSmem<T>& sm, unsigned& dropped_cols) {
 #pragma unroll 4
   for (int l = 0; l < 32; ++l) sm.acc[l * 32 + lane] = Lim<T>::max();
-  for (int j0 = 0; j0 < width; j0 += 8) {
-    int32_t c[8];
-    unsigned cm[8];
-    T wv[8];
+  for (int j0 = 0; j0 < width; j0 += kMsSellQ / 32) {
+    int32_t c[kMsSellQ / 32];
+    unsigned cm[kMsSellQ / 32];
+    T wv[kMsSellQ / 32];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < kMsSellQ / 32; ++k) {
       c[k] = j0 + k < width ? __ldcs(colval + pos0 + (int64_t)(j0 + k) * 32 + lane) : -1;
       wv[k] = j0 + k < width ? b_weight<T>(nz, tv, pos0 + (int64_t)(j0 + k) * 32 + lane) : T(0);
     }
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < kMsSellQ / 32; ++k)
       cm[k] = c[k] > 0 ? (__ldcg(chg + (c[k] - 1)) | __ldcg(chg_next + (c[k] - 1))) : 0u;
     __syncwarp();  // the previous step's queue has been drained
     int nq = 0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < kMsSellQ / 32; ++k) {
       const unsigned b = __ballot_sync(kFullB, cm[k] != 0);
       if (cm[k]) sm.q[nq + __popc(b & ((1u << lane) - 1u))] = make_int4(c[k] - 1, ms_bits<T>(wv[k]), (int)cm[k], lane);
       nq += __popc(b);
@@ -682,7 +683,7 @@ __device__ __forceinline__ void ms_sell_slice(const int32_t* __restrict__ colval
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kMsSellWarps * 32, 3)
+__global__ void __launch_bounds__(kMsSellWarps * 32, 4)
     k_ms_round_sell(const int32_t* __restrict__ colval, const void* __restrict__ nz, int tv,
                     const int32_t* __restrict__ perm, int64_t m, const int4* __restrict__ pitems,
                     int64_t nitems, T* D, const unsigned* __restrict__ chg, unsigned* chg_next,

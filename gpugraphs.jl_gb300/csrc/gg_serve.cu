@@ -485,7 +485,7 @@ static void ss_round(gg_server* S, Executor& E, const SrvGraph& sg, const HubPla
       if (sell) {
         // every vertex over the graph's SELL-32 copy (hubs as chunks of their rows), as
         // the batched rounds do
-        k_ms_round_sell<T><<<S->own.num_sms * 3, kMsSellWarps * 32,
+        k_ms_round_sell<T><<<S->own.num_sms * 4, kMsSellWarps * 32,
                              kMsSellWarps * sizeof(MsSellWarpSmem<T>), st>>>(
             sell->colval, sell->nzval, sell->dtype, sell->perm, sell->m, sell->sellplan->pitems,
             sell->sellplan->npitems, D, E.c0, E.c1, E.d_cnt, E.d_amask, E.cq[cur ^ 1], ncq_nxt);
