@@ -405,6 +405,11 @@ int gg_bfs_levels_batch(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, 
  * 32 sources per pass, relaxing only from vertices that changed in the previous
  * round.  Needs non-negative weights (GG_ERR_UNSUPPORTED otherwise; gg_sssp then
  * runs the reference's Jacobi rounds).  gg_sssp routes several sources here.
+ * Memory: a 32-column distance block (n x 32 elements) per group of 32 sources, up to
+ * 8 groups at once; for CSR graphs of at least 65536 vertices with 4-byte distances
+ * the rounds over every vertex also use the SELL-32 copy of A_T that single-source
+ * gg_sssp builds (about the size of the CSR), built by the first call that needs it
+ * (when it does not fit, those rounds run vertex by vertex instead).
  */
 int gg_sssp_batch(gg_ctx* ctx, const gg_mat* A_T, const int64_t* sources, int64_t S, void* dist,
                   int dist_dtype, int64_t ld, int64_t* rounds_out);
