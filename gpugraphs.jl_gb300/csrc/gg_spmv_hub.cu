@@ -15,17 +15,23 @@
 //
 // Layout (HubWinPlan in gg_common.cuh): row i of a group is accumulator slot i in
 // shared memory and belongs to warp i mod 32, so a row is only ever updated by one
-// warp and no atomics are needed.  For every (group, warp, window) the warp's rows
-// with entries in the window form SELL-32 slices (lane = row, sorted by entry count in
-// the window, padded with a zero slot), column offsets in 16 bits.  Work items are a
-// slice, or a group of consecutive slices of at most kHwNarrow entry rows in all
-// (loaded at once, like the narrow groups of k_sell_hot32).
+// warp and no atomics are needed.  For every (group, warp, window) the warp's runs (a
+// row's entries inside the window, storage order) of more than kHwRunMin entries are
+// run items (stored contiguously, the lanes take 4 entries each with 16-byte loads);
+// the other rows form SELL-32 slices (lane = row, sorted by entry count in the window,
+// padded with a zero slot), column offsets in 16 bits.  A slice of more than
+// kHwNarrow entry rows is a quad slice (each lane's entries in groups of 4, 16-byte
+// loads); narrower slices are packed kHwNarrow entry rows per item, across up to
+// kHwBufs consecutive windows of one unit (loaded at once, like the narrow groups of
+// k_sell_hot32).  A heavy window is split over several units by group warp.
 //
-// Kernel (k_hubwin): one 1024-thread CTA per SM walks its units (group, window range,
-// partial slot).  Windows pass through a ring of kHwBufs buffers: the copy of window j
-// completes on mbarrier j mod kHwBufs, and the last warp to leave window j issues the
-// copy of window j + kHwBufs (the sequence runs on across the CTA's units).  Warps
-// never wait for one another inside a unit.  A row's fold is sequential: slot value,
+// Kernel (k_hubwin): one 1024-thread CTA per SM walks its units (group and group-warp
+// range, window range, partial slot; assigned longest first to the least loaded CTA).
+// Windows pass through a ring of kHwBufs buffers: the copy of window j completes on
+// mbarrier j mod kHwBufs, and the last warp to leave window j issues the copy of
+// window j + kHwBufs (the sequence runs on across the CTA's units).  A warp waits for
+// every window before it leaves it, so the arrivals counted for a buffer always belong
+// to one window.  Warps never wait for one another inside a unit.  A row's fold is sequential: slot value,
 // then its entries in storage order, window after window; the unit's slots go to its
 // partial, and k_hw_combine adds a row's partials in window order.  Every sum is
 // formed in one fixed order, so repeated calls give identical bits.  Every wait is
